@@ -1,0 +1,64 @@
+"""GB300-native ISPH step for the porous-beach solver Sinchanrc/Beach_Slope_Confined.
+
+The product is ``libbsc.so`` (CUDA, sm_103a) behind the C ABI of
+``include/bsc.h``.  This package builds it in-tree and binds it with ctypes;
+``Solver`` exposes the reference's step routines by their Fortran names.
+There is no CPU fallback: if the library is missing or no GPU is visible,
+the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from .binding import BscError, Context, csr_solve, setup_tank  # noqa: F401
+from .scenario import Params, SolveInfo, Timing  # noqa: F401
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libbsc.so")
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """The CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with "
+                               "`python -m beach_slope_confined_gb300.build` (nvcc, sm_103a)")
+        _lib = ctypes.CDLL(LIB_PATH)
+        _lib.bsc_measure_peaks.argtypes = [ctypes.POINTER(ctypes.c_double)] * 3
+        _lib.bsc_measure_peaks.restype = ctypes.c_int
+        _lib.bsc_default_params.argtypes = [ctypes.POINTER(Params), ctypes.c_double]
+        _lib.bsc_default_params.restype = ctypes.c_int
+    return _lib
+
+
+class Solver(Context):
+    """A ``bsc_ctx`` on the current CUDA device."""
+
+    def __init__(self, params: Params):
+        super().__init__(lib(), "bsc_", params)
+
+
+def solve_csr(params: Params, rowptr, col, val, b, x0):
+    """bsc_csr_solve: standalone BiCGSTAB/FGMRES on a host CSR matrix."""
+    return csr_solve(lib(), "bsc_", params, rowptr, col, val, b, x0)
+
+
+def default_params(dl: float) -> Params:
+    p = Params()
+    rc = lib().bsc_default_params(ctypes.byref(p), dl)
+    if rc:
+        raise BscError(rc, "default_params", "")
+    return p
+
+
+def measure_peaks():
+    """(FP64 GFLOP/s, FP32 GFLOP/s, copy GB/s) measured on the current GPU."""
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    rc = lib().bsc_measure_peaks(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    if rc:
+        raise BscError(rc, "measure_peaks", "")
+    return a.value, b.value, c.value

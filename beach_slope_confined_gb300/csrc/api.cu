@@ -1,0 +1,808 @@
+// api.cu -- the extern "C" entry points of include/bsc.h.
+//
+// Each entry point replaces one argument-less module routine of the reference
+// (main.f90:46-64).  The context owns every device buffer; all of them are
+// sized at the first bsc_upload_state (memalloc/matrixid, memory.f90:10-147)
+// and reused by later uploads of the same particle count, so a step never
+// allocates.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "bsc_internal.cuh"
+
+struct bsc_ctx : bsc::Ctx {};
+
+namespace bsc {
+
+int set_err(Ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_err(Ctx* c, cudaError_t e, const char* where) {
+    char buf[256];
+    std::snprintf(buf, sizeof buf, "%s: %s (%s)", where, cudaGetErrorName(e), cudaGetErrorString(e));
+    return set_err(c, e == cudaErrorMemoryAllocation ? BSC_E_NOMEM : BSC_E_CUDA, buf);
+}
+
+void timing_flush(Ctx* c) {
+    if (c->ev_used == 0) return;
+    cudaEventSynchronize(c->evs[2 * (c->ev_used - 1) + 1]);
+    for (int k = 0; k < c->ev_used; ++k) {
+        float f = 0.f;
+        if (cudaEventElapsedTime(&f, c->evs[2 * k], c->evs[2 * k + 1]) == cudaSuccess) {
+            c->ms[c->ev_slot[k]] += f;
+            c->calls[c->ev_slot[k]]++;
+        }
+    }
+    c->ev_used = 0;
+}
+
+static void derive_kparams(Ctx* c) {
+    const bsc_params& P = c->P;
+    KParams& K = c->K;
+    const double h = P.h;
+    K.kernel = P.kernel;
+    K.h = h;
+    K.H = 2 * h;
+    K.H2 = K.H * K.H;
+    K.lam = P.lam;
+    K.dl = P.dl;
+    K.rho0 = P.rho0;
+    K.rel_den = P.rel_den;
+    K.g = P.g;
+    K.csh = P.csh;
+    K.maxshift = P.maxshift;
+    K.free_thr = P.free_threshold;
+    K.por = P.por;
+    K.alpha = P.darcy_alpha;
+    K.beta = P.forch_beta;
+    K.d50 = P.d50;
+    K.eddy_cs = P.eddy_cs;
+    K.eddy_cv = P.eddy_cv;
+    K.eddy_ce = P.eddy_ce;
+    K.varts_ps = P.varts_ps;
+    K.bxmin = P.buffer_release_xmin;
+    K.bxmax = P.buffer_release_xmax;
+    // kernel.f90:52-53: 10/(28*3.14 h^2) and 1/(3*3.14 h^2), 28.0*3.14 and
+    // 3.0*3.14 evaluated in single precision as the reference does
+    K.hyb_A = 0.1 * (10.0 / ((double)(28.0f * 3.14f) * (h * h)));
+    K.hyb_B = (1.0 - 0.1) * (1.0 / ((double)(3.0f * 3.14f) * (h * h)));
+    K.wend_F = 35.0 / (4.0 * 3.140 * ((h * h) * (h * h)));
+    K.wend_W = 7.0 / (4 * 3.140 * (h * h));
+    K.w0 = (P.kernel == BSC_KERNEL_WENDLAND_C2) ? K.wend_W : 4.0 * K.hyb_A + 6.0 * K.hyb_B;
+    K.kmax = P.max_neighbors;
+}
+
+static uint64_t spread_bits(uint32_t v) {
+    uint64_t x = v;
+    x = (x | (x << 16)) & 0x0000FFFF0000FFFFull;
+    x = (x | (x << 8)) & 0x00FF00FF00FF00FFull;
+    x = (x | (x << 4)) & 0x0F0F0F0F0F0F0F0Full;
+    x = (x | (x << 2)) & 0x3333333333333333ull;
+    x = (x | (x << 1)) & 0x5555555555555555ull;
+    return x;
+}
+
+static void free_all(Ctx* c) {
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : c->allocs) cudaFree(p);
+    c->allocs.clear();
+    if (c->h_sc) cudaFreeHost(c->h_sc);
+    if (c->h_flag) cudaFreeHost(c->h_flag);
+    c->h_sc = nullptr;
+    c->h_flag = nullptr;
+    c->cap = 0;
+}
+
+static int alloc_state(Ctx* c, State& S, int64_t n) {
+    double** f[N_DBL_FIELDS] = {&S.x, &S.y, &S.vx, &S.vy, &S.xs, &S.ys, &S.vxs, &S.vys, &S.p, &S.rho, &S.oden,
+                                &S.mass, &S.por, &S.gradvx, &S.nut, &S.tke, &S.resist, &S.varts, &S.vel, &S.xrest,
+                                &S.vol, &S.L0, &S.L1, &S.L2, &S.L3};
+    for (int k = 0; k < N_DBL_FIELDS; ++k)
+        if (int rc = dalloc(c, f[k], n)) return rc;
+    if (int rc = dalloc(c, &S.tid, n)) return rc;
+    if (int rc = dalloc(c, &S.flags, n)) return rc;
+    return dalloc(c, &S.id, n);
+}
+
+// Krylov and reduction work shared by the PPE and the standalone solve
+static int alloc_solver_work(Ctx* c, int64_t n, bool fp64, bool fp32) {
+    const int m = c->P.solver == BSC_SOLVER_FGMRES ? std::max(1, std::min(c->P.restart, 64)) : 1;
+    c->fg_m = m;
+    int rc;
+    if ((rc = dalloc(c, &c->r, 6 * n))) return rc;  // r rh pd v s tv contiguous (csr_solve relies on it)
+    c->rh = c->r + n; c->pd = c->r + 2 * n; c->v = c->r + 3 * n; c->s = c->r + 4 * n; c->tv = c->r + 5 * n;
+    if (c->P.solver == BSC_SOLVER_FGMRES && fp64)
+        if ((rc = dalloc(c, &c->V, (int64_t)(m + 1) * n))) return rc;
+    if (fp32) {
+        if ((rc = dalloc(c, &c->xf, 8 * n))) return rc;
+        c->rf = c->xf + n; c->sf = c->xf + 2 * n; c->rhf = c->xf + 3 * n; c->pf = c->xf + 4 * n;
+        c->vf = c->xf + 5 * n; c->tf = c->xf + 6 * n; c->bf = c->xf + 7 * n;
+        if (c->P.solver == BSC_SOLVER_FGMRES)
+            if ((rc = dalloc(c, &c->Vf, (int64_t)(m + 1) * n))) return rc;
+    }
+    if ((rc = dalloc(c, &c->Hd, fg_layout_size(m)))) return rc;
+    if ((rc = dalloc(c, &c->part, (int64_t)RED_GRID * 64))) return rc;
+    if ((rc = dalloc(c, &c->sc, 1))) return rc;
+    if (!c->h_sc) BSC_CUDA(c, cudaMallocHost((void**)&c->h_sc, sizeof(Scalars)));
+    std::memset(c->h_sc, 0, sizeof(Scalars));
+    return BSC_OK;
+}
+
+static int alloc_for(Ctx* c, int64_t n) {
+    free_all(c);
+    int rc;
+    if ((rc = alloc_state(c, c->S, n)) || (rc = alloc_state(c, c->S2, n))) return rc;
+    if ((rc = dalloc(c, &c->pcell, n)) || (rc = dalloc(c, &c->pslot, n)) || (rc = dalloc(c, &c->sorted, n))) return rc;
+    const int64_t slots = ((n + 31) / 32) * 32 * (int64_t)c->K.kmax;
+    if ((rc = dalloc(c, &c->nbr, slots)) || (rc = dalloc(c, &c->cnt, n))) return rc;
+    if (c->mixed) {
+        if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->avalf, slots))) return rc;
+    } else {
+        if ((rc = dalloc(c, &c->gw, slots)) || (rc = dalloc(c, &c->aval, slots))) return rc;
+    }
+    if ((rc = dalloc(c, &c->b, n))) return rc;
+    if ((rc = alloc_solver_work(c, n, !c->mixed, c->mixed))) return rc;
+    if ((rc = dalloc(c, &c->d_flag, 4))) return rc;
+    BSC_CUDA(c, cudaMallocHost((void**)&c->h_flag, 4 * sizeof(int32_t)));
+    if ((rc = dalloc(c, &c->stepsc, 4))) return rc;
+    BSC_CUDA(c, cudaMemsetAsync(c->stepsc, 0, 4 * sizeof(double), c->stream));
+    BSC_CUDA(c, cudaMemsetAsync(c->d_flag, 0, 4 * sizeof(int32_t), c->stream));
+    c->cap = n;
+    return BSC_OK;
+}
+
+// cell grid from the bounds (or the particle extents) and its Morton ranks
+static int setup_grid(Ctx* c, const double* hx, const double* hy, int64_t n) {
+    const bsc_params& P = c->P;
+    double xmin = P.xmin, xmax = P.xmax, ymin = P.ymin, ymax = P.ymax;
+    if (!(xmax > xmin && ymax > ymin)) {
+        xmin = *std::min_element(hx, hx + n) - 4 * P.h;
+        xmax = *std::max_element(hx, hx + n) + 4 * P.h;
+        ymin = *std::min_element(hy, hy + n) - 4 * P.h;
+        ymax = *std::max_element(hy, hy + n) + 4 * P.h;
+    }
+    KParams& K = c->K;
+    K.cs = 2.0 * P.h * (1.0 + 1e-9);  // >= 2h so the 3x3 stencil holds the support
+    K.gx0 = xmin - K.cs;
+    K.gy0 = ymin - K.cs;
+    const double nxd = std::ceil((xmax - K.gx0) / K.cs) + 1, nyd = std::ceil((ymax - K.gy0) / K.cs) + 1;
+    if (!(nxd * nyd < 16.0e6)) return set_err(c, BSC_E_CAPACITY, "cell grid larger than 16M cells");
+    K.nx = (int)nxd;
+    K.ny = (int)nyd;
+    const int ncell = K.nx * K.ny;
+    if (ncell != c->ncell) {
+        int rc;
+        if ((rc = dalloc(c, &c->cell_start, ncell)) || (rc = dalloc(c, &c->cell_count, ncell)) ||
+            (rc = dalloc(c, &c->cell_rank, ncell)) || (rc = dalloc(c, &c->cell_tmp, ncell)) ||
+            (rc = dalloc(c, &c->scan_part, 4096)) || (rc = dalloc(c, &c->scell_start, ncell)) ||
+            (rc = dalloc(c, &c->scell_count, ncell)))
+            return rc;
+        c->ncell = ncell;
+    }
+    // Morton (Z-order) rank of every cell
+    std::vector<uint64_t> code(ncell);
+    std::vector<int32_t> ord(ncell), rank(ncell);
+    for (int cx = 0; cx < K.nx; ++cx)
+        for (int cy = 0; cy < K.ny; ++cy) code[cx * K.ny + cy] = spread_bits(cx) | (spread_bits(cy) << 1);
+    std::iota(ord.begin(), ord.end(), 0);
+    std::sort(ord.begin(), ord.end(), [&](int a, int b) { return code[a] < code[b]; });
+    for (int q = 0; q < ncell; ++q) rank[ord[q]] = q;
+    BSC_CUDA(c, cudaMemcpy(c->cell_rank, rank.data(), sizeof(int32_t) * ncell, cudaMemcpyHostToDevice));
+    BSC_CUDA(c, cudaMemset(c->scell_start, 0, sizeof(int32_t) * ncell));
+    BSC_CUDA(c, cudaMemset(c->scell_count, 0, sizeof(int32_t) * ncell));
+    return BSC_OK;
+}
+
+__global__ void k_derive_after_upload(int64_t n, State S) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    S.vol[i] = S.mass[i] / S.rho[i];
+    S.id[i] = (int32_t)i;
+}
+
+__global__ void k_to_id_order(int64_t n, const double* __restrict__ src, double* __restrict__ dst,
+                              const int32_t* __restrict__ id) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < n) dst[id[k]] = src[k];
+}
+
+__global__ void k_to_id_order_u8(int64_t n, const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
+                                 const int32_t* __restrict__ id) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k < n) dst[id[k]] = src[k];
+}
+
+static int check_flags(Ctx* c) {
+    BSC_CUDA(c, cudaMemcpyAsync(c->h_flag, c->d_flag, 4 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    const int f = c->h_flag[0];
+    if (f) {
+        BSC_CUDA(c, cudaMemsetAsync(c->d_flag, 0, 4 * sizeof(int32_t), c->stream));
+        if (f & 1) return set_err(c, BSC_E_CAPACITY, "a particle has more neighbours than max_neighbors");
+        if (f & 2) return set_err(c, BSC_E_NONFINITE, "non-finite particle position");
+    }
+    return BSC_OK;
+}
+
+// the integrator.f90:949-972 time-step rule, on the host
+static void dt_rule(Ctx* c, double umax, double numax) {
+    const bsc_params& P = c->P;
+    const double sig1 = P.sig1, dl = P.dl, mu = P.mu, rho = P.rho0, t = c->t;
+    double dt;
+    if (t <= 1.0)
+        dt = std::min(std::min(sig1 * dl / umax, sig1 * (dl * dl) / ((mu / rho) + numax)), 0.0010);
+    else if (t > 1.0 && t <= 2.50)
+        dt = (double)std::min(std::min((float)(sig1 * dl / umax), (float)(sig1 * (dl * dl) * rho / mu)), 0.002f);
+    else if (t > 3.0 && t <= 4.0)
+        dt = (double)std::min(std::min((float)(sig1 * dl / umax), (float)(sig1 * (dl * dl) * rho / mu)), 0.004f);
+    else
+        dt = std::min(std::min(sig1 * dl / umax, sig1 * (dl * dl) / ((mu / rho) + numax)), 0.0050);
+    if (!std::isfinite(numax)) numax = 0.0;
+    double dtsol = sig1 * (dl * dl) / (P.diffusivity + numax / P.tschmidt);
+    int solsteps = 1;
+    if (dtsol < dt) {
+        solsteps = (int)std::ceil(dt / dtsol);
+        dtsol = dt / solsteps;
+    }
+    c->dtsol = dtsol < dt ? dtsol : dt;
+    c->solsteps = solsteps;
+    c->umax = umax;
+    c->numax = numax;
+    if (P.dt_mode == BSC_DT_ADAPTIVE) c->dt = dt;
+}
+
+static int timestep_host(Ctx* c) {
+    int rc = op_timestep_reduce(c);
+    if (rc) return rc;
+    double h[2];
+    BSC_CUDA(c, cudaMemcpyAsync(h, c->stepsc, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    dt_rule(c, h[0], h[1]);
+    return BSC_OK;
+}
+
+}  // namespace bsc
+
+using namespace bsc;
+
+#define CTX_GUARD(ctx)                                  \
+    do {                                                \
+        if (!(ctx)) return BSC_E_INVALID;               \
+    } while (0)
+#define STATE_GUARD(ctx)                                                           \
+    do {                                                                           \
+        if (!(ctx)) return BSC_E_INVALID;                                          \
+        if (!(ctx)->have_state) return set_err(ctx, BSC_E_INVALID, "no state uploaded"); \
+    } while (0)
+
+extern "C" {
+
+int bsc_default_params(bsc_params* p, double dl) {
+    if (!p || !(dl > 0)) return BSC_E_INVALID;
+    std::memset(p, 0, sizeof *p);
+    const double por = 0.38;
+    p->kernel = BSC_KERNEL_HYBRID;
+    p->precision = BSC_PREC_FP64;
+    p->h = dl * 5.08 / 4.0;  // setup.f90:47 with the fluid spacing 2 prrealx/sqrt(por)
+    p->dl = dl;
+    p->lam = 0.001 * p->h * p->h;
+    p->rho0 = 1000.0;
+    p->rel_den = 1.025;
+    p->g = -9.81;
+    p->mu = 0.001;
+    p->csh = 0.5;
+    p->maxshift = 0.1;
+    p->free_threshold = 0.8 * 2.0;
+    p->por = por;
+    p->darcy_alpha = 450.0;
+    p->forch_beta = 1.75 * std::sqrt(450.0 / 150.0);
+    p->d50 = 0.001020;
+    p->eddy_cs = 0.15;
+    p->eddy_cv = 0.08;
+    p->eddy_ce = 1.0;
+    p->varts_ps = 1.0;
+    p->buffer_release_xmin = -1e30;
+    p->buffer_release_xmax = 1e30;
+    p->dt_mode = BSC_DT_ADAPTIVE;
+    p->solver = BSC_SOLVER_FGMRES;
+    p->dt = (double)0.001f;
+    p->sig1 = 0.2;
+    p->tschmidt = 1.0;
+    p->diffusivity = 1e-9;
+    p->restart = 150 > 64 ? 64 : 150;
+    p->maxit = 150;
+    p->tol_mode = BSC_TOL_REL_R0;
+    p->max_outer = 20;
+    p->tol = (double)0.001f;
+    p->inner_tol = 1e-4;
+    p->max_neighbors = 64;
+    p->reorder_every = 20;
+    return BSC_OK;
+}
+
+int bsc_create(const bsc_params* p, bsc_ctx** out) {
+    if (!p || !out) return BSC_E_INVALID;
+    *out = nullptr;
+    if (!(p->h > 0) || !(p->dl > 0) || p->max_neighbors <= 0 || p->max_neighbors > 1024 || p->maxit < 0 ||
+        !(p->tol > 0) || (p->solver != BSC_SOLVER_BICGSTAB && p->solver != BSC_SOLVER_FGMRES) ||
+        (p->precision != BSC_PREC_FP64 && p->precision != BSC_PREC_MIXED) ||
+        (p->kernel != BSC_KERNEL_HYBRID && p->kernel != BSC_KERNEL_WENDLAND_C2) || p->piston_modes < 0 ||
+        p->piston_modes > BSC_MAX_PISTON_MODES)
+        return BSC_E_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BSC_E_NOT_BUILT;
+    bsc_ctx* c = new (std::nothrow) bsc_ctx();
+    if (!c) return BSC_E_NOMEM;
+    c->P = *p;
+    c->mixed = p->precision == BSC_PREC_MIXED;
+    c->dt = p->dt;
+    derive_kparams(c);
+    cudaGetDevice(&c->device);
+    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return BSC_E_CUDA;
+    }
+    for (int k = 0; k < 2 * Ctx::EVPOOL; ++k) cudaEventCreate(&c->evs[k]);
+    *out = c;
+    return BSC_OK;
+}
+
+int bsc_destroy(bsc_ctx* c) {
+    if (!c) return BSC_OK;
+    free_all(c);
+    for (int k = 0; k < 2 * Ctx::EVPOOL; ++k)
+        if (c->evs[k]) cudaEventDestroy(c->evs[k]);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return BSC_OK;
+}
+
+const char* bsc_last_error(const bsc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int bsc_set_time(bsc_ctx* c, double t, double dt) {
+    CTX_GUARD(c);
+    if (!(dt > 0)) return set_err(c, BSC_E_INVALID, "set_time: dt must be > 0");
+    c->t = t;
+    c->dt = dt;
+    return BSC_OK;
+}
+
+int bsc_get_time(const bsc_ctx* c, double* t, double* dt) {
+    if (!c) return BSC_E_INVALID;
+    if (t) *t = c->t;
+    if (dt) *dt = c->dt;
+    return BSC_OK;
+}
+
+int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
+    CTX_GUARD(c);
+    if (!s || s->n <= 0 || s->n > (1ll << 30) || !s->x || !s->y || !s->vx || !s->vy || !s->p || !s->rho ||
+        !s->oden || !s->mass || !s->tid || !s->flags)
+        return set_err(c, BSC_E_INVALID, "upload_state: missing required field or bad n");
+    StageTimer tm(c, BSC_T_UPLOAD);
+    const int64_t n = s->n;
+    int rc;
+    if (c->cap != n) {
+        c->ncell = 0;
+        if ((rc = alloc_for(c, n))) return rc;
+    }
+    c->n = n;
+    if ((rc = setup_grid(c, s->x, s->y, n))) return rc;
+    State& S = c->S;
+    auto up = [&](double* d, const double* h, double dflt) -> int {
+        if (h) {
+            BSC_CUDA(c, cudaMemcpyAsync(d, h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        } else if (dflt == 0.0) {
+            BSC_CUDA(c, cudaMemsetAsync(d, 0, sizeof(double) * n, c->stream));
+        } else {
+            std::vector<double> tmp(n, dflt);
+            BSC_CUDA(c, cudaMemcpy(d, tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+        }
+        return BSC_OK;
+    };
+    if ((rc = up(S.x, s->x, 0)) || (rc = up(S.y, s->y, 0)) || (rc = up(S.vx, s->vx, 0)) || (rc = up(S.vy, s->vy, 0)) ||
+        (rc = up(S.xs, s->xs, 0)) || (rc = up(S.ys, s->ys, 0)) || (rc = up(S.vxs, s->vxs, 0)) ||
+        (rc = up(S.vys, s->vys, 0)) || (rc = up(S.p, s->p, 0)) || (rc = up(S.rho, s->rho, 0)) ||
+        (rc = up(S.oden, s->oden, 0)) || (rc = up(S.mass, s->mass, 0)) || (rc = up(S.por, s->porosity, 1.0)) ||
+        (rc = up(S.gradvx, s->gradvx, 0)) || (rc = up(S.nut, s->nut, 0)) || (rc = up(S.tke, s->tke, 0)) ||
+        (rc = up(S.resist, s->resist, 0)) || (rc = up(S.varts, s->varts, 0)) || (rc = up(S.vel, s->vel, 0)) ||
+        (rc = up(S.xrest, s->xrest ? s->xrest : s->x, 0)))
+        return rc;
+    if (s->L) {
+        std::vector<double> l[4];
+        for (int q = 0; q < 4; ++q) l[q].resize(n);
+        for (int64_t i = 0; i < n; ++i)
+            for (int q = 0; q < 4; ++q) l[q][i] = s->L[4 * i + q];
+        double* d[4] = {S.L0, S.L1, S.L2, S.L3};
+        for (int q = 0; q < 4; ++q) BSC_CUDA(c, cudaMemcpy(d[q], l[q].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+    } else {
+        if ((rc = up(S.L0, nullptr, 1.0)) || (rc = up(S.L1, nullptr, 0)) || (rc = up(S.L2, nullptr, 0)) ||
+            (rc = up(S.L3, nullptr, 1.0)))
+            return rc;
+    }
+    BSC_CUDA(c, cudaMemcpyAsync(S.tid, s->tid, n, cudaMemcpyHostToDevice, c->stream));
+    BSC_CUDA(c, cudaMemcpyAsync(S.flags, s->flags, n, cudaMemcpyHostToDevice, c->stream));
+    k_derive_after_upload<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, S);
+    BSC_LAUNCH(c);
+    c->have_state = true;
+    c->have_lists = c->have_csr = false;
+    c->cellshifts = 0;  // the first build gathers the state into cell order
+    if ((rc = cells_build(c, true))) return rc;
+    if (c->ns > 0 && (rc = solids_build(c))) return rc;
+    return check_flags(c);
+}
+
+int bsc_upload_porosity(bsc_ctx* c, int32_t nx, int32_t ny, double x0, double y0, double dx, double dy,
+                        const double* v) {
+    CTX_GUARD(c);
+    if (nx <= 0 || ny <= 0 || !v || !(dx > 0) || !(dy > 0)) return set_err(c, BSC_E_INVALID, "upload_porosity");
+    int rc;
+    if ((rc = dalloc(c, &c->pgrid, (int64_t)nx * ny))) return rc;
+    BSC_CUDA(c, cudaMemcpy(c->pgrid, v, sizeof(double) * nx * ny, cudaMemcpyHostToDevice));
+    c->K.pnx = nx; c->K.pny = ny; c->K.px0 = x0; c->K.py0 = y0; c->K.pdx = dx; c->K.pdy = dy;
+    c->K.pgrid = c->pgrid;
+    return BSC_OK;
+}
+
+int bsc_upload_solids(bsc_ctx* c, int64_t ns, const double* x, const double* y, const double* m,
+                      const double* rho, const double* por) {
+    CTX_GUARD(c);
+    if (ns < 0 || (ns > 0 && (!x || !y || !m || !rho))) return set_err(c, BSC_E_INVALID, "upload_solids");
+    c->ns = ns;
+    if (ns == 0) return BSC_OK;
+    int rc;
+    if ((rc = dalloc(c, &c->sx, ns)) || (rc = dalloc(c, &c->sy, ns)) || (rc = dalloc(c, &c->svol, ns)) ||
+        (rc = dalloc(c, &c->spor, ns)))
+        return rc;
+    std::vector<double> vol(ns), sp(ns);
+    const KParams& K = c->K;
+    for (int64_t k = 0; k < ns; ++k) {
+        vol[k] = m[k] / rho[k];
+        if (por) {
+            sp[k] = por[k];
+        } else if (K.pnx > 0) {
+            // same lookup as the fluid-side cap (porosity_at in pairs.cu)
+            double fx = std::floor((x[k] - K.px0) / K.pdx), fy = std::floor((y[k] - K.py0) / K.pdy);
+            bool in = fx >= 0 && fx < K.pnx && fy >= 0 && fy < K.pny;
+            std::vector<double> g;
+            sp[k] = K.por;
+            if (in) {
+                double val;
+                BSC_CUDA(c, cudaMemcpy(&val, c->pgrid + (int64_t)fy * K.pnx + (int64_t)fx, sizeof(double),
+                                       cudaMemcpyDeviceToHost));
+                sp[k] = val;
+            }
+        } else {
+            sp[k] = K.por;
+        }
+    }
+    BSC_CUDA(c, cudaMemcpy(c->sx, x, sizeof(double) * ns, cudaMemcpyHostToDevice));
+    BSC_CUDA(c, cudaMemcpy(c->sy, y, sizeof(double) * ns, cudaMemcpyHostToDevice));
+    BSC_CUDA(c, cudaMemcpy(c->svol, vol.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
+    BSC_CUDA(c, cudaMemcpy(c->spor, sp.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
+    if (c->ncell > 0) return solids_build(c);
+    return BSC_OK;
+}
+
+int bsc_download_state(bsc_ctx* c, bsc_state_view* s) {
+    STATE_GUARD(c);
+    if (!s || s->n != c->n) return set_err(c, BSC_E_INVALID, "download_state: size mismatch");
+    StageTimer tm(c, BSC_T_DOWNLOAD);
+    const int64_t n = c->n;
+    State& S = c->S;
+    double* stage = c->S2.x;  // S2 is free outside a reorder
+    const unsigned g = blocks_for(n, 256);
+    auto dn = [&](const double* src, double* host) -> int {
+        if (!host) return BSC_OK;
+        k_to_id_order<<<g, 256, 0, c->stream>>>(n, src, stage, S.id);
+        BSC_LAUNCH(c);
+        BSC_CUDA(c, cudaMemcpyAsync(host, stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+        return BSC_OK;
+    };
+    int rc;
+    if ((rc = dn(S.x, s->x)) || (rc = dn(S.y, s->y)) || (rc = dn(S.vx, s->vx)) || (rc = dn(S.vy, s->vy)) ||
+        (rc = dn(S.xs, s->xs)) || (rc = dn(S.ys, s->ys)) || (rc = dn(S.vxs, s->vxs)) || (rc = dn(S.vys, s->vys)) ||
+        (rc = dn(S.p, s->p)) || (rc = dn(S.rho, s->rho)) || (rc = dn(S.oden, s->oden)) ||
+        (rc = dn(S.mass, s->mass)) || (rc = dn(S.por, s->porosity)) || (rc = dn(S.gradvx, s->gradvx)) ||
+        (rc = dn(S.nut, s->nut)) || (rc = dn(S.tke, s->tke)) || (rc = dn(S.resist, s->resist)) ||
+        (rc = dn(S.varts, s->varts)) || (rc = dn(S.vel, s->vel)) || (rc = dn(S.xrest, s->xrest)))
+        return rc;
+    if (s->L) {
+        std::vector<double> l(n);
+        double* d[4] = {S.L0, S.L1, S.L2, S.L3};
+        for (int q = 0; q < 4; ++q) {
+            if ((rc = dn(d[q], l.data()))) return rc;
+            for (int64_t i = 0; i < n; ++i) s->L[4 * i + q] = l[i];
+        }
+    }
+    uint8_t* st8 = (uint8_t*)c->S2.y;
+    if (s->tid) {
+        k_to_id_order_u8<<<g, 256, 0, c->stream>>>(n, (const uint8_t*)S.tid, st8, S.id);
+        BSC_LAUNCH(c);
+        BSC_CUDA(c, cudaMemcpyAsync(s->tid, st8, n, cudaMemcpyDeviceToHost, c->stream));
+        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    if (s->flags) {
+        k_to_id_order_u8<<<g, 256, 0, c->stream>>>(n, S.flags, st8, S.id);
+        BSC_LAUNCH(c);
+        BSC_CUDA(c, cudaMemcpyAsync(s->flags, st8, n, cudaMemcpyDeviceToHost, c->stream));
+        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return BSC_OK;
+}
+
+#define OP(name, slot, body)                 \
+    int name(bsc_ctx* c) {                   \
+        STATE_GUARD(c);                      \
+        StageTimer tm(c, slot);              \
+        return (body);                       \
+    }
+
+OP(bsc_projection, BSC_T_PROJECTION, op_projection(c))
+OP(bsc_piston, BSC_T_PISTON, op_piston(c))
+OP(bsc_comp_pos, BSC_T_COMP_POS, op_comp_pos(c))
+OP(bsc_freesurf, BSC_T_FREESURF, (c->have_lists ? op_freesurf(c) : set_err(c, BSC_E_INVALID, "freesurf before neighbour")))
+OP(bsc_eddyvis, BSC_T_EDDYVIS, op_eddyvis(c))
+OP(bsc_int_vel, BSC_T_INT_VEL, op_int_vel(c, c->stepsc))
+OP(bsc_comp_vel, BSC_T_COMP_VEL, op_comp_vel(c))
+OP(bsc_opt2_shift, BSC_T_SHIFT, op_opt2_shift(c))
+
+int bsc_effpor(bsc_ctx* c) {
+    STATE_GUARD(c);
+    StageTimer tm(c, BSC_T_EFFPOR);
+    return op_effpor(c);
+}
+
+int bsc_cellshift(bsc_ctx* c, int32_t alt) {
+    (void)alt;  // the outflow cut-offs of cellshiftalt belong to open-boundary runs
+    STATE_GUARD(c);
+    StageTimer tm(c, BSC_T_CELLSHIFT);
+    return cells_build(c, true);
+}
+
+// resetid: the slot order of the cell list is the row numbering of the PPE
+int bsc_resetid(bsc_ctx* c) {
+    STATE_GUARD(c);
+    return BSC_OK;
+}
+
+int bsc_neighbour(bsc_ctx* c) {
+    STATE_GUARD(c);
+    int rc;
+    {
+        StageTimer tm(c, BSC_T_NEIGHBOUR);
+        rc = op_neighbour(c);
+    }
+    if (rc) return rc;
+    return check_flags(c);
+}
+
+int bsc_ppesolve(bsc_ctx* c, bsc_solve_info* out) {
+    STATE_GUARD(c);
+    int rc;
+    {
+        StageTimer tm(c, BSC_T_PPE_ASSEMBLE);
+        rc = op_ppe_assemble(c);
+    }
+    if (rc) return rc;
+    StageTimer tm(c, BSC_T_PPE_SOLVE);
+    rc = op_ppe_solve(c, out);
+    if (rc == BSC_E_NOT_CONVERGED || rc == BSC_E_BREAKDOWN) {
+        char buf[160];
+        std::snprintf(buf, sizeof buf, "ppesolve: %s after %d iterations, rel residual %.3e",
+                      rc == BSC_E_BREAKDOWN ? "breakdown" : "not converged", out ? out->iterations : -1,
+                      out ? out->rel_residual : -1.0);
+        c->err = buf;
+    }
+    return rc;
+}
+
+int bsc_timestep(bsc_ctx* c, double* dt_inout) {
+    STATE_GUARD(c);
+    StageTimer tm(c, BSC_T_TIMESTEP);
+    int rc = timestep_host(c);
+    if (rc) return rc;
+    if (dt_inout) *dt_inout = c->dt;
+    return BSC_OK;
+}
+
+int bsc_step(bsc_ctx* c, int32_t nsteps, bsc_solve_info* last) {
+    STATE_GUARD(c);
+    if (nsteps < 0) return set_err(c, BSC_E_INVALID, "step: nsteps < 0");
+    bsc_solve_info loc{};
+    bsc_solve_info* info = last ? last : &loc;
+    for (int s = 0; s < nsteps; ++s) {
+        StageTimer whole(c, BSC_T_STEP);
+        int rc;
+        c->t = c->t + c->dt;
+#define RUN(slot, expr)                  \
+    do {                                 \
+        StageTimer tm_(c, slot);         \
+        if ((rc = (expr))) return rc;    \
+    } while (0)
+        RUN(BSC_T_PISTON, op_piston(c));
+        RUN(BSC_T_PROJECTION, op_projection(c));
+        RUN(BSC_T_CELLSHIFT, cells_build(c, true));
+        RUN(BSC_T_NEIGHBOUR, op_neighbour(c));
+        RUN(BSC_T_EFFPOR, op_effpor(c));
+        RUN(BSC_T_EDDYVIS, op_eddyvis(c));
+        RUN(BSC_T_INT_VEL, op_int_vel(c, c->stepsc));
+        RUN(BSC_T_PPE_ASSEMBLE, op_ppe_assemble(c));
+        {
+            StageTimer tm_(c, BSC_T_PPE_SOLVE);
+            rc = op_ppe_solve(c, info);
+            if (rc) {
+                char buf[160];
+                std::snprintf(buf, sizeof buf, "step %d: PPE %s after %d iterations, rel residual %.3e", s,
+                              rc == BSC_E_BREAKDOWN ? "breakdown" : "not converged", info->iterations,
+                              info->rel_residual);
+                if (rc == BSC_E_NOT_CONVERGED || rc == BSC_E_BREAKDOWN) c->err = buf;
+                return rc;
+            }
+        }
+        RUN(BSC_T_COMP_VEL, op_comp_vel(c));
+        RUN(BSC_T_COMP_POS, op_comp_pos(c));
+        RUN(BSC_T_CELLSHIFT, cells_build(c, true));
+        RUN(BSC_T_NEIGHBOUR, op_neighbour(c));
+        RUN(BSC_T_FREESURF, op_freesurf(c));
+        RUN(BSC_T_EFFPOR, op_effpor(c));
+        RUN(BSC_T_SHIFT, op_opt2_shift(c));
+        if (c->P.dt_mode == BSC_DT_ADAPTIVE) {
+            RUN(BSC_T_TIMESTEP, timestep_host(c));
+        } else {
+            RUN(BSC_T_TIMESTEP, op_timestep_reduce(c));
+        }
+#undef RUN
+    }
+    int rc = check_flags(c);
+    if (c->timing) timing_flush(c);
+    return rc;
+}
+
+int bsc_get_neighbors(bsc_ctx* c, int64_t* offsets, int32_t* ids) {
+    STATE_GUARD(c);
+    if (!c->have_lists) return set_err(c, BSC_E_INVALID, "get_neighbors before neighbour");
+    if (!offsets) return set_err(c, BSC_E_INVALID, "get_neighbors: offsets required");
+    const int64_t n = c->n, kmax = c->K.kmax, slots = ((n + 31) / 32) * 32 * kmax;
+    std::vector<int32_t> cnt(n), id(n), nb;
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    BSC_CUDA(c, cudaMemcpy(cnt.data(), c->cnt, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    BSC_CUDA(c, cudaMemcpy(id.data(), c->S.id, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> slot_of(n);
+    for (int64_t k = 0; k < n; ++k) slot_of[id[k]] = k;
+    offsets[0] = 0;
+    for (int64_t q = 0; q < n; ++q) offsets[q + 1] = offsets[q] + cnt[slot_of[q]];
+    if (!ids) return BSC_OK;
+    nb.resize(slots);
+    BSC_CUDA(c, cudaMemcpy(nb.data(), c->nbr, sizeof(int32_t) * slots, cudaMemcpyDeviceToHost));
+    for (int64_t q = 0; q < n; ++q) {
+        const int64_t k = slot_of[q];
+        int32_t* dst = ids + offsets[q];
+        for (int e = 0; e < cnt[k]; ++e) dst[e] = id[nb[ell(k, e, (int)kmax)]];
+        std::sort(dst, dst + cnt[k]);
+    }
+    return BSC_OK;
+}
+
+int bsc_export_csr(bsc_ctx* c, int64_t* rowptr, int32_t* col, double* val, double* rhs) {
+    STATE_GUARD(c);
+    if (!c->have_csr) return set_err(c, BSC_E_INVALID, "export_csr before ppesolve");
+    if (!rowptr) return set_err(c, BSC_E_INVALID, "export_csr: rowptr required");
+    const int64_t n = c->n, kmax = c->K.kmax, slots = ((n + 31) / 32) * 32 * kmax;
+    std::vector<int32_t> cnt(n), id(n);
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    BSC_CUDA(c, cudaMemcpy(cnt.data(), c->cnt, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    BSC_CUDA(c, cudaMemcpy(id.data(), c->S.id, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    std::vector<int64_t> slot_of(n);
+    for (int64_t k = 0; k < n; ++k) slot_of[id[k]] = k;
+    rowptr[0] = 0;
+    for (int64_t q = 0; q < n; ++q) rowptr[q + 1] = rowptr[q] + cnt[slot_of[q]] + 1;
+    if (rhs) {
+        std::vector<double> b(n);
+        BSC_CUDA(c, cudaMemcpy(b.data(), c->b, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        for (int64_t q = 0; q < n; ++q) rhs[q] = b[slot_of[q]];
+    }
+    if (!col && !val) return BSC_OK;
+    std::vector<int32_t> nb(slots);
+    std::vector<double> v(slots);
+    BSC_CUDA(c, cudaMemcpy(nb.data(), c->nbr, sizeof(int32_t) * slots, cudaMemcpyDeviceToHost));
+    if (c->mixed) {
+        std::vector<float> vf(slots);
+        BSC_CUDA(c, cudaMemcpy(vf.data(), c->avalf, sizeof(float) * slots, cudaMemcpyDeviceToHost));
+        for (int64_t e = 0; e < slots; ++e) v[e] = vf[e];
+    } else {
+        BSC_CUDA(c, cudaMemcpy(v.data(), c->aval, sizeof(double) * slots, cudaMemcpyDeviceToHost));
+    }
+    std::vector<std::pair<int32_t, double>> row;
+    for (int64_t q = 0; q < n; ++q) {
+        const int64_t k = slot_of[q];
+        row.clear();
+        row.push_back({(int32_t)q, 1.0});
+        for (int e = 0; e < cnt[k]; ++e) {
+            const int64_t x = ell(k, e, (int)kmax);
+            row.push_back({id[nb[x]], v[x]});
+        }
+        std::stable_sort(row.begin(), row.end(), [](auto& a, auto& b) { return a.first < b.first; });
+        for (size_t e = 0; e < row.size(); ++e) {
+            if (col) col[rowptr[q] + e] = row[e].first;
+            if (val) val[rowptr[q] + e] = row[e].second;
+        }
+    }
+    return BSC_OK;
+}
+
+int bsc_probe_eta(bsc_ctx* c, int32_t np, const double* xp, double depth, double* eta) {
+    STATE_GUARD(c);
+    if (!xp || !eta) return set_err(c, BSC_E_INVALID, "probe_eta: null pointer");
+    return op_probe_eta(c, np, xp, depth, eta);
+}
+
+int bsc_get_timings(bsc_ctx* c, bsc_timing* out) {
+    CTX_GUARD(c);
+    if (!out) return BSC_E_INVALID;
+    timing_flush(c);
+    for (int k = 0; k < BSC_TIMING_SLOTS; ++k) {
+        out->ms[k] = c->ms[k];
+        out->calls[k] = c->calls[k];
+    }
+    out->kernel_launches = c->launches;
+    return BSC_OK;
+}
+
+int bsc_reset_timings(bsc_ctx* c) {
+    CTX_GUARD(c);
+    timing_flush(c);
+    for (int k = 0; k < BSC_TIMING_SLOTS; ++k) {
+        c->ms[k] = 0;
+        c->calls[k] = 0;
+    }
+    c->launches = 0;
+    return BSC_OK;
+}
+
+int bsc_synchronize(bsc_ctx* c) {
+    CTX_GUARD(c);
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BSC_OK;
+}
+
+int bsc_csr_solve(const bsc_params* p, int32_t n, const int32_t* rowptr, const int32_t* col, const double* val,
+                  const double* b, double* x, bsc_solve_info* info) {
+    if (!p || n <= 0 || !rowptr || !col || !val || !b || !x || !info) return BSC_E_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BSC_E_NOT_BUILT;
+    Ctx c;
+    c.P = *p;
+    if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) return BSC_E_CUDA;
+    const int64_t nnz = rowptr[n];
+    int rc = alloc_solver_work(&c, n, true, false);
+    int32_t *drp = nullptr, *dcol = nullptr;
+    double *dval = nullptr, *db = nullptr, *dx = nullptr;
+    if (!rc) rc = dalloc(&c, &drp, n + 1);
+    if (!rc) rc = dalloc(&c, &dcol, nnz);
+    if (!rc) rc = dalloc(&c, &dval, nnz);
+    if (!rc) rc = dalloc(&c, &db, n);
+    if (!rc) rc = dalloc(&c, &dx, n);
+    if (!rc) {
+        cudaMemcpy(drp, rowptr, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice);
+        cudaMemcpy(dcol, col, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice);
+        cudaMemcpy(dval, val, sizeof(double) * nnz, cudaMemcpyHostToDevice);
+        cudaMemcpy(db, b, sizeof(double) * n, cudaMemcpyHostToDevice);
+        cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice);
+        rc = csr_solve_device(&c, n, drp, dcol, dval, db, dx, info);
+        if (rc == BSC_OK || rc == BSC_E_NOT_CONVERGED || rc == BSC_E_BREAKDOWN)
+            cudaMemcpy(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost);
+    }
+    free_all(&c);
+    cudaStreamDestroy(c.stream);
+    return rc;
+}
+
+}  // extern "C"

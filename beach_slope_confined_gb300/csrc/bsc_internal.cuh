@@ -1,0 +1,215 @@
+// bsc_internal.cuh -- device state layout and shared helpers of libbsc.
+//
+// Layout in HBM (one context = one GPU, state resident across steps):
+//  * particle state: structure of arrays, FP64, one slot per particle, slots
+//    kept sorted by cell (Morton order of the 2h cells) and re-sorted every
+//    `reorder_every` cell shifts; `id[slot]` maps back to the caller's order;
+//  * cell list: cells of side >= 2h (3x3 stencil covers the 2h support),
+//    cell_start/cell_count over cells, `sorted[]` = slots in cell order;
+//  * neighbour lists: ELL with 32-slot slices stored column-major
+//    (entry k of slot i at ((i/32)*kmax + k)*32 + i%32), holding the
+//    neighbour slot and grad_i W, so each column read by a warp is one
+//    coalesced transaction;
+//  * PPE: the Jacobi-scaled matrix has a unit diagonal; its off-diagonal
+//    values share the neighbour-list layout (no extra column indices).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/bsc.h"
+
+namespace bsc {
+
+constexpr int WARP = 32;
+constexpr int NB_BLOCK = 128;     // threads per block for particle kernels
+constexpr int RED_BLOCK = 256;    // threads per block for reductions
+constexpr int RED_GRID = 304;     // fixed reduction grid (2 x 152 SMs): deterministic sums
+
+// ---- particle state (SoA) --------------------------------------------------
+struct State {
+    double *x, *y, *vx, *vy, *xs, *ys, *vxs, *vys, *p, *rho, *oden, *mass;
+    double *por, *gradvx, *nut, *tke, *resist, *varts, *vel, *xrest, *vol;
+    double *L0, *L1, *L2, *L3;
+    int8_t* tid;
+    uint8_t* flags;
+    int32_t* id;
+};
+constexpr int N_DBL_FIELDS = 25;
+
+// ---- neighbour list (ELL, 32-slot slices) ----------------------------------
+__host__ __device__ inline int64_t ell(int64_t i, int k, int kmax) {
+    return ((i >> 5) * (int64_t)kmax + k) * 32 + (i & 31);
+}
+
+// ---- solver scalars kept on the device -------------------------------------
+struct Scalars {
+    double rhob[2];            // rho of the current iteration, by iteration parity
+    double rho, alpha, omega, beta;
+    double rr, bnorm, r0norm, target;
+    double tmp[8];
+    int32_t done, breakdown, it, pad;
+};
+
+// ---- kernel constants --------------------------------------------------------
+struct KParams {
+    int kernel;
+    double h, H, H2, lam, dl, rho0, rel_den, g, csh, maxshift, free_thr;
+    double por, alpha, beta, d50;
+    double eddy_cs, eddy_cv, eddy_ce, varts_ps;
+    double bxmin, bxmax;
+    // kernel coefficients: grad_i W = F(r) (x_i - x_j)
+    double hyb_A, hyb_B, wend_F, wend_W, w0;
+    // cell grid
+    double gx0, gy0, cs;
+    int nx, ny;
+    int kmax;
+    // porosity field
+    int pnx, pny;
+    double px0, py0, pdx, pdy;
+    const double* pgrid;
+};
+
+struct Ctx;
+
+// ---- error handling ----------------------------------------------------------
+int set_err(Ctx* c, int code, const std::string& msg);
+int cuda_err(Ctx* c, cudaError_t e, const char* where);
+#define BSC_CUDA(c, call)                                  \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return cuda_err((c), e_, #call); \
+    } while (0)
+#define BSC_LAUNCH(c)                                      \
+    do {                                                   \
+        (c)->launches++;                                   \
+        cudaError_t e_ = cudaGetLastError();               \
+        if (e_ != cudaSuccess) return cuda_err((c), e_, __func__); \
+    } while (0)
+
+template <typename T> struct Vec2;
+template <> struct Vec2<double> { using type = double2; };
+template <> struct Vec2<float> { using type = float2; };
+
+inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// ---- the context ---------------------------------------------------------------
+struct Ctx {
+    bsc_params P{};
+    KParams K{};
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    std::string err;
+    double t = 0.0, dt = 0.0, umax = 0.0, numax = 0.0, dtsol = 0.0;
+    int solsteps = 1;
+    int64_t n = 0, cap = 0, ns = 0;
+    int64_t launches = 0;
+    int64_t cellshifts = 0;
+    bool have_lists = false, have_csr = false, have_state = false;
+    bool mixed = false;
+
+    State S{}, S2{};           // S2: gather target of the Morton reorder
+    std::vector<void*> allocs; // everything cudaMalloc'ed, freed at destroy
+
+    // cell list
+    int ncell = 0;
+    int32_t *cell_start = nullptr, *cell_count = nullptr, *cell_rank = nullptr, *cell_tmp = nullptr;
+    int32_t *pcell = nullptr, *pslot = nullptr, *sorted = nullptr;
+    int32_t *scan_part = nullptr;
+    // solids: their own cell list, static after upload
+    double *sx = nullptr, *sy = nullptr, *svol = nullptr, *spor = nullptr;
+    int32_t *scell_start = nullptr, *scell_count = nullptr;
+    double* pgrid = nullptr;
+
+    // neighbour lists
+    int32_t* nbr = nullptr;
+    double2* gw = nullptr;        // FP64 grad W
+    float2* gwf = nullptr;        // FP32 grad W (mixed)
+    int32_t* cnt = nullptr;
+    int32_t* d_flag = nullptr;    // device error flags (capacity, nonfinite)
+    int32_t* h_flag = nullptr;    // pinned mirror
+
+    // PPE
+    double* aval = nullptr;       // FP64 off-diagonals (ELL layout)
+    float* avalf = nullptr;       // FP32 off-diagonals (mixed)
+    double* b = nullptr;
+    float* bf = nullptr;
+    // Krylov work (FP64) and (FP32)
+    double *r = nullptr, *rh = nullptr, *pd = nullptr, *v = nullptr, *s = nullptr, *tv = nullptr, *xw = nullptr;
+    float *rf = nullptr, *rhf = nullptr, *pf = nullptr, *vf = nullptr, *sf = nullptr, *tf = nullptr, *xf = nullptr;
+    double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64
+    float* Vf = nullptr;          // FGMRES basis FP32 (mixed)
+    double* Hd = nullptr;         // Hessenberg + Givens + y on device
+    double* part = nullptr;       // reduction partials RED_GRID x 64
+    Scalars* sc = nullptr;
+    Scalars* h_sc = nullptr;      // pinned mirror
+    int fg_m = 0;
+
+    // timing: stage events recorded on the stream, resolved lazily
+    static constexpr int EVPOOL = 256;
+    cudaEvent_t evs[2 * EVPOOL] = {};
+    int ev_slot[EVPOOL] = {};
+    int ev_used = 0;
+    double ms[BSC_TIMING_SLOTS] = {0};
+    int64_t calls[BSC_TIMING_SLOTS] = {0};
+    bool timing = true;
+    double* stepsc = nullptr;     // device: umax, numax (timestep reductions)
+};
+
+void timing_flush(Ctx* c);
+
+// ---- stage timer: a pair of CUDA events on the context stream -----------------
+struct StageTimer {
+    Ctx* c;
+    int k = -1;
+    StageTimer(Ctx* c_, int slot) : c(c_) {
+        if (!c->timing) return;
+        if (c->ev_used == Ctx::EVPOOL) timing_flush(c);
+        k = c->ev_used++;
+        c->ev_slot[k] = slot;
+        cudaEventRecord(c->evs[2 * k], c->stream);
+    }
+    ~StageTimer() {
+        if (k >= 0) cudaEventRecord(c->evs[2 * k + 1], c->stream);
+    }
+};
+
+// ---- module entry points (implemented in the .cu files) -----------------------
+// cells.cu
+int cells_build(Ctx* c, bool allow_reorder);
+int solids_build(Ctx* c);
+int op_projection(Ctx* c);
+int op_piston(Ctx* c);
+int op_comp_pos(Ctx* c);
+// pairs.cu
+int op_neighbour(Ctx* c);
+int op_freesurf(Ctx* c);
+int op_effpor(Ctx* c);
+int op_eddyvis(Ctx* c);
+int op_int_vel(Ctx* c, const double* d_umax);
+int op_comp_vel(Ctx* c);
+int op_opt2_shift(Ctx* c);
+int op_timestep_reduce(Ctx* c);
+int op_probe_eta(Ctx* c, int np, const double* xp, double depth, double* eta);
+// ppe.cu
+int op_ppe_assemble(Ctx* c);
+int op_ppe_solve(Ctx* c, bsc_solve_info* info);
+int fg_layout_size(int m);
+int csr_solve_device(Ctx* c, int32_t n, const int32_t* rp, const int32_t* col, const double* val,
+                     const double* b, double* x, bsc_solve_info* info);
+
+template <typename T>
+int dalloc(Ctx* c, T** p, int64_t count) {
+    void* q = nullptr;
+    size_t bytes = (size_t)(count > 0 ? count : 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc");
+    c->allocs.push_back(q);
+    *p = (T*)q;
+    return BSC_OK;
+}
+
+}  // namespace bsc

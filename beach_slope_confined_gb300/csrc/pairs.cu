@@ -1,0 +1,646 @@
+// pairs.cu -- neighbour search and the per-pair SPH operators.
+//
+// One thread per particle.  Candidates come from the 3x3 block of 2h cells
+// around the particle (the reference scans the 2x2 block of 4h cells picked
+// by the particle's quadrant, search.f90:328-388; both blocks contain the
+// whole 2h disc, so the neighbour sets are the same).  The neighbour test is
+// the reference's sqrt((xi-xj)^2+(yi-yj)^2) < 2h (functions.f90:38,
+// search.f90:59) evaluated with correctly rounded FP64 operations and no
+// contraction, so the sets are bit-identical to the CPU restatement; an FP32
+// pre-test with a 1e-5 relative margin rejects the far candidates first.
+//
+// Every operator is templated on R, the type of the pair arithmetic: double
+// for the FP64 drop-in path, float for the mixed path (which keeps the
+// particle state, the neighbour predicate and the 2x2 inversion in FP64).
+#include <cmath>
+
+#include "bsc_internal.cuh"
+
+namespace bsc {
+
+// ---- smoothing kernel --------------------------------------------------------
+// grad_i W = F(r) (x_i - x_j).  Hybrid (kernel.f90:94-162):
+//   r <  h: F = A (9r/h^3 - 12/h^2) + B (3r/h^3 - 6/(r h))
+//   r >= h: F = -(A + B) (3/(r h)) (2 - r/h)^2
+// with A = 0.1*10/(28*3.14 h^2), B = 0.9/(3*3.14 h^2) (3.14 is the
+// reference's single-precision literal).  Wendland C2 (kernel.f90:102-103):
+//   F = -35/(4*3.14 h^4) (1 - r/(2h))^3.
+template <typename R>
+__device__ __forceinline__ R grad_factor(const KParams& K, R r) {
+    const R h = (R)K.h;
+    if (K.kernel == BSC_KERNEL_WENDLAND_C2) {
+        R a = (R)1 - r / ((R)2 * h);
+        return -(R)K.wend_F * (a * a * a);
+    }
+    const R A = (R)K.hyb_A, B = (R)K.hyb_B;
+    const R h2 = h * h, h3 = h2 * h;
+    if (r < h) return A * ((R)9 * r / h3 - (R)12 / h2) + B * ((R)3 * r / h3 - (R)6 / (r * h));
+    R a = (R)2 - r / h;
+    return -(A + B) * ((R)3 / (r * h)) * (a * a);
+}
+
+// W(r) (kernel.f90:34-66 and the Wendland comment at :42-43)
+template <typename R>
+__device__ __forceinline__ R kern_w(const KParams& K, R r) {
+    const R h = (R)K.h;
+    if (K.kernel == BSC_KERNEL_WENDLAND_C2) {
+        R q = r / h, a = (R)1 - r / ((R)2 * h), a2 = a * a;
+        return (R)K.wend_W * ((R)1 + (R)2 * q) * (a2 * a2);
+    }
+    const R A = (R)K.hyb_A, B = (R)K.hyb_B;
+    R q = r / h;
+    if (r < h) return A * ((R)4 - (R)6 * q * q + (R)3 * q * q * q) + B * (q * q * q - (R)6 * q + (R)6);
+    R a = (R)2 - q;
+    return (A + B) * (a * a * a);
+}
+
+// vis(oden) of porous.f90:12-30 / integrator.f90:12-30
+__device__ __forceinline__ double vis_of(double oden) {
+    double Sp = oden - 1000.0;
+    return (1.002 + 0.001652 * Sp + 0.0000083 * (Sp * Sp)) * 0.001;
+}
+
+__device__ __forceinline__ double porosity_at(const KParams& K, double x, double y) {
+    if (K.pnx <= 0) return K.por;
+    double fx = floor((x - K.px0) / K.pdx), fy = floor((y - K.py0) / K.pdy);
+    if (!(fx >= 0.0 && fx < (double)K.pnx && fy >= 0.0 && fy < (double)K.pny)) return K.por;
+    return K.pgrid[(int64_t)fy * K.pnx + (int64_t)fx];
+}
+
+// ---- search.f90:13-399 neighbour / nsearch2 ----------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KParams K,
+                                                         const int32_t* __restrict__ cstart,
+                                                         const int32_t* __restrict__ ccount,
+                                                         const int32_t* __restrict__ sorted,
+                                                         const int32_t* __restrict__ pcell,
+                                                         int32_t* __restrict__ nbr,
+                                                         typename Vec2<R>::type* __restrict__ gw,
+                                                         int32_t* __restrict__ cnt, int32_t* __restrict__ flag) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double xi = S.x[i], yi = S.y[i];
+    const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
+    const float H2f = (float)(K.H2 * (1.0 + 1e-5));
+    R m0 = 0, m1 = 0, m2 = 0, m3 = 0;
+    int count = 0;
+    for (int ax = cx - 1; ax <= cx + 1; ++ax) {
+        if (ax < 0 || ax >= K.nx) continue;
+        for (int ay = cy - 1; ay <= cy + 1; ++ay) {
+            if (ay < 0 || ay >= K.ny) continue;
+            const int cc = ax * K.ny + ay;
+            const int s0 = cstart[cc], s1 = s0 + ccount[cc];
+            for (int s = s0; s < s1; ++s) {
+                const int j = sorted[s];
+                if (j == (int)i) continue;  // (tid,matid) self test, search.f90:53-55
+                const double dx = xi - S.x[j], dy = yi - S.y[j];
+                const float fdx = (float)dx, fdy = (float)dy;
+                if (fdx * fdx + fdy * fdy > H2f) continue;
+                const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                if (!(r < K.H)) continue;
+                const R F = grad_factor<R>(K, (R)r);
+                const R gx = F * (R)dx, gy = F * (R)dy;
+                if (count < K.kmax) {
+                    const int64_t e = ell(i, count, K.kmax);
+                    nbr[e] = j;
+                    gw[e] = {gx, gy};
+                }
+                ++count;
+                const R vj = (R)S.vol[j];
+                const R rx = -vj * (R)dx, ry = -vj * (R)dy;  // m_j (x_j - x_i) / rho_j
+                m0 += gx * rx;
+                m1 += gy * rx;
+                m2 += gx * ry;
+                m3 += gy * ry;
+            }
+        }
+    }
+    if (count > K.kmax) {
+        atomicOr(flag, 1);
+        count = K.kmax;
+    }
+    cnt[i] = count;
+    uint8_t f = S.flags[i] & (uint8_t)~BSC_FLAG_FREE;  // search.f90:41
+    double gv = 0.0;
+    if (S.tid[i] == BSC_TID_FLUID) {  // search.f90:268-306
+        f &= (uint8_t)~BSC_FLAG_VICINITY;
+        const double a0 = m0, a1 = m1, a2 = m2, a3 = m3;
+        gv = a0 + a3;
+        // invertmat2D (functions.f90:62-96), FP64 in both precisions
+        const double det = __dsub_rn(__dmul_rn(a0, a3), __dmul_rn(a1, a2));
+        double l0 = 1.0, l1 = 0.0, l2 = 0.0, l3 = 1.0;
+        if (fabs(det) >= (double)1e-5f && isfinite(det)) {
+            l0 = a3 / det;
+            l1 = -a1 / det;
+            l2 = -a2 / det;
+            l3 = a0 / det;
+        }
+        S.L0[i] = l0; S.L1[i] = l1; S.L2[i] = l2; S.L3[i] = l3;
+        if (gv <= K.free_thr && !(f & BSC_FLAG_BUFFER)) f |= BSC_FLAG_FREE;
+    }
+    S.gradvx[i] = gv;
+    S.flags[i] = f;
+}
+
+int op_neighbour(Ctx* c) {
+    const unsigned g = blocks_for(c->n, NB_BLOCK);
+    if (c->mixed)
+        k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
+                                                          c->pcell, c->nbr, c->gwf, c->cnt, c->d_flag);
+    else
+        k_neighbour<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count,
+                                                           c->sorted, c->pcell, c->nbr, c->gw, c->cnt, c->d_flag);
+    BSC_LAUNCH(c);
+    c->have_lists = true;
+    return BSC_OK;
+}
+
+// ---- isph.f90:49-86 freesurf, gather form --------------------------------------
+// vicinity_j |= (exists neighbour i: fluid, not buffer, tr M_i <= threshold).
+// The neighbour relation is symmetric, so j's own list enumerates the i that
+// would have scattered to it; this removes the reference's racy scatter.
+__global__ void k_freesurf(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
+                           const int32_t* __restrict__ cnt) {
+    const int64_t j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int m = cnt[j];
+    bool hit = false;
+    for (int k = 0; k < m && !hit; ++k) {
+        const int i = nbr[ell(j, k, K.kmax)];
+        hit = (S.tid[i] == BSC_TID_FLUID) && !(S.flags[i] & BSC_FLAG_BUFFER) && (S.gradvx[i] <= K.free_thr);
+    }
+    if (hit) S.flags[j] |= BSC_FLAG_VICINITY;
+}
+
+int op_freesurf(Ctx* c) {
+    k_freesurf<<<blocks_for(c->n, NB_BLOCK), NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->cnt);
+    BSC_LAUNCH(c);
+    return BSC_OK;
+}
+
+// ---- porous.f90:107-224 effpor ---------------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams K, const int32_t* __restrict__ pcell,
+                                                      const int32_t* __restrict__ scs, const int32_t* __restrict__ scc,
+                                                      const double* __restrict__ sx, const double* __restrict__ sy,
+                                                      const double* __restrict__ svol,
+                                                      const double* __restrict__ spor) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    S.resist[i] = 0.0;
+    if (S.tid[i] != BSC_TID_FLUID) return;
+    const double xi = S.x[i], yi = S.y[i];
+    const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
+    const float H2f = (float)(K.H2 * (1.0 + 1e-5));
+    R frac = 0;
+    for (int ax = cx - 1; ax <= cx + 1; ++ax) {
+        if (ax < 0 || ax >= K.nx) continue;
+        for (int ay = cy - 1; ay <= cy + 1; ++ay) {
+            if (ay < 0 || ay >= K.ny) continue;
+            const int cc = ax * K.ny + ay;
+            const int s0 = scs[cc], s1 = s0 + scc[cc];
+            for (int s = s0; s < s1; ++s) {
+                const double dx = xi - sx[s], dy = yi - sy[s];
+                const float fdx = (float)dx, fdy = (float)dy;
+                if (fdx * fdx + fdy * fdy > H2f) continue;
+                const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
+                if (!(r < K.H)) continue;
+                frac += ((R)1 - (R)spor[s]) * kern_w<R>(K, (R)r) * (R)svol[s];
+            }
+        }
+    }
+    double sf = (double)frac;
+    const double cap = 1.0 - porosity_at(K, xi, yi);
+    if (sf > cap) sf = cap;
+    const double nn = 1.0 - sf;
+    const double oden = S.oden[i];
+    const double rho = nn * oden;
+    S.por[i] = nn;
+    S.rho[i] = rho;
+    S.vol[i] = S.mass[i] / rho;
+    // Ergun/Darcy-Forchheimer coefficient (porous.f90:192,204-212),
+    // Fch*sqrt(lamk) written as beta/sqrt(n^3)
+    const double n3 = nn * nn * nn, d = K.d50;
+    const double vx = S.vx[i], vy = S.vy[i];
+    const double vmag = sqrt(vx * vx + vy * vy);
+    S.resist[i] = -((vis_of(oden) / oden) * K.alpha * ((1.0 - nn) * (1.0 - nn)) / (n3 * (d * d))) -
+                  ((K.beta / sqrt(n3)) * vmag * (1.0 - nn)) / (sqrt(n3) * d);
+}
+
+int op_effpor(Ctx* c) {
+    const unsigned g = blocks_for(c->n, NB_BLOCK);
+    if (c->mixed)
+        k_effpor<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
+                                                       c->sx, c->sy, c->svol, c->spor);
+    else
+        k_effpor<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
+                                                        c->sx, c->sy, c->svol, c->spor);
+    BSC_LAUNCH(c);
+    return BSC_OK;
+}
+
+// per-particle quotients shared by the pair loops: u = v/n (eddyvis, int_vel)
+__global__ void k_vel_over_por(int64_t n, State S, double* __restrict__ ux, double* __restrict__ uy) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double nn = S.por[i];
+    ux[i] = S.vx[i] / nn;
+    uy[i] = S.vy[i] / nn;
+}
+
+// ---- turbulence.f90:12-110 eddyvis -----------------------------------------------
+template <typename R>
+__global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
+                                                       const typename Vec2<R>::type* __restrict__ gw,
+                                                       const int32_t* __restrict__ cnt, const double* __restrict__ ux,
+                                                       const double* __restrict__ uy) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n || S.tid[i] != BSC_TID_FLUID) return;
+    const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+    const double uxi = ux[i], uyi = uy[i];
+    R t1 = 0, t2 = 0, t3 = 0;
+    const int m = cnt[i];
+    for (int k = 0; k < m; ++k) {
+        const int64_t e = ell(i, k, K.kmax);
+        const int j = nbr[e];
+        const auto g = gw[e];
+        const R vj = (R)S.vol[j];
+        const R du = (R)(ux[j] - uxi), dv = (R)(uy[j] - uyi);
+        const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
+        t1 += vj * du * gx;
+        t2 += vj * dv * gy;
+        t3 += (R)0.5 * vj * (du * gy + dv * gx);
+    }
+    const double T1 = t1, T2 = t2, T3 = t3;
+    const double t4 = sqrt(2 * (T1 * T1 + T2 * T2) + (2 * T3) * (2 * T3));
+    const double csdl = K.eddy_cs * K.dl, dlt = K.dl * t4;
+    S.nut[i] = (csdl * csdl) * t4;
+    S.tke[i] = (K.eddy_cv / K.eddy_ce) * (dlt * dlt);
+}
+
+int op_eddyvis(Ctx* c) {
+    if (!c->have_lists) return set_err(c, BSC_E_INVALID, "eddyvis before neighbour");
+    double *ux = c->r, *uy = c->rh;  // Krylov work vectors double as scratch outside the solve
+    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy);
+    BSC_LAUNCH(c);
+    const unsigned g = blocks_for(c->n, NB_BLOCK);
+    if (c->mixed)
+        k_eddyvis<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy);
+    else
+        k_eddyvis<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy);
+    BSC_LAUNCH(c);
+    return BSC_OK;
+}
+
+// ---- integrator.f90:458-713 int_vel ------------------------------------------------
+// pass 1: free-surface artificial viscosity (:467-506)
+template <typename R>
+__global__ void __launch_bounds__(NB_BLOCK) k_varts(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
+                                                     const typename Vec2<R>::type* __restrict__ gw,
+                                                     const int32_t* __restrict__ cnt, const double* __restrict__ ux,
+                                                     const double* __restrict__ uy, const double* __restrict__ umax) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n || !(S.flags[i] & BSC_FLAG_FREE)) return;
+    const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+    const double uxi = ux[i], uyi = uy[i];
+    R t1 = 0, t2 = 0;
+    const int m = cnt[i];
+    for (int k = 0; k < m; ++k) {
+        const int64_t e = ell(i, k, K.kmax);
+        const int j = nbr[e];
+        const auto g = gw[e];
+        const R vj = (R)S.vol[j];
+        t1 += (R)(ux[j] - uxi) * (L0 * g.x + L1 * g.y) * vj;
+        t2 += (R)(uy[j] - uyi) * (L2 * g.x + L3 * g.y) * vj;
+    }
+    const double T1 = t1, T2 = t2, vx = S.vx[i], vy = S.vy[i];
+    S.varts[i] = K.varts_ps * (K.dl * K.dl) * sqrt(T1 * T1 + T2 * T2) * sqrt(vx * vx + vy * vy) /
+                 ((*umax + (double)1e-6f) * S.por[i]);
+}
+
+// pass 2: viscous (Morris, harmonic mu/oden), eddy viscosity, SPS k gradient,
+// implicit porous drag and gravity (:509-711)
+template <typename R>
+__global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
+                                                       const typename Vec2<R>::type* __restrict__ gw,
+                                                       const int32_t* __restrict__ cnt,
+                                                       const double* __restrict__ nu, double dt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint8_t fi = S.flags[i];
+    if (S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD))) {
+        const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+        const double xi = S.x[i], yi = S.y[i], vxi = S.vx[i], vyi = S.vy[i];
+        const R nui = (R)nu[i], nuti = (R)S.nut[i], tkei = (R)S.tke[i], ni = (R)S.por[i];
+        const bool free_i = fi & BSC_FLAG_FREE;
+        const R varts_i = (R)S.varts[i];
+        const R inv_w0 = (R)(1.0 / K.w0);
+        const R eps6 = (R)(double)1e-6f;
+        R ax = 0, ay = 0;
+        const int m = cnt[i];
+        for (int k = 0; k < m; ++k) {
+            const int64_t e = ell(i, k, K.kmax);
+            const int j = nbr[e];
+            const auto g = gw[e];
+            const bool fluid_j = S.tid[j] == BSC_TID_FLUID;
+            R cmu;
+            if (fluid_j) {
+                const R nuj = (R)nu[j];
+                cmu = (R)2 * nui * nuj / (nui + nuj);
+            } else {
+                cmu = nui;
+            }
+            const double dx = xi - S.x[j], dy = yi - S.y[j];
+            R vart = 0;
+            if (free_i) {
+                vart = varts_i;
+            } else if ((S.flags[j] & BSC_FLAG_FREE) && !(fi & BSC_FLAG_BUFFER)) {
+                const R r = (R)sqrt(dx * dx + dy * dy);
+                vart = kern_w<R>(K, r) * (R)S.varts[j] * inv_w0;
+            }
+            const R pvol = (R)S.vol[j];
+            const R p_dist = (R)1 / ((R)(dx * dx + dy * dy) + (R)K.lam);
+            const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
+            const R geo = (R)2 * pvol * ((R)dx * gx + (R)dy * gy) * p_dist;
+            const R dvx = (R)(vxi - S.vx[j]), dvy = (R)(vyi - S.vy[j]);
+            R visc = cmu + vart;
+            if (fluid_j) {
+                const R nutj = (R)S.nut[j];
+                if (nuti < eps6 && nutj < eps6) visc += (nuti + nutj) * (R)0.5;
+                else visc += ((R)2 * nuti * nutj) / (nuti + nutj);
+            }
+            ax += geo * dvx * visc;
+            ay += geo * dvy * visc;
+            // SPS turbulence (:645-666)
+            const R dk = pvol * ((R)S.tke[j] - tkei);
+            ax -= dk * gx * ni * (R)2 / (R)3;
+            ay -= dk * gy * ni * (R)2 / (R)3;
+        }
+        const double nn = S.por[i], R_ = S.resist[i];
+        double vxs = (vxi + dt * (double)ax) / (1.0 - dt * R_ * nn);
+        double vys = (vyi + dt * (double)ay) / (1.0 - dt * R_ * nn);
+        vys = vys + K.g * nn * dt;
+        S.vxs[i] = vxs;
+        S.vys[i] = vys;
+    }
+    if (fi & BSC_FLAG_BUFFER) {  // :691-698
+        S.vxs[i] = S.vx[i];
+        S.vys[i] = K.g * S.por[i] * dt;
+    }
+}
+
+__global__ void k_kin_visc(int64_t n, State S, double* __restrict__ nu) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double o = S.oden[i];
+    nu[i] = vis_of(o) / o;
+}
+
+int op_int_vel(Ctx* c, const double* d_umax) {
+    if (!c->have_lists) return set_err(c, BSC_E_INVALID, "int_vel before neighbour");
+    double *ux = c->r, *uy = c->rh, *nu = c->pd;
+    const unsigned g = blocks_for(c->n, NB_BLOCK);
+    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy);
+    BSC_LAUNCH(c);
+    if (c->mixed)
+        k_varts<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy, d_umax);
+    else
+        k_varts<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy, d_umax);
+    BSC_LAUNCH(c);
+    k_kin_visc<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, nu);
+    BSC_LAUNCH(c);
+    if (c->mixed)
+        k_int_vel<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, nu, c->dt);
+    else
+        k_int_vel<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, nu, c->dt);
+    BSC_LAUNCH(c);
+    return BSC_OK;
+}
+
+// ---- integrator.f90:715-865 comp_vel (comp_pos is separate, cells.cu) ---------------
+__global__ void k_rho_over_por(int64_t n, State S, double* __restrict__ q) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) q[i] = S.rho[i] / S.por[i];
+}
+
+template <typename R>
+__global__ void __launch_bounds__(NB_BLOCK) k_comp_vel(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
+                                                        const typename Vec2<R>::type* __restrict__ gw,
+                                                        const int32_t* __restrict__ cnt,
+                                                        const double* __restrict__ q, double dt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint8_t fi = S.flags[i];
+    if (S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD))) {
+        const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+        const R ni = (R)S.por[i], rhoi = (R)S.rho[i], pi = (R)S.p[i], qi = (R)q[i];
+        const R c0 = ni * ni / rhoi;
+        R ax = 0, ay = 0;
+        const int m = cnt[i];
+        for (int k = 0; k < m; ++k) {
+            const int64_t e = ell(i, k, K.kmax);
+            const int j = nbr[e];
+            const auto g = gw[e];
+            const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
+            const R vj = (R)S.vol[j], pj = (R)S.p[j];
+            R w;
+            if (S.tid[j] == BSC_TID_FLUID) {
+                const R qj = (R)q[j];
+                w = (R)2 * vj * c0 * (pj * qi + pi * qj) / (qi + qj);
+            } else {
+                w = vj * c0 * (pj + pi);
+            }
+            ax += w * gx;
+            ay += w * gy;
+        }
+        const double vx = S.vxs[i] - dt * (double)ax;
+        const double vy = S.vys[i] - dt * (double)ay;
+        S.vx[i] = vx;
+        S.vy[i] = vy;
+        S.vel[i] = sqrt(vx * vx + vy * vy) / S.por[i];
+    }
+    if (fi & BSC_FLAG_BUFFER) {
+        S.vx[i] = S.vxs[i];
+        S.vy[i] = 0.0;
+    }
+    if ((fi & BSC_FLAG_DEAD) && !(fi & BSC_FLAG_BUFFER)) {
+        S.vx[i] = 0.0; S.vy[i] = 0.0; S.vxs[i] = 0.0; S.vys[i] = 0.0;
+    }
+}
+
+int op_comp_vel(Ctx* c) {
+    if (!c->have_lists) return set_err(c, BSC_E_INVALID, "comp_vel before neighbour");
+    double* q = c->r;
+    k_rho_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, q);
+    BSC_LAUNCH(c);
+    const unsigned g = blocks_for(c->n, NB_BLOCK);
+    if (c->mixed)
+        k_comp_vel<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, q, c->dt);
+    else
+        k_comp_vel<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, q, c->dt);
+    BSC_LAUNCH(c);
+    return BSC_OK;
+}
+
+// ---- part_shift.f90:12-192 opt2_shift ------------------------------------------------
+// The surface normal and pint are forced to zero in the reference
+// (part_shift.f90:68-70), so the shift is -csh h^2 frac sum V_j grad W
+// (uncorrected), clamped per component to maxshift*dl; the velocity is
+// corrected with the unclamped shift and the corrected gradient.
+template <typename R>
+__global__ void __launch_bounds__(NB_BLOCK) k_shift(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
+                                                     const typename Vec2<R>::type* __restrict__ gw,
+                                                     const int32_t* __restrict__ cnt, int8_t* __restrict__ mark) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    mark[i] = 0;
+    const uint8_t fi = S.flags[i];
+    if (!(S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD)))) return;
+    const int m = cnt[i];
+    if (m == 0) return;
+    const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+    const double vxi = S.vx[i], vyi = S.vy[i];
+    R sx = 0, sy = 0, tx1 = 0, tx2 = 0, ty1 = 0, ty2 = 0;
+    for (int k = 0; k < m; ++k) {
+        const int64_t e = ell(i, k, K.kmax);
+        const int j = nbr[e];
+        const auto g = gw[e];
+        const R vj = (R)S.vol[j];
+        sx += g.x * vj;
+        sy += g.y * vj;
+        const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
+        const R dvx = (R)(S.vx[j] - vxi), dvy = (R)(S.vy[j] - vyi);
+        tx1 += gx * dvx * vj;
+        tx2 += gy * dvx * vj;
+        ty1 += gx * dvy * vj;
+        ty2 += gy * dvy * vj;
+    }
+    const double frac = (fi & BSC_FLAG_FREE) ? 0.01 : 1.0;
+    const double coef = -K.csh * (K.h * K.h) * frac;
+    const double xs = coef * (double)sx, ys = coef * (double)sy;
+    const double lim = K.maxshift * K.dl;
+    const double cx = (xs == 0.0) ? 0.0 : fmin(fabs(xs), lim) * xs / fabs(xs);
+    const double cy = (ys == 0.0) ? 0.0 : fmin(fabs(ys), lim) * ys / fabs(ys);
+    S.xs[i] = cx;
+    S.ys[i] = cy;
+    S.vxs[i] = (double)tx1 * xs + (double)tx2 * ys;
+    S.vys[i] = (double)ty1 * xs + (double)ty2 * ys;
+    mark[i] = 1;
+}
+
+__global__ void k_shift_apply(int64_t n, State S, const int8_t* __restrict__ mark) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n || !mark[i]) return;
+    S.x[i] += S.xs[i];
+    S.y[i] += S.ys[i];
+    S.vx[i] += S.vxs[i];
+    S.vy[i] += S.vys[i];
+}
+
+int op_opt2_shift(Ctx* c) {
+    if (!c->have_lists) return set_err(c, BSC_E_INVALID, "opt2_shift before neighbour");
+    int8_t* mark = (int8_t*)c->pslot;  // scratch: pslot is free between cell builds
+    const unsigned g = blocks_for(c->n, NB_BLOCK);
+    if (c->mixed)
+        k_shift<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, mark);
+    else
+        k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, mark);
+    BSC_LAUNCH(c);
+    k_shift_apply<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, mark);
+    BSC_LAUNCH(c);
+    return BSC_OK;
+}
+
+// ---- integrator.f90:908-976 timestep: max |vel|, max |nut| (comp_vel :853-861) --------
+__global__ void k_maxred(int64_t n, const double* __restrict__ a, const double* __restrict__ b,
+                         double* __restrict__ part) {
+    __shared__ double sa[RED_BLOCK], sb[RED_BLOCK];
+    double ma = 0.0, mb = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        ma = fmax(ma, fabs(a[i]));
+        mb = fmax(mb, fabs(b[i]));
+    }
+    sa[threadIdx.x] = ma;
+    sb[threadIdx.x] = mb;
+    __syncthreads();
+    for (int s = RED_BLOCK / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sa[threadIdx.x] = fmax(sa[threadIdx.x], sa[threadIdx.x + s]);
+            sb[threadIdx.x] = fmax(sb[threadIdx.x], sb[threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = sa[0];
+        part[2 * blockIdx.x + 1] = sb[0];
+    }
+}
+
+__global__ void k_maxfin(int nb, const double* __restrict__ part, double* __restrict__ out) {
+    double ma = 0.0, mb = 0.0;
+    for (int k = 0; k < nb; ++k) {
+        ma = fmax(ma, part[2 * k]);
+        mb = fmax(mb, part[2 * k + 1]);
+    }
+    out[0] = ma;
+    out[1] = mb;
+}
+
+// ---- free-surface elevation probes (greenfield) ------------------------------------
+__global__ void k_probe(int64_t n, State S, double R, int np, const double* __restrict__ xp,
+                        double* __restrict__ part) {
+    extern __shared__ double sh[];
+    double acc[16];
+    for (int k = 0; k < np; ++k) acc[k] = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        if (S.tid[i] != BSC_TID_FLUID) continue;
+        const double xi = S.x[i], vi = S.vol[i];
+        for (int k = 0; k < np; ++k) {
+            const double q = fabs(xi - xp[k]) / R;
+            if (q < 1.0) {
+                const double a = 1.0 - q;
+                acc[k] += vi * (1.25 / R) * (a * a * a) * (1.0 + 3.0 * q);
+            }
+        }
+    }
+    for (int k = 0; k < np; ++k) {
+        sh[threadIdx.x] = acc[k];
+        __syncthreads();
+        for (int s = RED_BLOCK / 2; s > 0; s >>= 1) {
+            if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) part[blockIdx.x * np + k] = sh[0];
+        __syncthreads();
+    }
+}
+
+int op_probe_eta(Ctx* c, int np, const double* xp, double depth, double* eta) {
+    if (np <= 0 || np > 16) return set_err(c, BSC_E_INVALID, "probe_eta: 1..16 probes");
+    double* dxp = c->tv;
+    BSC_CUDA(c, cudaMemcpyAsync(dxp, xp, sizeof(double) * np, cudaMemcpyHostToDevice, c->stream));
+    k_probe<<<RED_GRID, RED_BLOCK, RED_BLOCK * sizeof(double), c->stream>>>(c->n, c->S, 2 * c->K.h, np, dxp, c->part);
+    BSC_LAUNCH(c);
+    std::vector<double> h((size_t)RED_GRID * np);
+    BSC_CUDA(c, cudaMemcpyAsync(h.data(), c->part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int k = 0; k < np; ++k) {
+        double s = 0.0;
+        for (int b = 0; b < RED_GRID; ++b) s += h[(size_t)b * np + k];
+        eta[k] = s - depth;
+    }
+    return BSC_OK;
+}
+
+}  // namespace bsc
+
+namespace bsc {
+// max |vel| and max |nut| over all particles -> stepsc[0..1] (device)
+int op_timestep_reduce(Ctx* c) {
+    k_maxred<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(c->n, c->S.vel, c->S.nut, c->part);
+    BSC_LAUNCH(c);
+    k_maxfin<<<1, 1, 0, c->stream>>>(RED_GRID, c->part, c->stepsc);
+    BSC_LAUNCH(c);
+    return BSC_OK;
+}
+}  // namespace bsc

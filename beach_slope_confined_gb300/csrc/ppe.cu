@@ -1,0 +1,832 @@
+// ppe.cu -- pressure Poisson equation: assembly, SpMV, Krylov solvers.
+//
+// Assembly follows isph.f90:115-456 row by row: fluid rows use the row
+// particle's corrected gradient, ghost (tid 2) rows couple to walls only with
+// the raw gradient, fixed-wall (tid 1) rows use each fluid neighbour's
+// correction matrix and the row particle's m/rho; free-surface rows weight the
+// diagonal contributions of fluid neighbours by 1 + oden_j/(rho0*rel_den).
+// Each row is divided by its diagonal (the Jacobi scaling of :434-442), so the
+// stored matrix is I + N with N's values in the neighbour-list layout.
+//
+// Solvers: BiCGSTAB (the update order of solver.f90:163-213) and restarted
+// FGMRES(m) (the public algorithm behind the MKL call of solver.f90:319-343)
+// with classical Gram-Schmidt and one re-orthogonalisation pass.  All scalars
+// live on the device; each kernel starts by checking the `done` flag so the
+// host can queue a batch of iterations and test convergence once per batch.
+// Reductions are two-stage with a fixed grid, hence deterministic.
+//
+// Mixed precision: the pair sums of the assembly run in FP32, the inner
+// Krylov solve runs in FP32 with FP64 dot products and norms, and an FP64
+// iterative-refinement loop (true residual b - A x in FP64) drives the
+// relative residual to the requested tolerance.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "bsc_internal.cuh"
+
+namespace bsc {
+
+// ============================================================================
+// assembly
+// ============================================================================
+template <typename R>
+__global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
+                                                        const typename Vec2<R>::type* __restrict__ gw,
+                                                        const int32_t* __restrict__ cnt, R* __restrict__ aval,
+                                                        double* __restrict__ b, const double* __restrict__ q,
+                                                        const double* __restrict__ usx, const double* __restrict__ usy,
+                                                        double dt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int tid_i = S.tid[i];
+    const bool free_i = S.flags[i] & BSC_FLAG_FREE;
+    const double xi = S.x[i], yi = S.y[i];
+    const R ni = (R)S.por[i], rhoi = (R)S.rho[i], qi = (R)q[i];
+    const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+    const double usxi = usx[i], usyi = usy[i];
+    const R mi_over_rhoi = (R)(S.mass[i] / S.rho[i]);
+    const R lamp_f = (R)(1.0 / (K.rho0 * K.rel_den));
+    const int m = cnt[i];
+    R dia = 0, fv = 0;
+    for (int k = 0; k < m; ++k) {
+        const int64_t e = ell(i, k, K.kmax);
+        const int j = nbr[e];
+        const auto g = gw[e];
+        const int tid_j = S.tid[j];
+        const double dx = xi - S.x[j], dy = yi - S.y[j];
+        const R p_dist = (R)1 / ((R)(dx * dx + dy * dy) + (R)K.lam);
+        const R pvol = (R)S.vol[j];
+        R val = 0;
+        if (tid_i == BSC_TID_FLUID) {
+            const R lamp = (free_i && tid_j == BSC_TID_FLUID) ? (R)1 + (R)S.oden[j] * lamp_f : (R)1;
+            const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
+            const R t = (R)2 * pvol * ((R)dx * gx + (R)dy * gy) * p_dist;
+            val = -t;
+            dia += t * lamp;
+            // divergence of the porous-weighted predicted velocity (:241-270)
+            R ddx, ddy;
+            if (tid_j == BSC_TID_FLUID) {
+                const R nj = (R)S.por[j], rhoj = (R)S.rho[j], qj = (R)q[j];
+                const R rho_ij = (R)2 * rhoj * rhoi / (nj * ni) / (qj + qi);
+                ddx = rho_ij * (R)(usx[j] - usxi);
+                ddy = rho_ij * (R)(usy[j] - usyi);
+            } else {
+                ddx = qi * ((R)(S.vxs[j] - S.vxs[i]) / ni);
+                ddy = qi * ((R)(S.vys[j] - S.vys[i]) / ni);
+            }
+            fv += pvol * (ddx * gx + ddy * gy);
+        } else if (tid_i == BSC_TID_GHOST) {
+            if (tid_j <= 2) {
+                const R t = (R)2 * pvol * ((R)dx * g.x + (R)dy * g.y) * p_dist;
+                val = -t;
+                dia += t;
+            }
+        } else if (tid_i == BSC_TID_WALL) {
+            if (tid_j == BSC_TID_FLUID) {
+                const R Lj0 = (R)S.L0[j], Lj1 = (R)S.L1[j], Lj2 = (R)S.L2[j], Lj3 = (R)S.L3[j];
+                const R gx = Lj0 * g.x + Lj1 * g.y, gy = Lj2 * g.x + Lj3 * g.y;
+                const R t = (R)2 * mi_over_rhoi * ((R)dx * gx + (R)dy * gy) * p_dist;
+                val = -t;
+                dia += t;
+                const R qj = (R)q[j];
+                const R ddx = qj * (R)(usx[j] - S.vxs[i] / (double)ni);
+                const R ddy = qj * (R)(usy[j] - S.vys[i] / (double)ni);
+                fv += mi_over_rhoi * (ddx * gx + ddy * gy);
+            } else {
+                const R t = (R)2 * pvol * ((R)dx * g.x + (R)dy * g.y) * p_dist;
+                val = -t;
+                dia += t;
+            }
+        }
+        aval[e] = val;
+    }
+    const double d = (double)dia;
+    if (d == 0.0 || !isfinite(d)) {
+        // zero-neighbour guard: identity row, b = 0 (the reference divides by 0)
+        for (int k = 0; k < m; ++k) aval[ell(i, k, K.kmax)] = 0;
+        b[i] = 0.0;
+        return;
+    }
+    const R inv = (R)(1.0 / d);
+    for (int k = 0; k < m; ++k) {
+        const int64_t e = ell(i, k, K.kmax);
+        aval[e] = aval[e] * inv;
+    }
+    b[i] = ((double)fv / dt) / d;
+}
+
+__global__ void k_vs_over_por(int64_t n, State S, double* __restrict__ q, double* __restrict__ ux,
+                              double* __restrict__ uy) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double nn = S.por[i];
+    q[i] = S.rho[i] / nn;
+    ux[i] = S.vxs[i] / nn;
+    uy[i] = S.vys[i] / nn;
+}
+
+int op_ppe_assemble(Ctx* c) {
+    if (!c->have_lists) return set_err(c, BSC_E_INVALID, "ppesolve before neighbour");
+    double *q = c->s, *ux = c->tv, *uy = c->v;
+    k_vs_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, q, ux, uy);
+    BSC_LAUNCH(c);
+    const unsigned g = blocks_for(c->n, NB_BLOCK);
+    if (c->mixed)
+        k_assemble<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, c->avalf, c->b, q,
+                                                         ux, uy, c->dt);
+    else
+        k_assemble<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval, c->b, q,
+                                                          ux, uy, c->dt);
+    BSC_LAUNCH(c);
+    c->have_csr = true;
+    return BSC_OK;
+}
+
+// ============================================================================
+// operators: unit-diagonal ELL (the PPE) and general CSR (standalone solve)
+// ============================================================================
+template <typename T>
+struct EllOp {
+    const T* aval;
+    const int32_t* nbr;
+    const int32_t* cnt;
+    int kmax;
+    template <typename X, typename A>
+    __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
+        A s = (A)x[i];
+        const int m = cnt[i];
+        for (int k = 0; k < m; ++k) {
+            const int64_t e = ell(i, k, kmax);
+            s += (A)aval[e] * (A)x[nbr[e]];
+        }
+        return s;
+    }
+};
+
+struct CsrOp {
+    const int32_t* rp;
+    const int32_t* col;
+    const double* val;
+    template <typename X, typename A>
+    __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
+        A s = 0;
+        for (int k = rp[i]; k < rp[i + 1]; ++k) s += (A)val[k] * (A)x[col[k]];
+        return s;
+    }
+};
+
+// ============================================================================
+// reductions: RED_GRID blocks write partials; consumers reduce them in a
+// fixed order (deterministic for a given n)
+// ============================================================================
+template <int D>
+__device__ __forceinline__ void block_partials(double (&v)[D], double* __restrict__ part) {
+    __shared__ double sh[D][RED_BLOCK / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        double x = v[d];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[d][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            double x = (lane < RED_BLOCK / 32) ? sh[d][lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) part[d * RED_GRID + blockIdx.x] = x;
+        }
+    }
+}
+
+// every block reduces the partials itself (fixed order): no finalize launch
+template <int D>
+__device__ __forceinline__ void reduce_partials(const double* __restrict__ part, double (&out)[D]) {
+    __shared__ double sh[D][RED_BLOCK / 32];
+    __shared__ double res[D];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int d = 0; d < D; ++d) {
+        double x = 0.0;
+        for (int k = threadIdx.x; k < RED_GRID; k += blockDim.x) x += part[d * RED_GRID + k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) sh[d][w] = x;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+#pragma unroll
+        for (int d = 0; d < D; ++d) {
+            double x = (lane < RED_BLOCK / 32) ? sh[d][lane] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            if (lane == 0) res[d] = x;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int d = 0; d < D; ++d) out[d] = res[d];
+}
+
+#define GRID_LOOP(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+// ============================================================================
+// BiCGSTAB, value type T (double or float), dots accumulated in double
+// ============================================================================
+// r = b - A x; rhat = r; p = r; partials (r.r, b.b)
+template <typename Op, typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_bicg_init(int64_t n, Op A, const T* __restrict__ x,
+                                                          const T* __restrict__ b, T* __restrict__ r,
+                                                          T* __restrict__ rh, T* __restrict__ p,
+                                                          double* __restrict__ part) {
+    double acc[2] = {0.0, 0.0};
+    GRID_LOOP(i, n) {
+        const double ri = (double)b[i] - A.template row<T, double>(i, x);
+        const T rt = (T)ri;
+        r[i] = rt; rh[i] = rt; p[i] = rt;
+        acc[0] += (double)rt * (double)rt;
+        acc[1] += (double)b[i] * (double)b[i];
+    }
+    block_partials<2>(acc, part);
+}
+
+__global__ void k_bicg_setup(const double* __restrict__ part, Scalars* sc, double tol, int rel_r0) {
+    double v[2];
+    reduce_partials<2>(part, v);
+    if (threadIdx.x == 0) {
+        sc->rr = v[0];
+        sc->rhob[0] = v[0];
+        sc->bnorm = sqrt(v[1]);
+        sc->r0norm = sqrt(v[0]);
+        sc->target = tol * (rel_r0 ? sc->r0norm : sc->bnorm);
+        sc->done = (sc->r0norm <= sc->target) ? 1 : 0;
+        sc->breakdown = 0;
+        sc->it = 0;
+        sc->alpha = sc->omega = 1.0;
+    }
+}
+
+// v = A p; partial (rhat . v)
+template <typename Op, typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_bicg_1(int64_t n, Op A, const T* __restrict__ p, T* __restrict__ v,
+                                                       const T* __restrict__ rh, double* __restrict__ part,
+                                                       const Scalars* __restrict__ sc) {
+    if (sc->done | sc->breakdown) return;
+    double acc[1] = {0.0};
+    GRID_LOOP(i, n) {
+        const T vi = (T)A.template row<T, T>(i, p);
+        v[i] = vi;
+        acc[0] += (double)rh[i] * (double)vi;
+    }
+    block_partials<1>(acc, part);
+}
+
+// alpha = rho / (rhat.v); s = r - alpha v
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_bicg_2(int64_t n, const T* __restrict__ r, const T* __restrict__ v,
+                                                       T* __restrict__ s, const double* __restrict__ part,
+                                                       Scalars* sc, int par) {
+    if (sc->done | sc->breakdown) return;
+    double d[1];
+    reduce_partials<1>(part, d);
+    const double rho = sc->rhob[par];
+    if (d[0] == 0.0 || rho == 0.0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) sc->tmp[0] = 0.0;
+        return;
+    }
+    const double alpha = rho / d[0];
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->tmp[0] = alpha;
+    const T a = (T)alpha;
+    GRID_LOOP(i, n) s[i] = r[i] - a * v[i];
+}
+
+// t = A s; partials (t.s, t.t)
+template <typename Op, typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_bicg_3(int64_t n, Op A, const T* __restrict__ s, T* __restrict__ t,
+                                                       double* __restrict__ part, const Scalars* __restrict__ sc) {
+    if (sc->done | sc->breakdown) return;
+    double acc[2] = {0.0, 0.0};
+    GRID_LOOP(i, n) {
+        const T ti = (T)A.template row<T, T>(i, s);
+        t[i] = ti;
+        acc[0] += (double)ti * (double)s[i];
+        acc[1] += (double)ti * (double)ti;
+    }
+    block_partials<2>(acc, part + 2 * RED_GRID);
+}
+
+// omega = (t.s)/(t.t); x += alpha p + omega s; r = s - omega t; partials (r.r, rhat.r)
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_bicg_4(int64_t n, T* __restrict__ x, const T* __restrict__ p,
+                                                       const T* __restrict__ s, const T* __restrict__ t,
+                                                       T* __restrict__ r, const T* __restrict__ rh,
+                                                       double* __restrict__ part, Scalars* sc) {
+    if (sc->done | sc->breakdown) return;
+    double d[2];
+    reduce_partials<2>(part + 2 * RED_GRID, d);
+    const double alpha = sc->tmp[0];
+    if (alpha == 0.0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) sc->breakdown = 1;
+        return;
+    }
+    const double omega = (d[1] == 0.0) ? 0.0 : d[0] / d[1];
+    if (blockIdx.x == 0 && threadIdx.x == 0) sc->tmp[1] = omega;
+    const T a = (T)alpha, w = (T)omega;
+    double acc[2] = {0.0, 0.0};
+    GRID_LOOP(i, n) {
+        const T si = s[i];
+        x[i] = x[i] + a * p[i] + w * si;
+        const T ri = si - w * t[i];
+        r[i] = ri;
+        acc[0] += (double)ri * (double)ri;
+        acc[1] += (double)rh[i] * (double)ri;
+    }
+    block_partials<2>(acc, part + 4 * RED_GRID);
+}
+
+// convergence, beta, p = r + beta (p - omega v)
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_bicg_5(int64_t n, T* __restrict__ p, const T* __restrict__ r,
+                                                       const T* __restrict__ v, const double* __restrict__ part,
+                                                       Scalars* sc, int par, int it_next) {
+    if (sc->done | sc->breakdown) return;
+    double d[2];
+    reduce_partials<2>(part + 4 * RED_GRID, d);
+    // every block derives the same scalars; block 0 publishes them for the
+    // next kernels (rho goes to the other parity slot, never read here)
+    const double alpha = sc->tmp[0], omega = sc->tmp[1], rho = sc->rhob[par];
+    const double rn = sqrt(d[0]);
+    const bool conv = rn <= sc->target;
+    const bool brk = !conv && (omega == 0.0 || d[1] == 0.0);
+    const double beta = brk || conv ? 0.0 : (d[1] / rho) * (alpha / omega);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc->rr = d[0];
+        sc->rhob[par ^ 1] = d[1];
+        sc->it = it_next;
+        sc->done = conv ? 1 : 0;
+        sc->breakdown = brk ? 1 : 0;
+    }
+    if (conv || brk) return;
+    const T bt = (T)beta, w = (T)omega;
+    GRID_LOOP(i, n) p[i] = r[i] + bt * (p[i] - w * v[i]);
+}
+
+// ============================================================================
+// FGMRES(m) with CGS2, value type T, basis V[(m+1) x n], Hessenberg on device
+// ============================================================================
+// layout of Hd: H[(m+1)*m] | cs[m] | sn[m] | g[m+1] | y[m] | hcol[m+1] | ctl[4]
+struct FgLayout {
+    int m;
+    __host__ __device__ int H(int i, int j) const { return i * m + j; }
+    __host__ __device__ int cs(int k) const { return (m + 1) * m + k; }
+    __host__ __device__ int sn(int k) const { return (m + 1) * m + m + k; }
+    __host__ __device__ int g(int k) const { return (m + 1) * m + 2 * m + k; }
+    __host__ __device__ int y(int k) const { return (m + 1) * m + 3 * m + 1 + k; }
+    __host__ __device__ int hc(int k) const { return (m + 1) * m + 4 * m + 1 + k; }
+    __host__ __device__ int size() const { return (m + 1) * m + 5 * m + 2; }
+};
+
+// r = b - A x; partials (r.r, b.b)
+template <typename Op, typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_resid(int64_t n, Op A, const T* __restrict__ x,
+                                                      const T* __restrict__ b, T* __restrict__ r,
+                                                      double* __restrict__ part) {
+    double acc[2] = {0.0, 0.0};
+    GRID_LOOP(i, n) {
+        const double ri = (double)b[i] - A.template row<T, double>(i, x);
+        const T rt = (T)ri;
+        r[i] = rt;
+        acc[0] += ri * ri;
+        acc[1] += (double)b[i] * (double)b[i];
+    }
+    block_partials<2>(acc, part);
+}
+
+// cycle start: beta = ||r||; v0 = r/beta; g = beta e1; ctl: j = 0, cycle_done
+__global__ void k_fg_start(const double* __restrict__ part, Scalars* sc, double* Hd, FgLayout F, int first,
+                           double tol, int rel_r0) {
+    double v[2];
+    reduce_partials<2>(part, v);
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double beta = sqrt(v[0]);
+        if (first) {
+            sc->bnorm = sqrt(v[1]);
+            sc->r0norm = beta;
+            sc->target = tol * (rel_r0 ? beta : sc->bnorm);
+            sc->it = 0;
+            sc->breakdown = 0;
+        }
+        sc->rr = v[0];
+        sc->done = (beta <= sc->target) ? 1 : 0;
+        sc->tmp[0] = beta;  // scale for v0
+        sc->tmp[1] = 0.0;   // j (columns completed in this cycle)
+        sc->tmp[2] = 0.0;   // cycle finished flag
+        for (int k = 0; k <= F.m; ++k) Hd[F.g(k)] = 0.0;
+        Hd[F.g(0)] = beta;
+    }
+}
+
+template <typename T>
+__global__ void k_fg_v0(int64_t n, const T* __restrict__ r, T* __restrict__ V0, const Scalars* __restrict__ sc) {
+    if (sc->done) return;
+    const double inv = 1.0 / sc->tmp[0];
+    GRID_LOOP(i, n) V0[i] = (T)((double)r[i] * inv);
+}
+
+__device__ __forceinline__ bool fg_skip(const Scalars* sc) { return sc->done || sc->tmp[2] != 0.0; }
+
+// w = A v_j
+template <typename Op, typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_fg_spmv(int64_t n, Op A, const T* __restrict__ V, T* __restrict__ w,
+                                                        int j, const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    const T* vj = V + (int64_t)j * n;
+    GRID_LOOP(i, n) w[i] = (T)A.template row<T, T>(i, vj);
+}
+
+constexpr int FG_MAXM = 64;
+
+// partials of V_i . w for i = 0..j
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_fg_mdot(int64_t n, const T* __restrict__ V, const T* __restrict__ w,
+                                                        int j, double* __restrict__ part,
+                                                        const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    // up to j+1 <= FG_MAXM dots, 8 at a time to bound registers
+    for (int i0 = 0; i0 <= j; i0 += 8) {
+        double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int cntv = min(8, j + 1 - i0);
+        GRID_LOOP(k, n) {
+            const double wk = (double)w[k];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q < cntv) acc[q] += (double)V[(int64_t)(i0 + q) * n + k] * wk;
+        }
+        block_partials<8>(acc, part + (int64_t)i0 * RED_GRID);
+        __syncthreads();
+    }
+}
+
+// h(0..j) = reduced dots (added to column j of H on the second pass)
+__global__ void k_fg_hcol(const double* __restrict__ part, double* Hd, FgLayout F, int j, int accumulate,
+                          const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    // one warp per dot, fixed order
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = w; i <= j; i += nw) {
+        double x = 0.0;
+        for (int k = lane; k < RED_GRID; k += 32) x += part[(int64_t)i * RED_GRID + k];
+        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        if (lane == 0) {
+            Hd[F.hc(i)] = x;
+            Hd[F.H(i, j)] = accumulate ? Hd[F.H(i, j)] + x : x;
+        }
+    }
+}
+
+// w -= sum_i h_i V_i; partial (w.w) when `norm`
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_fg_maxpy(int64_t n, const T* __restrict__ V, T* __restrict__ w, int j,
+                                                         const double* __restrict__ Hd, FgLayout F, int norm,
+                                                         double* __restrict__ part, const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    __shared__ double h[FG_MAXM];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) h[i] = Hd[F.hc(i)];
+    __syncthreads();
+    double acc[1] = {0.0};
+    GRID_LOOP(k, n) {
+        double s = (double)w[k];
+        for (int i = 0; i <= j; ++i) s -= h[i] * (double)V[(int64_t)i * n + k];
+        const T st = (T)s;
+        w[k] = st;
+        acc[0] += (double)st * (double)st;
+    }
+    if (norm) block_partials<1>(acc, part);
+}
+
+// h(j+1,j) = ||w||; Givens; residual estimate; cycle/convergence control
+__global__ void k_fg_givens(const double* __restrict__ part, Scalars* sc, double* Hd, FgLayout F, int j) {
+    if (fg_skip(sc)) return;
+    double v[1];
+    reduce_partials<1>(part, v);
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double hn = sqrt(v[0]);
+    Hd[F.H(j + 1, j)] = hn;
+    for (int i = 0; i < j; ++i) {
+        const double a = Hd[F.H(i, j)], c = Hd[F.H(i + 1, j)];
+        Hd[F.H(i, j)] = Hd[F.cs(i)] * a + Hd[F.sn(i)] * c;
+        Hd[F.H(i + 1, j)] = -Hd[F.sn(i)] * a + Hd[F.cs(i)] * c;
+    }
+    const double a = Hd[F.H(j, j)], c = Hd[F.H(j + 1, j)];
+    const double den = sqrt(a * a + c * c);
+    sc->it += 1;
+    sc->tmp[1] = (double)(j + 1);
+    if (den == 0.0) {
+        sc->breakdown = 1;
+        sc->tmp[1] = (double)j;
+        sc->tmp[2] = 1.0;
+        return;
+    }
+    const double cs = a / den, sn = c / den;
+    Hd[F.cs(j)] = cs;
+    Hd[F.sn(j)] = sn;
+    Hd[F.H(j, j)] = den;
+    Hd[F.H(j + 1, j)] = 0.0;
+    const double gj = Hd[F.g(j)];
+    Hd[F.g(j + 1)] = -sn * gj;
+    Hd[F.g(j)] = cs * gj;
+    sc->tmp[3] = hn;  // scale of v_{j+1}
+    if (fabs(Hd[F.g(j + 1)]) <= sc->target || hn == 0.0 || j + 1 == F.m) sc->tmp[2] = 1.0;
+}
+
+// v_{j+1} = w / h(j+1,j)
+template <typename T>
+__global__ void k_fg_next(int64_t n, const T* __restrict__ w, T* __restrict__ V, int j, const Scalars* __restrict__ sc) {
+    if (sc->done || sc->tmp[2] != 0.0) return;
+    const double inv = 1.0 / sc->tmp[3];
+    T* vn = V + (int64_t)(j + 1) * n;
+    GRID_LOOP(i, n) vn[i] = (T)((double)w[i] * inv);
+}
+
+// y = H^-1 g over the completed columns
+__global__ void k_fg_backsolve(Scalars* sc, double* Hd, FgLayout F) {
+    if (sc->done) return;
+    const int k = (int)sc->tmp[1];
+    for (int i = k - 1; i >= 0; --i) {
+        double s = Hd[F.g(i)];
+        for (int q = i + 1; q < k; ++q) s -= Hd[F.H(i, q)] * Hd[F.y(q)];
+        Hd[F.y(i)] = s / Hd[F.H(i, i)];
+    }
+    for (int i = k; i < F.m; ++i) Hd[F.y(i)] = 0.0;
+}
+
+// x += sum_i y_i V_i
+template <typename T>
+__global__ void k_fg_update(int64_t n, T* __restrict__ x, const T* __restrict__ V, const double* __restrict__ Hd,
+                            FgLayout F, const Scalars* __restrict__ sc) {
+    if (sc->done) return;
+    __shared__ double y[FG_MAXM];
+    const int k = (int)sc->tmp[1];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) y[i] = Hd[F.y(i)];
+    __syncthreads();
+    GRID_LOOP(q, n) {
+        double s = (double)x[q];
+        for (int i = 0; i < k; ++i) s += y[i] * (double)V[(int64_t)i * n + q];
+        x[q] = (T)s;
+    }
+}
+
+// ============================================================================
+// host drivers
+// ============================================================================
+template <typename T>
+struct Work {
+    T *x, *b, *r, *rh, *p, *v, *s, *t, *V;
+};
+
+int fetch_scalars(Ctx* c) {
+    BSC_CUDA(c, cudaMemcpyAsync(c->h_sc, c->sc, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BSC_OK;
+}
+
+constexpr int BATCH = 8;
+
+template <typename Op, typename T>
+int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_r0, int maxit, int* iters,
+                 double* rr_out) {
+    const int G = RED_GRID, B = RED_BLOCK;
+    k_bicg_init<Op, T><<<G, B, 0, c->stream>>>(n, A, w.x, w.b, w.r, w.rh, w.p, c->part);
+    BSC_LAUNCH(c);
+    k_bicg_setup<<<1, B, 0, c->stream>>>(c->part, c->sc, tol, rel_r0);
+    BSC_LAUNCH(c);
+    int launched = 0;
+    for (;;) {
+        int rc = fetch_scalars(c);
+        if (rc) return rc;
+        const Scalars& h = *c->h_sc;
+        if (h.done || h.breakdown || h.it >= maxit || launched >= maxit) break;
+        const int nb = std::min(BATCH, maxit - h.it);
+        for (int q = 0; q < nb; ++q) {
+            const int g = h.it + q, par = g & 1;  // iterations run in order until done
+            k_bicg_1<Op, T><<<G, B, 0, c->stream>>>(n, A, w.p, w.v, w.rh, c->part, c->sc);
+            k_bicg_2<T><<<G, B, 0, c->stream>>>(n, w.r, w.v, w.s, c->part, c->sc, par);
+            k_bicg_3<Op, T><<<G, B, 0, c->stream>>>(n, A, w.s, w.t, c->part, c->sc);
+            k_bicg_4<T><<<G, B, 0, c->stream>>>(n, w.x, w.p, w.s, w.t, w.r, w.rh, c->part, c->sc);
+            k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->part, c->sc, par, g + 1);
+            c->launches += 5;
+        }
+        launched += nb;
+        BSC_CUDA(c, cudaGetLastError());
+    }
+    *iters = c->h_sc->it;
+    *rr_out = c->h_sc->rr;
+    return c->h_sc->breakdown && !c->h_sc->done ? BSC_E_BREAKDOWN : BSC_OK;
+}
+
+template <typename Op, typename T>
+int run_fgmres(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_r0, int maxit, int m, int* iters,
+               double* rr_out) {
+    const int G = RED_GRID, B = RED_BLOCK;
+    FgLayout F{m};
+    int first = 1;
+    T* wv = w.t;
+    for (;;) {
+        k_resid<Op, T><<<G, B, 0, c->stream>>>(n, A, w.x, w.b, w.r, c->part);
+        BSC_LAUNCH(c);
+        k_fg_start<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, first, tol, rel_r0);
+        BSC_LAUNCH(c);
+        first = 0;
+        int rc = fetch_scalars(c);
+        if (rc) return rc;
+        if (c->h_sc->done || c->h_sc->it >= maxit) break;
+        k_fg_v0<T><<<G, B, 0, c->stream>>>(n, w.r, w.V, c->sc);
+        BSC_LAUNCH(c);
+        const int mm = std::min(m, maxit - c->h_sc->it);
+        for (int j = 0; j < mm; ++j) {
+            k_fg_spmv<Op, T><<<G, B, 0, c->stream>>>(n, A, w.V, wv, j, c->sc);
+            for (int pass = 0; pass < 2; ++pass) {
+                k_fg_mdot<T><<<G, B, 0, c->stream>>>(n, w.V, wv, j, c->part, c->sc);
+                k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc);
+                k_fg_maxpy<T><<<G, B, 0, c->stream>>>(n, w.V, wv, j, c->Hd, F, pass, c->part, c->sc);
+                c->launches += 3;
+            }
+            k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, j);
+            k_fg_next<T><<<G, B, 0, c->stream>>>(n, wv, w.V, j, c->sc);
+            c->launches += 3;
+        }
+        BSC_LAUNCH(c);
+        k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc, c->Hd, F);
+        k_fg_update<T><<<G, B, 0, c->stream>>>(n, w.x, w.V, c->Hd, F, c->sc);
+        c->launches += 2;
+        BSC_LAUNCH(c);
+        rc = fetch_scalars(c);
+        if (rc) return rc;
+        if (c->h_sc->breakdown && c->h_sc->tmp[1] == 0.0) break;
+    }
+    *iters = c->h_sc->it;
+    *rr_out = c->h_sc->rr;
+    return BSC_OK;
+}
+
+// FP64 true residual of the FP32-valued unit-diagonal matrix: r = b - A x
+__global__ void __launch_bounds__(RED_BLOCK) k_ir_resid(int64_t n, EllOp<float> A, const double* __restrict__ x,
+                                                         const double* __restrict__ b, double* __restrict__ r,
+                                                         float* __restrict__ rf, double* __restrict__ part) {
+    double acc[2] = {0.0, 0.0};
+    GRID_LOOP(i, n) {
+        const double ri = b[i] - A.template row<double, double>(i, x);
+        r[i] = ri;
+        rf[i] = (float)ri;
+        acc[0] += ri * ri;
+        acc[1] += b[i] * b[i];
+    }
+    block_partials<2>(acc, part);
+}
+
+__global__ void k_ir_norms(const double* __restrict__ part, double* out) {
+    double v[2];
+    reduce_partials<2>(part, v);
+    if (threadIdx.x == 0) {
+        out[0] = sqrt(v[0]);
+        out[1] = sqrt(v[1]);
+    }
+}
+
+__global__ void k_ir_add(int64_t n, double* __restrict__ x, const float* __restrict__ d) {
+    GRID_LOOP(i, n) x[i] += (double)d[i];
+}
+
+__global__ void k_copy_f64(int64_t n, const double* __restrict__ a, double* __restrict__ b) {
+    GRID_LOOP(i, n) b[i] = a[i];
+}
+
+int solve_status(bsc_solve_info* info, int rc) {
+    if (rc != BSC_OK) return rc;
+    return info->converged ? BSC_OK : BSC_E_NOT_CONVERGED;
+}
+
+// x <- solution of the PPE, warm-started from the current pressure
+int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
+    if (!c->have_csr) return set_err(c, BSC_E_INVALID, "ppe solve before assembly");
+    const int64_t n = c->n;
+    const bsc_params& P = c->P;
+    const int rel_r0 = P.tol_mode == BSC_TOL_REL_R0;
+    bsc_solve_info loc{};
+    bsc_solve_info* si = info ? info : &loc;
+    *si = bsc_solve_info{};
+    int rc = BSC_OK, iters = 0;
+    double rr = 0.0;
+    if (!c->mixed) {
+        EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax};
+        Work<double> w{c->S.p, c->b, c->r, c->rh, c->pd, c->v, c->s, c->tv, c->V};
+        if (P.solver == BSC_SOLVER_FGMRES)
+            rc = run_fgmres<EllOp<double>, double>(c, n, A, w, P.tol, rel_r0, P.maxit, c->fg_m, &iters, &rr);
+        else
+            rc = run_bicgstab<EllOp<double>, double>(c, n, A, w, P.tol, rel_r0, P.maxit, &iters, &rr);
+        if (rc) return rc;
+        // true residual of the returned pressure
+        k_resid<EllOp<double>, double><<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, A, c->S.p, c->b, c->r, c->part);
+        BSC_LAUNCH(c);
+        k_ir_norms<<<1, RED_BLOCK, 0, c->stream>>>(c->part, c->Hd + FgLayout{c->fg_m}.size());
+        BSC_LAUNCH(c);
+        double nrm[2];
+        BSC_CUDA(c, cudaMemcpyAsync(nrm, c->Hd + FgLayout{c->fg_m}.size(), 2 * sizeof(double), cudaMemcpyDeviceToHost,
+                                    c->stream));
+        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+        si->iterations = iters;
+        si->outer = 1;
+        si->b_norm = c->h_sc->bnorm;
+        si->r0_norm = c->h_sc->r0norm;
+        si->rel_residual = nrm[1] > 0 ? nrm[0] / nrm[1] : nrm[0];
+        const double ref = rel_r0 ? si->r0_norm : si->b_norm;
+        si->converged = (c->h_sc->done != 0) || (nrm[0] <= P.tol * ref);
+        si->status = c->h_sc->breakdown && !si->converged ? BSC_E_BREAKDOWN
+                     : (si->converged ? BSC_OK : BSC_E_NOT_CONVERGED);
+        return si->status;
+    }
+    // ---- mixed: FP64 iterative refinement around an FP32 inner solve
+    EllOp<float> Af{c->avalf, c->nbr, c->cnt, c->K.kmax};
+    double* x = c->S.p;
+    double* r64 = c->r;
+    double* norms = c->Hd + FgLayout{c->fg_m}.size();
+    double r0 = -1.0, bn = 0.0, rn = 0.0;
+    int outer = 0, total = 0, st = BSC_OK;
+    bool conv = false;
+    for (;;) {
+        k_ir_resid<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, Af, x, c->b, r64, c->rf, c->part);
+        BSC_LAUNCH(c);
+        k_ir_norms<<<1, RED_BLOCK, 0, c->stream>>>(c->part, norms);
+        BSC_LAUNCH(c);
+        double nrm[2];
+        BSC_CUDA(c, cudaMemcpyAsync(nrm, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+        rn = nrm[0];
+        bn = nrm[1];
+        if (r0 < 0) r0 = rn;
+        const double target = P.tol * (rel_r0 ? r0 : bn);
+        if (rn <= target) { conv = true; break; }
+        if (outer >= P.max_outer || total >= P.maxit) break;
+        ++outer;
+        // inner: A d = r (FP32), d0 = 0, relative tolerance inner_tol
+        BSC_CUDA(c, cudaMemsetAsync(c->xf, 0, sizeof(float) * n, c->stream));
+        // FP32 work: x = correction, b = residual, then r, rhat, p, v, s, t
+        Work<float> w{c->xf, c->rf, c->sf, c->rhf, c->pf, c->vf, c->tf, c->bf, c->Vf};
+        int it = 0;
+        double rri = 0;
+        const int budget = P.maxit - total;
+        int rc2 = (P.solver == BSC_SOLVER_FGMRES)
+                      ? run_fgmres<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, c->fg_m, &it, &rri)
+                      : run_bicgstab<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, &it, &rri);
+        total += it;
+        if (rc2 == BSC_E_BREAKDOWN && it == 0) { st = BSC_E_BREAKDOWN; break; }
+        k_ir_add<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, x, c->xf);
+        BSC_LAUNCH(c);
+    }
+    si->iterations = total;
+    si->outer = outer;
+    si->converged = conv ? 1 : 0;
+    si->b_norm = bn;
+    si->r0_norm = r0;
+    si->rel_residual = bn > 0 ? rn / bn : rn;
+    si->status = conv ? BSC_OK : (st != BSC_OK ? st : BSC_E_NOT_CONVERGED);
+    return si->status;
+}
+
+// ---- standalone CSR solve (device buffers allocated by the caller context) ----
+int csr_solve_device(Ctx* c, int32_t n, const int32_t* rp, const int32_t* col, const double* val, const double* b,
+                     double* x, bsc_solve_info* info) {
+    CsrOp A{rp, col, val};
+    double* work = c->r;  // [r rh p v s t] laid out by the caller
+    Work<double> w{x, const_cast<double*>(b), work, work + n, work + 2 * n, work + 3 * n, work + 4 * n, work + 5 * n,
+                   c->V};
+    const bsc_params& P = c->P;
+    const int rel_r0 = P.tol_mode == BSC_TOL_REL_R0;
+    int iters = 0;
+    double rr = 0;
+    int rc = (P.solver == BSC_SOLVER_FGMRES)
+                 ? run_fgmres<CsrOp, double>(c, n, A, w, P.tol, rel_r0, P.maxit, c->fg_m, &iters, &rr)
+                 : run_bicgstab<CsrOp, double>(c, n, A, w, P.tol, rel_r0, P.maxit, &iters, &rr);
+    if (rc) return rc;
+    k_resid<CsrOp, double><<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, A, x, b, work, c->part);
+    BSC_LAUNCH(c);
+    double* norms = c->Hd + FgLayout{c->fg_m}.size();
+    k_ir_norms<<<1, RED_BLOCK, 0, c->stream>>>(c->part, norms);
+    BSC_LAUNCH(c);
+    double nrm[2];
+    BSC_CUDA(c, cudaMemcpyAsync(nrm, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    info->iterations = iters;
+    info->outer = 1;
+    info->b_norm = c->h_sc->bnorm;
+    info->r0_norm = c->h_sc->r0norm;
+    info->rel_residual = nrm[1] > 0 ? nrm[0] / nrm[1] : nrm[0];
+    const double ref = rel_r0 ? info->r0_norm : info->b_norm;
+    info->converged = (c->h_sc->done != 0) || nrm[0] <= P.tol * ref;
+    info->status = info->converged ? BSC_OK : (c->h_sc->breakdown ? BSC_E_BREAKDOWN : BSC_E_NOT_CONVERGED);
+    return info->status;
+}
+
+int fg_layout_size(int m) { return FgLayout{m}.size() + 8; }
+
+}  // namespace bsc

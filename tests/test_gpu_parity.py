@@ -1,0 +1,169 @@
+"""CUDA path against the CPU oracle, routine by routine (FP64).
+
+Each test uploads the same seeded tank to both, runs the reference's routines
+in main.f90 order and compares what each routine produced:
+  * neighbour sets bit-exact (sorted id sets per particle);
+  * FP64 fields within 1e-11 (normwise, max|a-b|/max|b|): the two sides add
+    the same terms in a different order and the CUDA side contracts to FMA;
+  * the pressure after the solve within 1e-9 (both solve to 1e-12).
+"""
+import numpy as np
+import pytest
+
+from beach_slope_confined_gb300 import Solver, scenario as sc, solve_csr
+from pairrun import advance_to_lists, make_pair, rel_err, rel_l2, small_spec, sprinkle_flags
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-11
+
+
+def _pair(kernel=1, dx=0.02, flags=False, solver="bicgstab", **kw):
+    spec = small_spec(dx=dx, kernel=kernel)
+    scen = sc.build(spec)
+    if flags:
+        sprinkle_flags(scen)
+    P = sc.make_params(spec, scen.bounds, solver=solver, tol=1e-12, maxit=20000, **kw)
+    if kernel == 0:
+        P.csh = 0.5
+    g, c = make_pair(scen, P, Solver)
+    return spec, scen, g, c
+
+
+@pytest.mark.parametrize("kernel", [1, 0])
+def test_neighbour_sets_bit_exact(kernel):
+    _, scen, g, c = _pair(kernel=kernel)
+    advance_to_lists((g, c))
+    og, ig = g.get_neighbors()
+    oc, ic = c.get_neighbors()
+    assert np.array_equal(og, oc)
+    assert np.array_equal(ig, ic)
+    a, b = g.download_state(), c.download_state()
+    assert np.array_equal(a["flags"], b["flags"])
+    assert rel_err(a["gradvx"], b["gradvx"]) < FIELD_TOL
+    assert rel_err(a["L"], b["L"]) < 1e-10
+
+
+@pytest.mark.parametrize("kernel,flags", [(1, False), (1, True), (0, True)])
+def test_routines_in_step_order(kernel, flags):
+    spec, scen, g, c = _pair(kernel=kernel, flags=flags)
+    both = (g, c)
+    advance_to_lists(both)
+    for ctx in both:
+        ctx.effpor()
+    a, b = g.download_state(), c.download_state()
+    for f in ("porosity", "rho", "resist"):
+        assert rel_err(a[f], b[f]) < FIELD_TOL, f
+    for ctx in both:
+        ctx.eddyvis()
+    a, b = g.download_state(), c.download_state()
+    for f in ("nut", "tke"):
+        assert rel_err(a[f], b[f]) < 1e-9, f
+    for ctx in both:
+        ctx.int_vel()
+    a, b = g.download_state(), c.download_state()
+    for f in ("vxs", "vys"):
+        assert rel_err(a[f], b[f]) < FIELD_TOL, f
+    free = (b["flags"] & sc.FLAG_FREE) != 0
+    assert rel_err(a["varts"][free], b["varts"][free]) < 1e-9
+    ig = g.ppesolve()
+    ic = c.ppesolve()
+    assert ig.converged and ic.converged
+    rg, cg, vg, bg = g.export_csr()
+    rc_, cc, vc, bc = c.export_csr()
+    assert np.array_equal(rg, rc_) and np.array_equal(cg, cc)
+    assert rel_err(vg, vc) < 1e-10
+    assert rel_err(bg, bc) < 1e-9
+    a, b = g.download_state(), c.download_state()
+    assert rel_l2(a["p"], b["p"]) < 1e-9
+    for ctx in both:
+        ctx.comp_vel()
+        ctx.comp_pos()
+    a, b = g.download_state(), c.download_state()
+    for f in ("vx", "vy", "vel"):
+        assert rel_err(a[f], b[f]) < 1e-8, f
+    for f in ("x", "y"):
+        assert rel_err(a[f], b[f]) < 1e-13, f
+    for ctx in both:
+        ctx.cellshift(alt=True)
+        ctx.neighbour()
+        ctx.freesurf()
+        ctx.effpor()
+    og, ig2 = g.get_neighbors()
+    oc, ic2 = c.get_neighbors()
+    assert np.array_equal(og, oc) and np.array_equal(ig2, ic2)
+    a, b = g.download_state(), c.download_state()
+    assert np.array_equal(a["flags"], b["flags"])
+    for ctx in both:
+        ctx.opt2_shift()
+    a, b = g.download_state(), c.download_state()
+    for f in ("x", "y"):
+        assert rel_err(a[f], b[f]) < 1e-13, f
+    for f in ("vx", "vy"):
+        assert rel_err(a[f], b[f]) < 1e-8, f
+    dtg, dtc = g.timestep(), c.timestep()
+    assert dtg == dtc
+
+
+@pytest.mark.parametrize("solver", ["bicgstab", "fgmres"])
+def test_steps_against_oracle(solver):
+    spec, scen, g, c = _pair(solver=solver)
+    for ctx in (g, c):
+        ctx.step(5)
+    a, b = g.download_state(), c.download_state()
+    for f in ("x", "y"):
+        assert rel_l2(a[f], b[f]) < 1e-12, f
+    for f in ("vx", "vy", "p"):
+        assert rel_l2(a[f], b[f]) < 1e-7, f
+
+
+def test_reorder_keeps_results():
+    """A Morton reorder every cell shift gives the same physics as every 20."""
+    spec = small_spec()
+    scen = sc.build(spec)
+    out = []
+    for every in (1, 20):
+        P = sc.make_params(spec, scen.bounds, tol=1e-12, maxit=20000, reorder_every=every)
+        g, _ = make_pair(scen, P, Solver)
+        g.step(4)
+        out.append(g.download_state())
+    for f in ("x", "y", "vx", "vy", "p"):
+        assert rel_l2(out[0][f], out[1][f]) < 1e-9, f
+
+
+KAT_ROWPTR = [0, 3, 5, 7, 10, 13]
+KAT_COL = [0, 2, 3, 1, 3, 0, 2, 1, 2, 3, 0, 1, 4]
+KAT_B = [8.0, 6.0, 4.0, 9.0, 8.0]
+
+
+@pytest.mark.parametrize("solver", ["bicgstab", "fgmres"])
+def test_csr_solve_known_answer(solver):
+    """solvertest.f90:10-19: unit values on the given pattern, solution 1..5."""
+    spec = small_spec()
+    P = sc.make_params(spec, solver=solver, tol=1e-12, maxit=100, restart=5)
+    rc, x, info = solve_csr(P, KAT_ROWPTR, KAT_COL, np.ones(13), KAT_B, np.ones(5))
+    assert rc == 0 and info.converged
+    assert np.allclose(x, [1, 2, 3, 4, 5], rtol=0, atol=1e-9)
+
+
+def test_probe_eta_matches_oracle():
+    spec, scen, g, c = _pair()
+    xp = np.array(spec.probes)
+    eg, ec = g.probe_eta(xp, spec.depth), c.probe_eta(xp, spec.depth)
+    assert np.allclose(eg, ec, rtol=0, atol=1e-12)
+    assert np.all(np.abs(ec) < 0.02)  # still water: the column integral is the depth
+
+
+def test_capacity_overflow_is_reported():
+    spec = small_spec()
+    scen = sc.build(spec)
+    P = sc.make_params(spec, scen.bounds, max_neighbors=8)
+    g = Solver(P)
+    from beach_slope_confined_gb300 import BscError, setup_tank
+
+    setup_tank(g, scen, initial_effpor=False)
+    g.projection()
+    g.cellshift()
+    with pytest.raises(BscError) as e:
+        g.neighbour()
+    assert e.value.code == -4
