@@ -173,6 +173,12 @@ static int setup_grid(Ctx* c, const double* hx, const double* hy, int64_t n) {
     K.gy0 = ymin - K.cs;
     const double nxd = std::ceil((xmax - K.gx0) / K.cs) + 1, nyd = std::ceil((ymax - K.gy0) / K.cs) + 1;
     if (!(nxd * nyd < 16.0e6)) return set_err(c, BSC_E_CAPACITY, "cell grid larger than 16M cells");
+    const bool same = c->ncell > 0 && K.nx == (int)nxd && K.ny == (int)nyd && c->grid_x0 == K.gx0 &&
+                      c->grid_y0 == K.gy0;
+    if (same) return BSC_OK;  // re-upload on the same grid: ranks and solid lists stay valid
+    c->grid_x0 = K.gx0;
+    c->grid_y0 = K.gy0;
+    c->solids_dirty = true;
     K.nx = (int)nxd;
     K.ny = (int)nyd;
     const int ncell = K.nx * K.ny;
@@ -193,9 +199,9 @@ static int setup_grid(Ctx* c, const double* hx, const double* hy, int64_t n) {
     std::iota(ord.begin(), ord.end(), 0);
     std::sort(ord.begin(), ord.end(), [&](int a, int b) { return code[a] < code[b]; });
     for (int q = 0; q < ncell; ++q) rank[ord[q]] = q;
-    BSC_CUDA(c, cudaMemcpy(c->cell_rank, rank.data(), sizeof(int32_t) * ncell, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemset(c->scell_start, 0, sizeof(int32_t) * ncell));
-    BSC_CUDA(c, cudaMemset(c->scell_count, 0, sizeof(int32_t) * ncell));
+    BSC_H2D(c, c->cell_rank, rank.data(), sizeof(int32_t) * ncell);
+    BSC_MEMSET(c, c->scell_start, 0, sizeof(int32_t) * ncell);
+    BSC_MEMSET(c, c->scell_count, 0, sizeof(int32_t) * ncell);
     return BSC_OK;
 }
 
@@ -356,6 +362,9 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
 int bsc_destroy(bsc_ctx* c) {
     if (!c) return BSC_OK;
     free_all(c);
+    for (void* p : c->pallocs)
+        if (p) cudaFree(p);
+    c->pallocs.clear();
     for (int k = 0; k < 2 * Ctx::EVPOOL; ++k)
         if (c->evs[k]) cudaEventDestroy(c->evs[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -402,7 +411,7 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
             BSC_CUDA(c, cudaMemsetAsync(d, 0, sizeof(double) * n, c->stream));
         } else {
             std::vector<double> tmp(n, dflt);
-            BSC_CUDA(c, cudaMemcpy(d, tmp.data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+            BSC_H2D(c, d, tmp.data(), sizeof(double) * n);
         }
         return BSC_OK;
     };
@@ -420,7 +429,7 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
         for (int64_t i = 0; i < n; ++i)
             for (int q = 0; q < 4; ++q) l[q][i] = s->L[4 * i + q];
         double* d[4] = {S.L0, S.L1, S.L2, S.L3};
-        for (int q = 0; q < 4; ++q) BSC_CUDA(c, cudaMemcpy(d[q], l[q].data(), sizeof(double) * n, cudaMemcpyHostToDevice));
+        for (int q = 0; q < 4; ++q) BSC_H2D(c, d[q], l[q].data(), sizeof(double) * n);
     } else {
         if ((rc = up(S.L0, nullptr, 1.0)) || (rc = up(S.L1, nullptr, 0)) || (rc = up(S.L2, nullptr, 0)) ||
             (rc = up(S.L3, nullptr, 1.0)))
@@ -443,8 +452,9 @@ int bsc_upload_porosity(bsc_ctx* c, int32_t nx, int32_t ny, double x0, double y0
     CTX_GUARD(c);
     if (nx <= 0 || ny <= 0 || !v || !(dx > 0) || !(dy > 0)) return set_err(c, BSC_E_INVALID, "upload_porosity");
     int rc;
-    if ((rc = dalloc(c, &c->pgrid, (int64_t)nx * ny))) return rc;
-    BSC_CUDA(c, cudaMemcpy(c->pgrid, v, sizeof(double) * nx * ny, cudaMemcpyHostToDevice));
+    if ((rc = palloc(c, &c->pgrid, (int64_t)nx * ny))) return rc;
+    BSC_H2D(c, c->pgrid, v, sizeof(double) * nx * ny);
+    c->hpgrid.assign(v, v + (int64_t)nx * ny);
     c->K.pnx = nx; c->K.pny = ny; c->K.px0 = x0; c->K.py0 = y0; c->K.pdx = dx; c->K.pdy = dy;
     c->K.pgrid = c->pgrid;
     return BSC_OK;
@@ -457,8 +467,8 @@ int bsc_upload_solids(bsc_ctx* c, int64_t ns, const double* x, const double* y, 
     c->ns = ns;
     if (ns == 0) return BSC_OK;
     int rc;
-    if ((rc = dalloc(c, &c->sx, ns)) || (rc = dalloc(c, &c->sy, ns)) || (rc = dalloc(c, &c->svol, ns)) ||
-        (rc = dalloc(c, &c->spor, ns)))
+    if ((rc = palloc(c, &c->sx, ns)) || (rc = palloc(c, &c->sy, ns)) || (rc = palloc(c, &c->svol, ns)) ||
+        (rc = palloc(c, &c->spor, ns)))
         return rc;
     std::vector<double> vol(ns), sp(ns);
     const KParams& K = c->K;
@@ -470,22 +480,16 @@ int bsc_upload_solids(bsc_ctx* c, int64_t ns, const double* x, const double* y, 
             // same lookup as the fluid-side cap (porosity_at in pairs.cu)
             double fx = std::floor((x[k] - K.px0) / K.pdx), fy = std::floor((y[k] - K.py0) / K.pdy);
             bool in = fx >= 0 && fx < K.pnx && fy >= 0 && fy < K.pny;
-            std::vector<double> g;
-            sp[k] = K.por;
-            if (in) {
-                double val;
-                BSC_CUDA(c, cudaMemcpy(&val, c->pgrid + (int64_t)fy * K.pnx + (int64_t)fx, sizeof(double),
-                                       cudaMemcpyDeviceToHost));
-                sp[k] = val;
-            }
+            sp[k] = in ? c->hpgrid[(int64_t)fy * K.pnx + (int64_t)fx] : K.por;
         } else {
             sp[k] = K.por;
         }
     }
-    BSC_CUDA(c, cudaMemcpy(c->sx, x, sizeof(double) * ns, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemcpy(c->sy, y, sizeof(double) * ns, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemcpy(c->svol, vol.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemcpy(c->spor, sp.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
+    BSC_H2D(c, c->sx, x, sizeof(double) * ns);
+    BSC_H2D(c, c->sy, y, sizeof(double) * ns);
+    BSC_H2D(c, c->svol, vol.data(), sizeof(double) * ns);
+    BSC_H2D(c, c->spor, sp.data(), sizeof(double) * ns);
+    c->solids_dirty = true;
     if (c->ncell > 0) return solids_build(c);
     return BSC_OK;
 }
@@ -673,15 +677,15 @@ int bsc_get_neighbors(bsc_ctx* c, int64_t* offsets, int32_t* ids) {
     const int64_t n = c->n, kmax = c->K.kmax, slots = ((n + 31) / 32) * 32 * kmax;
     std::vector<int32_t> cnt(n), id(n), nb;
     BSC_CUDA(c, cudaStreamSynchronize(c->stream));
-    BSC_CUDA(c, cudaMemcpy(cnt.data(), c->cnt, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
-    BSC_CUDA(c, cudaMemcpy(id.data(), c->S.id, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    BSC_D2H(c, cnt.data(), c->cnt, sizeof(int32_t) * n);
+    BSC_D2H(c, id.data(), c->S.id, sizeof(int32_t) * n);
     std::vector<int64_t> slot_of(n);
     for (int64_t k = 0; k < n; ++k) slot_of[id[k]] = k;
     offsets[0] = 0;
     for (int64_t q = 0; q < n; ++q) offsets[q + 1] = offsets[q] + cnt[slot_of[q]];
     if (!ids) return BSC_OK;
     nb.resize(slots);
-    BSC_CUDA(c, cudaMemcpy(nb.data(), c->nbr, sizeof(int32_t) * slots, cudaMemcpyDeviceToHost));
+    BSC_D2H(c, nb.data(), c->nbr, sizeof(int32_t) * slots);
     for (int64_t q = 0; q < n; ++q) {
         const int64_t k = slot_of[q];
         int32_t* dst = ids + offsets[q];
@@ -698,27 +702,27 @@ int bsc_export_csr(bsc_ctx* c, int64_t* rowptr, int32_t* col, double* val, doubl
     const int64_t n = c->n, kmax = c->K.kmax, slots = ((n + 31) / 32) * 32 * kmax;
     std::vector<int32_t> cnt(n), id(n);
     BSC_CUDA(c, cudaStreamSynchronize(c->stream));
-    BSC_CUDA(c, cudaMemcpy(cnt.data(), c->cnt, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
-    BSC_CUDA(c, cudaMemcpy(id.data(), c->S.id, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+    BSC_D2H(c, cnt.data(), c->cnt, sizeof(int32_t) * n);
+    BSC_D2H(c, id.data(), c->S.id, sizeof(int32_t) * n);
     std::vector<int64_t> slot_of(n);
     for (int64_t k = 0; k < n; ++k) slot_of[id[k]] = k;
     rowptr[0] = 0;
     for (int64_t q = 0; q < n; ++q) rowptr[q + 1] = rowptr[q] + cnt[slot_of[q]] + 1;
     if (rhs) {
         std::vector<double> b(n);
-        BSC_CUDA(c, cudaMemcpy(b.data(), c->b, sizeof(double) * n, cudaMemcpyDeviceToHost));
+        BSC_D2H(c, b.data(), c->b, sizeof(double) * n);
         for (int64_t q = 0; q < n; ++q) rhs[q] = b[slot_of[q]];
     }
     if (!col && !val) return BSC_OK;
     std::vector<int32_t> nb(slots);
     std::vector<double> v(slots);
-    BSC_CUDA(c, cudaMemcpy(nb.data(), c->nbr, sizeof(int32_t) * slots, cudaMemcpyDeviceToHost));
+    BSC_D2H(c, nb.data(), c->nbr, sizeof(int32_t) * slots);
     if (c->mixed) {
         std::vector<float> vf(slots);
-        BSC_CUDA(c, cudaMemcpy(vf.data(), c->avalf, sizeof(float) * slots, cudaMemcpyDeviceToHost));
+        BSC_D2H(c, vf.data(), c->avalf, sizeof(float) * slots);
         for (int64_t e = 0; e < slots; ++e) v[e] = vf[e];
     } else {
-        BSC_CUDA(c, cudaMemcpy(v.data(), c->aval, sizeof(double) * slots, cudaMemcpyDeviceToHost));
+        BSC_D2H(c, v.data(), c->aval, sizeof(double) * slots);
     }
     std::vector<std::pair<int32_t, double>> row;
     for (int64_t q = 0; q < n; ++q) {
@@ -791,14 +795,19 @@ int bsc_csr_solve(const bsc_params* p, int32_t n, const int32_t* rowptr, const i
     if (!rc) rc = dalloc(&c, &db, n);
     if (!rc) rc = dalloc(&c, &dx, n);
     if (!rc) {
-        cudaMemcpy(drp, rowptr, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice);
-        cudaMemcpy(dcol, col, sizeof(int32_t) * nnz, cudaMemcpyHostToDevice);
-        cudaMemcpy(dval, val, sizeof(double) * nnz, cudaMemcpyHostToDevice);
-        cudaMemcpy(db, b, sizeof(double) * n, cudaMemcpyHostToDevice);
-        cudaMemcpy(dx, x, sizeof(double) * n, cudaMemcpyHostToDevice);
-        rc = csr_solve_device(&c, n, drp, dcol, dval, db, dx, info);
-        if (rc == BSC_OK || rc == BSC_E_NOT_CONVERGED || rc == BSC_E_BREAKDOWN)
-            cudaMemcpy(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost);
+        auto up = [&](void* d, const void* h, size_t bytes) {
+            if (!rc && cudaMemcpyAsync(d, h, bytes, cudaMemcpyHostToDevice, c.stream) != cudaSuccess) rc = BSC_E_CUDA;
+        };
+        up(drp, rowptr, sizeof(int32_t) * (n + 1));
+        up(dcol, col, sizeof(int32_t) * nnz);
+        up(dval, val, sizeof(double) * nnz);
+        up(db, b, sizeof(double) * n);
+        up(dx, x, sizeof(double) * n);
+        if (!rc) rc = csr_solve_device(&c, n, drp, dcol, dval, db, dx, info);
+        if (rc == BSC_OK || rc == BSC_E_NOT_CONVERGED || rc == BSC_E_BREAKDOWN) {
+            cudaMemcpyAsync(x, dx, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream);
+            cudaStreamSynchronize(c.stream);
+        }
     }
     free_all(&c);
     cudaStreamDestroy(c.stream);

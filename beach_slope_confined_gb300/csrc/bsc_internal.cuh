@@ -90,6 +90,21 @@ int cuda_err(Ctx* c, cudaError_t e, const char* where);
         if (e_ != cudaSuccess) return cuda_err((c), e_, __func__); \
     } while (0)
 
+// every transfer is ordered on the context stream (a non-blocking stream does
+// not synchronise with the legacy default stream); host buffers may be
+// temporaries, so host-side copies complete before the macro returns
+#define BSC_H2D(c, dst, src, bytes)                                                                 \
+    do {                                                                                            \
+        BSC_CUDA(c, cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyHostToDevice, (c)->stream));   \
+        BSC_CUDA(c, cudaStreamSynchronize((c)->stream));                                            \
+    } while (0)
+#define BSC_D2H(c, dst, src, bytes)                                                                 \
+    do {                                                                                            \
+        BSC_CUDA(c, cudaMemcpyAsync((dst), (src), (bytes), cudaMemcpyDeviceToHost, (c)->stream));   \
+        BSC_CUDA(c, cudaStreamSynchronize((c)->stream));                                            \
+    } while (0)
+#define BSC_MEMSET(c, dst, v, bytes) BSC_CUDA(c, cudaMemsetAsync((dst), (v), (bytes), (c)->stream))
+
 template <typename T> struct Vec2;
 template <> struct Vec2<double> { using type = double2; };
 template <> struct Vec2<float> { using type = float2; };
@@ -112,7 +127,8 @@ struct Ctx {
     bool mixed = false;
 
     State S{}, S2{};           // S2: gather target of the Morton reorder
-    std::vector<void*> allocs; // everything cudaMalloc'ed, freed at destroy
+    std::vector<void*> allocs; // buffers sized by the particle count
+    std::vector<void*> pallocs; // porosity field and solids
 
     // cell list
     int ncell = 0;
@@ -123,6 +139,9 @@ struct Ctx {
     double *sx = nullptr, *sy = nullptr, *svol = nullptr, *spor = nullptr;
     int32_t *scell_start = nullptr, *scell_count = nullptr;
     double* pgrid = nullptr;
+    std::vector<double> hpgrid;   // host copy of the porosity field
+    bool solids_dirty = true;     // solid cell list needs a rebuild
+    double grid_x0 = 0.0, grid_y0 = 0.0;
 
     // neighbour lists
     int32_t* nbr = nullptr;
@@ -201,6 +220,7 @@ int fg_layout_size(int m);
 int csr_solve_device(Ctx* c, int32_t n, const int32_t* rp, const int32_t* col, const double* val,
                      const double* b, double* x, bsc_solve_info* info);
 
+// per-particle-count buffers: freed and re-made when the count changes
 template <typename T>
 int dalloc(Ctx* c, T** p, int64_t count) {
     void* q = nullptr;
@@ -208,6 +228,26 @@ int dalloc(Ctx* c, T** p, int64_t count) {
     cudaError_t e = cudaMalloc(&q, bytes);
     if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc");
     c->allocs.push_back(q);
+    *p = (T*)q;
+    return BSC_OK;
+}
+
+// buffers that outlive a state re-upload (porosity field, solids): replaced
+// in place when uploaded again, freed at destroy
+template <typename T>
+int palloc(Ctx* c, T** p, int64_t count) {
+    if (*p) {
+        cudaStreamSynchronize(c->stream);
+        cudaFree(*p);
+        for (auto& q : c->pallocs)
+            if (q == (void*)*p) q = nullptr;
+        *p = nullptr;
+    }
+    void* q = nullptr;
+    size_t bytes = (size_t)(count > 0 ? count : 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc");
+    c->pallocs.push_back(q);
     *p = (T*)q;
     return BSC_OK;
 }

@@ -214,13 +214,15 @@ int cells_build(Ctx* c, bool allow_reorder) {
 
 // solids: static, sorted by cell on the host once
 int solids_build(Ctx* c) {
+    if (!c->solids_dirty) return BSC_OK;
+    c->solids_dirty = false;
     const KParams& K = c->K;
     const int64_t ns = c->ns;
     std::vector<double> hx(ns), hy(ns), hv(ns), hp(ns);
-    BSC_CUDA(c, cudaMemcpy(hx.data(), c->sx, sizeof(double) * ns, cudaMemcpyDeviceToHost));
-    BSC_CUDA(c, cudaMemcpy(hy.data(), c->sy, sizeof(double) * ns, cudaMemcpyDeviceToHost));
-    BSC_CUDA(c, cudaMemcpy(hv.data(), c->svol, sizeof(double) * ns, cudaMemcpyDeviceToHost));
-    BSC_CUDA(c, cudaMemcpy(hp.data(), c->spor, sizeof(double) * ns, cudaMemcpyDeviceToHost));
+    BSC_D2H(c, hx.data(), c->sx, sizeof(double) * ns);
+    BSC_D2H(c, hy.data(), c->sy, sizeof(double) * ns);
+    BSC_D2H(c, hv.data(), c->svol, sizeof(double) * ns);
+    BSC_D2H(c, hp.data(), c->spor, sizeof(double) * ns);
     std::vector<int32_t> key(ns), ord(ns);
     const double inv = 1.0 / K.cs;
     for (int64_t k = 0; k < ns; ++k)
@@ -234,12 +236,12 @@ int solids_build(Ctx* c) {
     for (int64_t k = 0; k < ns; ++k) {
         sx2[k] = hx[ord[k]]; sy2[k] = hy[ord[k]]; sv2[k] = hv[ord[k]]; sp2[k] = hp[ord[k]];
     }
-    BSC_CUDA(c, cudaMemcpy(c->sx, sx2.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemcpy(c->sy, sy2.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemcpy(c->svol, sv2.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemcpy(c->spor, sp2.data(), sizeof(double) * ns, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemcpy(c->scell_start, start.data(), sizeof(int32_t) * c->ncell, cudaMemcpyHostToDevice));
-    BSC_CUDA(c, cudaMemcpy(c->scell_count, count.data(), sizeof(int32_t) * c->ncell, cudaMemcpyHostToDevice));
+    BSC_H2D(c, c->sx, sx2.data(), sizeof(double) * ns);
+    BSC_H2D(c, c->sy, sy2.data(), sizeof(double) * ns);
+    BSC_H2D(c, c->svol, sv2.data(), sizeof(double) * ns);
+    BSC_H2D(c, c->spor, sp2.data(), sizeof(double) * ns);
+    BSC_H2D(c, c->scell_start, start.data(), sizeof(int32_t) * c->ncell);
+    BSC_H2D(c, c->scell_count, count.data(), sizeof(int32_t) * c->ncell);
     return BSC_OK;
 }
 

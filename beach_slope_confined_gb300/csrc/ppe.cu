@@ -724,7 +724,7 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
             rc = run_fgmres<EllOp<double>, double>(c, n, A, w, P.tol, rel_r0, P.maxit, c->fg_m, &iters, &rr);
         else
             rc = run_bicgstab<EllOp<double>, double>(c, n, A, w, P.tol, rel_r0, P.maxit, &iters, &rr);
-        if (rc) return rc;
+        if (rc && rc != BSC_E_BREAKDOWN) return rc;
         // true residual of the returned pressure
         k_resid<EllOp<double>, double><<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, A, c->S.p, c->b, c->r, c->part);
         BSC_LAUNCH(c);

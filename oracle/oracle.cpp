@@ -1231,3 +1231,17 @@ int orc_num_threads(void) { return omp_get_max_threads(); }
 void orc_set_threads(int32_t nt) { if (nt > 0) omp_set_num_threads(nt); }
 
 }  // extern "C"
+
+extern "C" {
+// test hook: W(r), grad factor F(r) (grad_i W = F (x_i - x_j)) and Wo of the
+// selected kernel, evaluated with the restated kernel.f90 formulae
+int orc_eval_kernel(const bsc_params* p, double r, double* w, double* f, double* w0) {
+    if (!p) return BSC_E_INVALID;
+    Orc o;
+    o.P = *p;
+    if (w) *w = Wab(&o, r, p->h);
+    if (f) *f = (r > 0) ? Wab_grad(&o, 1.0, r, p->h) : 0.0;
+    if (w0) *w0 = Wo(&o, p->h);
+    return BSC_OK;
+}
+}

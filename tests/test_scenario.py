@@ -1,0 +1,59 @@
+"""Seeded scenario generator: counts, determinism, consistency of the inputs."""
+import numpy as np
+import pytest
+
+from beach_slope_confined_gb300 import scenario as sc
+
+
+def test_splitmix64_reference_values():
+    # splitmix64 from state 0: first output 0xE220A8397B1DCDAF
+    u = sc.splitmix64_uniform(0, 2)
+    assert int(u[0] * 2 ** 53) == 0xE220A8397B1DCDAF >> 11
+
+
+@pytest.mark.parametrize("name,fluid", [("c1", 12000), ("c2", 192000), ("c4", 1142 * 85)])
+def test_fluid_counts(name, fluid):
+    spec = sc.config_spec(name)
+    assert int(spec.length / spec.dx + 1e-9) * int(spec.depth / spec.dx + 1e-9) == fluid
+    if name == "c1":
+        scen = sc.build(spec)
+        assert scen.n_fluid == fluid
+        assert scen.sx.size > 0
+
+
+def test_deterministic_and_consistent():
+    spec = sc.config_spec("c1")
+    a, b = sc.build(spec), sc.build(spec)
+    for f in ("x", "y", "mass", "sx", "sy"):
+        assert np.array_equal(getattr(a, f), getattr(b, f))
+    fluid = a.tid == sc.TID_FLUID
+    # jitter is within +/- 0.01 dx of the lattice
+    lat = (np.floor(a.x[fluid] / spec.dx) + 0.5) * spec.dx
+    assert np.max(np.abs(a.x[fluid] - lat)) <= 0.01 * spec.dx + 1e-15
+    # fluid mass = rho0 n dx^2, n in [por, 1]
+    n = a.mass[fluid] / (spec.rho0 * spec.dx ** 2)
+    assert n.min() >= spec.por - 1e-12 and n.max() <= 1.0
+    # every solid lies below the slope line
+    assert np.all(a.sy < spec.slope * (a.sx - spec.toe_x))
+    # three wall layers with tid 1 innermost
+    assert set(np.unique(a.tid)) == {1, 2, 3}
+
+
+def test_porosity_field_per_cell():
+    spec = sc.config_spec("c3")
+    assert spec.por_jitter == 0.05
+    spec.dx = 0.01  # the field does not depend on resolution
+    scen = sc.build(spec)
+    g = scen.por_grid
+    assert g.shape == (8, 40)
+    assert g.min() >= 0.35 and g.max() <= 0.45 and g.std() > 0.01
+
+
+def test_piston_ramp_starts_at_rest():
+    spec = sc.config_spec("c5")
+    assert len(spec.piston_amp) == 8 and abs(sum(spec.piston_amp) - 0.03) < 1e-12
+    assert min(spec.piston_period) == 0.8 and max(spec.piston_period) == 2.0
+    x0, v0 = sc.piston_stroke(spec, 0.0)
+    assert x0 == 0.0 and v0 == 0.0
+    x1, v1 = sc.piston_stroke(spec, 10.0)
+    assert abs(x1) <= 0.03
