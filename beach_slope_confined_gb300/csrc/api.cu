@@ -75,6 +75,11 @@ static void derive_kparams(Ctx* c) {
     K.wend_F = 35.0 / (4.0 * 3.140 * ((h * h) * (h * h)));
     K.wend_W = 7.0 / (4 * 3.140 * (h * h));
     K.w0 = (P.kernel == BSC_KERNEL_WENDLAND_C2) ? K.wend_W : 4.0 * K.hyb_A + 6.0 * K.hyb_B;
+    K.inv_h = 1.0 / h;
+    K.hyb_n1 = (9.0 * K.hyb_A + 3.0 * K.hyb_B) / (h * h * h);  // r < h: n1 r - n0 - n2/(r h)
+    K.hyb_n0 = 12.0 * K.hyb_A / (h * h);
+    K.hyb_n2 = 6.0 * K.hyb_B;
+    K.hyb_f = 3.0 * (K.hyb_A + K.hyb_B);                        // r >= h: -f (2-q)^2/(r h)
     K.kmax = P.max_neighbors;
 }
 

@@ -27,7 +27,7 @@ namespace bsc {
 constexpr int WARP = 32;
 constexpr int NB_BLOCK = 128;     // threads per block for particle kernels
 constexpr int RED_BLOCK = 256;    // threads per block for reductions
-constexpr int RED_GRID = 304;     // fixed reduction grid (2 x 152 SMs): deterministic sums
+constexpr int RED_GRID = 912;     // fixed reduction grid (6 x 152 SMs): deterministic sums
 
 // ---- particle state (SoA) --------------------------------------------------
 struct State {
@@ -63,6 +63,7 @@ struct KParams {
     double bxmin, bxmax;
     // kernel coefficients: grad_i W = F(r) (x_i - x_j)
     double hyb_A, hyb_B, wend_F, wend_W, w0;
+    double inv_h, hyb_n0, hyb_n1, hyb_n2, hyb_f;  // folded hybrid-gradient constants
     // cell grid
     double gx0, gy0, cs;
     int nx, ny;

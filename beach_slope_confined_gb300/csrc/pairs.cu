@@ -27,29 +27,28 @@ namespace bsc {
 //   F = -35/(4*3.14 h^4) (1 - r/(2h))^3.
 template <typename R>
 __device__ __forceinline__ R grad_factor(const KParams& K, R r) {
-    const R h = (R)K.h;
+    const R q = r * (R)K.inv_h;
     if (K.kernel == BSC_KERNEL_WENDLAND_C2) {
-        R a = (R)1 - r / ((R)2 * h);
+        R a = (R)1 - (R)0.5 * q;
         return -(R)K.wend_F * (a * a * a);
     }
-    const R A = (R)K.hyb_A, B = (R)K.hyb_B;
-    const R h2 = h * h, h3 = h2 * h;
-    if (r < h) return A * ((R)9 * r / h3 - (R)12 / h2) + B * ((R)3 * r / h3 - (R)6 / (r * h));
-    R a = (R)2 - r / h;
-    return -(A + B) * ((R)3 / (r * h)) * (a * a);
+    // A (9r/h^3 - 12/h^2) + B (3r/h^3 - 6/(rh)) = (9A+3B) r/h^3 - 12A/h^2 - 6B/(rh)
+    const R inv_rh = (R)K.inv_h / r;
+    if (q < (R)1) return (R)K.hyb_n1 * r - (R)K.hyb_n0 - (R)K.hyb_n2 * inv_rh;
+    R a = (R)2 - q;
+    return -(R)K.hyb_f * inv_rh * (a * a);
 }
 
 // W(r) (kernel.f90:34-66 and the Wendland comment at :42-43)
 template <typename R>
 __device__ __forceinline__ R kern_w(const KParams& K, R r) {
-    const R h = (R)K.h;
+    const R q = r * (R)K.inv_h;
     if (K.kernel == BSC_KERNEL_WENDLAND_C2) {
-        R q = r / h, a = (R)1 - r / ((R)2 * h), a2 = a * a;
+        R a = (R)1 - (R)0.5 * q, a2 = a * a;
         return (R)K.wend_W * ((R)1 + (R)2 * q) * (a2 * a2);
     }
     const R A = (R)K.hyb_A, B = (R)K.hyb_B;
-    R q = r / h;
-    if (r < h) return A * ((R)4 - (R)6 * q * q + (R)3 * q * q * q) + B * (q * q * q - (R)6 * q + (R)6);
+    if (q < (R)1) return A * ((R)4 - (R)6 * q * q + (R)3 * q * q * q) + B * (q * q * q - (R)6 * q + (R)6);
     R a = (R)2 - q;
     return (A + B) * (a * a * a);
 }

@@ -774,12 +774,16 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
         Work<float> w{c->xf, c->rf, c->sf, c->rhf, c->pf, c->vf, c->tf, c->bf, c->Vf};
         int it = 0;
         double rri = 0;
-        const int budget = P.maxit - total;
+        // an FP32 Krylov solve stagnates near its attainable accuracy, so
+        // each sweep gets a bounded share of the iteration budget
+        const int share = std::max(50, P.maxit / std::max(1, P.max_outer));
+        const int budget = std::min(share, P.maxit - total);
         int rc2 = (P.solver == BSC_SOLVER_FGMRES)
                       ? run_fgmres<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, c->fg_m, &it, &rri)
                       : run_bicgstab<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, &it, &rri);
         total += it;
         if (rc2 == BSC_E_BREAKDOWN && it == 0) { st = BSC_E_BREAKDOWN; break; }
+        if (!std::isfinite(rri)) { st = BSC_E_BREAKDOWN; break; }  // keep x: the correction is unusable
         k_ir_add<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, x, c->xf);
         BSC_LAUNCH(c);
     }

@@ -27,6 +27,21 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / nb) if nb > 0 else float(np.linalg.norm(a - b))
 
 
+def canonical_csr(rp, col, val, n):
+    """The exported PPE as a canonical sparse matrix: duplicates summed and
+    explicit zeros dropped.  The reference (and the oracle) leave the slots of
+    a ghost row's fluid neighbours at column `pos` with value 0
+    (isph.f90:125-128,274-296); the CUDA path stores them at the neighbour's
+    column with value 0.  Both are the same matrix."""
+    import scipy.sparse as sp
+
+    A = sp.csr_matrix((val, col, rp), shape=(n, n))
+    A.sum_duplicates()
+    A.eliminate_zeros()
+    A.sort_indices()
+    return A
+
+
 def make_pair(scen, params, gpu_factory):
     """(gpu, cpu) contexts with the same scenario uploaded and effpor run."""
     g = gpu_factory(params)
