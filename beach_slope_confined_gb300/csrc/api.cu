@@ -125,9 +125,9 @@ static int alloc_solver_work(Ctx* c, int64_t n, bool fp64, bool fp32) {
     if (c->P.solver == BSC_SOLVER_FGMRES && fp64)
         if ((rc = dalloc(c, &c->V, (int64_t)(m + 1) * n))) return rc;
     if (fp32) {
-        if ((rc = dalloc(c, &c->xf, 8 * n))) return rc;
+        if ((rc = dalloc(c, &c->xf, 9 * n))) return rc;
         c->rf = c->xf + n; c->sf = c->xf + 2 * n; c->rhf = c->xf + 3 * n; c->pf = c->xf + 4 * n;
-        c->vf = c->xf + 5 * n; c->tf = c->xf + 6 * n; c->bf = c->xf + 7 * n;
+        c->vf = c->xf + 5 * n; c->tf = c->xf + 6 * n; c->bf = c->xf + 7 * n; c->xbf = c->xf + 8 * n;
         if (c->P.solver == BSC_SOLVER_FGMRES)
             if ((rc = dalloc(c, &c->Vf, (int64_t)(m + 1) * n))) return rc;
     }

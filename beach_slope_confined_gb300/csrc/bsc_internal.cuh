@@ -48,6 +48,7 @@ __host__ __device__ inline int64_t ell(int64_t i, int k, int kmax) {
 // ---- solver scalars kept on the device -------------------------------------
 struct Scalars {
     double rhob[2];            // rho of the current iteration, by iteration parity
+    double bestb[2];           // smallest residual norm so far, by iteration parity
     double rho, alpha, omega, beta;
     double rr, bnorm, r0norm, target;
     double tmp[8];
@@ -160,6 +161,7 @@ struct Ctx {
     // Krylov work (FP64) and (FP32)
     double *r = nullptr, *rh = nullptr, *pd = nullptr, *v = nullptr, *s = nullptr, *tv = nullptr, *xw = nullptr;
     float *rf = nullptr, *rhf = nullptr, *pf = nullptr, *vf = nullptr, *sf = nullptr, *tf = nullptr, *xf = nullptr;
+    float* xbf = nullptr;         // best inner iterate (mixed)
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64
     float* Vf = nullptr;          // FGMRES basis FP32 (mixed)
     double* Hd = nullptr;         // Hessenberg + Givens + y on device

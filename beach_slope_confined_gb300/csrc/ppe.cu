@@ -256,6 +256,7 @@ __global__ void k_bicg_setup(const double* __restrict__ part, Scalars* sc, doubl
     if (threadIdx.x == 0) {
         sc->rr = v[0];
         sc->rhob[0] = v[0];
+        sc->bestb[0] = sqrt(v[0]);
         sc->bnorm = sqrt(v[1]);
         sc->r0norm = sqrt(v[0]);
         sc->target = tol * (rel_r0 ? sc->r0norm : sc->bnorm);
@@ -345,28 +346,40 @@ __global__ void __launch_bounds__(RED_BLOCK) k_bicg_4(int64_t n, T* __restrict__
 }
 
 // convergence, beta, p = r + beta (p - omega v)
+// With `xbest` set (the FP32 inner solve of the mixed path) the iterate of
+// smallest residual is kept and a sweep whose residual grows past `blowup`
+// times that minimum stops: BiCGSTAB's residual is not monotone, and in FP32
+// on this operator it can diverge, while refinement needs a correction that
+// does not increase the residual.
 template <typename T>
 __global__ void __launch_bounds__(RED_BLOCK) k_bicg_5(int64_t n, T* __restrict__ p, const T* __restrict__ r,
                                                        const T* __restrict__ v, const double* __restrict__ part,
-                                                       Scalars* sc, int par, int it_next) {
+                                                       Scalars* sc, int par, int it_next, const T* __restrict__ x,
+                                                       T* __restrict__ xbest, double blowup) {
     if (sc->done | sc->breakdown) return;
     double d[2];
     reduce_partials<2>(part + 4 * RED_GRID, d);
     // every block derives the same scalars; block 0 publishes them for the
-    // next kernels (rho goes to the other parity slot, never read here)
-    const double alpha = sc->tmp[0], omega = sc->tmp[1], rho = sc->rhob[par];
+    // next kernels (rho and best go to the other parity slot, never read here)
+    const double alpha = sc->tmp[0], omega = sc->tmp[1], rho = sc->rhob[par], best = sc->bestb[par];
     const double rn = sqrt(d[0]);
     const bool conv = rn <= sc->target;
-    const bool brk = !conv && (omega == 0.0 || d[1] == 0.0);
-    const double beta = brk || conv ? 0.0 : (d[1] / rho) * (alpha / omega);
+    const bool improved = rn < best;
+    const bool stop = xbest && !conv && (!(rn == rn) || rn > blowup * best);
+    const bool brk = !conv && !stop && (omega == 0.0 || d[1] == 0.0);
+    const double beta = brk || conv || stop ? 0.0 : (d[1] / rho) * (alpha / omega);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         sc->rr = d[0];
         sc->rhob[par ^ 1] = d[1];
+        sc->bestb[par ^ 1] = improved ? rn : best;
         sc->it = it_next;
-        sc->done = conv ? 1 : 0;
+        sc->done = (conv || stop) ? 1 : 0;
         sc->breakdown = brk ? 1 : 0;
     }
-    if (conv || brk) return;
+    if (xbest && improved) {
+        GRID_LOOP(i, n) xbest[i] = x[i];
+    }
+    if (conv || brk || stop) return;
     const T bt = (T)beta, w = (T)omega;
     GRID_LOOP(i, n) p[i] = r[i] + bt * (p[i] - w * v[i]);
 }
@@ -592,14 +605,17 @@ int fetch_scalars(Ctx* c) {
 
 constexpr int BATCH = 8;
 
+// `xbest` (optional): keep the minimum-residual iterate there and stop a
+// diverging solve; *rr_out is then the squared best residual
 template <typename Op, typename T>
 int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_r0, int maxit, int* iters,
-                 double* rr_out) {
+                 double* rr_out, T* xbest = nullptr) {
     const int G = RED_GRID, B = RED_BLOCK;
     k_bicg_init<Op, T><<<G, B, 0, c->stream>>>(n, A, w.x, w.b, w.r, w.rh, w.p, c->part);
     BSC_LAUNCH(c);
     k_bicg_setup<<<1, B, 0, c->stream>>>(c->part, c->sc, tol, rel_r0);
     BSC_LAUNCH(c);
+    if (xbest) BSC_CUDA(c, cudaMemcpyAsync(xbest, w.x, sizeof(T) * n, cudaMemcpyDeviceToDevice, c->stream));
     int launched = 0;
     for (;;) {
         int rc = fetch_scalars(c);
@@ -613,14 +629,19 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
             k_bicg_2<T><<<G, B, 0, c->stream>>>(n, w.r, w.v, w.s, c->part, c->sc, par);
             k_bicg_3<Op, T><<<G, B, 0, c->stream>>>(n, A, w.s, w.t, c->part, c->sc);
             k_bicg_4<T><<<G, B, 0, c->stream>>>(n, w.x, w.p, w.s, w.t, w.r, w.rh, c->part, c->sc);
-            k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->part, c->sc, par, g + 1);
+            k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->part, c->sc, par, g + 1, w.x, xbest, 1e3);
             c->launches += 5;
         }
         launched += nb;
         BSC_CUDA(c, cudaGetLastError());
     }
     *iters = c->h_sc->it;
-    *rr_out = c->h_sc->rr;
+    if (xbest) {
+        const double b = c->h_sc->bestb[c->h_sc->it & 1];
+        *rr_out = b * b;
+    } else {
+        *rr_out = c->h_sc->rr;
+    }
     return c->h_sc->breakdown && !c->h_sc->done ? BSC_E_BREAKDOWN : BSC_OK;
 }
 
@@ -778,13 +799,16 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
         // each sweep gets a bounded share of the iteration budget
         const int share = std::max(50, P.maxit / std::max(1, P.max_outer));
         const int budget = std::min(share, P.maxit - total);
-        int rc2 = (P.solver == BSC_SOLVER_FGMRES)
-                      ? run_fgmres<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, c->fg_m, &it, &rri)
-                      : run_bicgstab<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, &it, &rri);
+        // FGMRES minimises the residual (its iterate is the best one); the
+        // BiCGSTAB sweep returns its minimum-residual iterate
+        const bool gm = P.solver == BSC_SOLVER_FGMRES;
+        int rc2 = gm ? run_fgmres<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, c->fg_m, &it, &rri)
+                     : run_bicgstab<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, &it, &rri, c->xbf);
         total += it;
         if (rc2 == BSC_E_BREAKDOWN && it == 0) { st = BSC_E_BREAKDOWN; break; }
         if (!std::isfinite(rri)) { st = BSC_E_BREAKDOWN; break; }  // keep x: the correction is unusable
-        k_ir_add<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, x, c->xf);
+        if (!(rri < (double)rn * rn)) { st = BSC_E_NOT_CONVERGED; break; }  // the sweep made no progress
+        k_ir_add<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, x, gm ? c->xf : c->xbf);
         BSC_LAUNCH(c);
     }
     si->iterations = total;

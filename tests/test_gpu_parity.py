@@ -168,3 +168,25 @@ def test_capacity_overflow_is_reported():
     with pytest.raises(BscError) as e:
         g.neighbour()
     assert e.value.code == -4
+
+
+@pytest.mark.parametrize("solver", ["bicgstab", "fgmres"])
+def test_mixed_against_fp64(solver):
+    """FP32 pair sums / inner Krylov with FP64 refinement against the FP64 path:
+    the PPE reaches the same relative residual and every field stays close."""
+    spec = small_spec(dx=0.01)
+    scen = sc.build(spec)
+    out, infos = {}, {}
+    for prec in ("fp64", "mixed"):
+        P = sc.make_params(spec, scen.bounds, precision=prec, solver=solver, tol=1e-8, maxit=20000,
+                           inner_tol=1e-2, max_outer=40)
+        g, _ = make_pair(scen, P, Solver)
+        infos[prec] = g.step(2)
+        out[prec] = g.download_state()
+    assert infos["mixed"].converged and infos["mixed"].rel_residual <= 1e-8
+    assert infos["mixed"].outer >= 1
+    errs = {f: rel_l2(out["mixed"][f], out["fp64"][f]) for f in ("x", "y", "vx", "vy", "p", "porosity", "nut")}
+    print("mixed vs fp64 relative L2:", errs)
+    assert errs["x"] < 1e-9 and errs["y"] < 1e-9
+    assert errs["porosity"] < 1e-6
+    assert errs["p"] < 1e-4 and errs["vx"] < 1e-3 and errs["vy"] < 1e-3
