@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -95,6 +96,8 @@ static uint64_t spread_bits(uint32_t v) {
 
 static void free_all(Ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
     for (void* p : c->allocs) cudaFree(p);
     c->allocs.clear();
     if (c->h_sc) cudaFreeHost(c->h_sc);
@@ -146,10 +149,11 @@ static int alloc_for(Ctx* c, int64_t n) {
     if ((rc = dalloc(c, &c->pcell, n)) || (rc = dalloc(c, &c->pslot, n)) || (rc = dalloc(c, &c->sorted, n))) return rc;
     const int64_t slots = ((n + 31) / 32) * 32 * (int64_t)c->K.kmax;
     if ((rc = dalloc(c, &c->nbr, slots)) || (rc = dalloc(c, &c->cnt, n))) return rc;
+    // FP64 grad W and PPE values in both precisions; the mixed path adds FP32
+    // copies for its FP32 pair sums and inner Krylov sweeps
+    if ((rc = dalloc(c, &c->gw, slots)) || (rc = dalloc(c, &c->aval, slots))) return rc;
     if (c->mixed) {
         if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->avalf, slots))) return rc;
-    } else {
-        if ((rc = dalloc(c, &c->gw, slots)) || (rc = dalloc(c, &c->aval, slots))) return rc;
     }
     if ((rc = dalloc(c, &c->b, n))) return rc;
     if ((rc = alloc_solver_work(c, n, !c->mixed, c->mixed))) return rc;
@@ -360,6 +364,8 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
         return BSC_E_CUDA;
     }
     for (int k = 0; k < 2 * Ctx::EVPOOL; ++k) cudaEventCreate(&c->evs[k]);
+    if (const char* e = std::getenv("BSC_GRAPHS")) c->use_graphs = e[0] != '0';
+    if (const char* e = std::getenv("BSC_DEBUG")) c->debug = e[0] == '1';
     *out = c;
     return BSC_OK;
 }

@@ -52,7 +52,7 @@ struct Scalars {
     double rho, alpha, omega, beta;
     double rr, bnorm, r0norm, target;
     double tmp[8];
-    int32_t done, breakdown, it, pad;
+    int32_t done, breakdown, it, it_copy;  // it_copy: `it` as seen by the update kernel
 };
 
 // ---- kernel constants --------------------------------------------------------
@@ -162,6 +162,18 @@ struct Ctx {
     double *r = nullptr, *rh = nullptr, *pd = nullptr, *v = nullptr, *s = nullptr, *tv = nullptr, *xw = nullptr;
     float *rf = nullptr, *rhf = nullptr, *pf = nullptr, *vf = nullptr, *sf = nullptr, *tf = nullptr, *xf = nullptr;
     float* xbf = nullptr;         // best inner iterate (mixed)
+    // instantiated CUDA graphs of one batch of Krylov iterations, keyed by
+    // the operator and vectors they were captured with
+    struct GraphEntry {
+        const void* k0;
+        const void* k1;
+        const void* k2;
+        int64_t n;
+        cudaGraphExec_t exec;
+    };
+    std::vector<GraphEntry> graphs;
+    bool use_graphs = true;
+    bool debug = false;           // BSC_DEBUG=1: per-sweep solver trace on stderr
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64
     float* Vf = nullptr;          // FGMRES basis FP32 (mixed)
     double* Hd = nullptr;         // Hessenberg + Givens + y on device

@@ -73,8 +73,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                                                          const int32_t* __restrict__ ccount,
                                                          const int32_t* __restrict__ sorted,
                                                          const int32_t* __restrict__ pcell,
-                                                         int32_t* __restrict__ nbr,
-                                                         typename Vec2<R>::type* __restrict__ gw,
+                                                         int32_t* __restrict__ nbr, double2* __restrict__ gw,
+                                                         float2* __restrict__ gwf,
                                                          int32_t* __restrict__ cnt, int32_t* __restrict__ flag) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -97,12 +97,16 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                 if (fdx * fdx + fdy * fdy > H2f) continue;
                 const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
                 if (!(r < K.H)) continue;
-                const R F = grad_factor<R>(K, (R)r);
-                const R gx = F * (R)dx, gy = F * (R)dy;
+                // grad W per pair in FP64 (stored in FP64, and in FP32 for the
+                // FP32 pair sums of the mixed path); the M sum runs in R
+                const double F = grad_factor<double>(K, r);
+                const double gx64 = F * dx, gy64 = F * dy;
+                const R gx = (R)gx64, gy = (R)gy64;
                 if (count < K.kmax) {
                     const int64_t e = ell(i, count, K.kmax);
                     nbr[e] = j;
-                    gw[e] = {gx, gy};
+                    gw[e] = {gx64, gy64};
+                    if (gwf) gwf[e] = {(float)gx64, (float)gy64};
                 }
                 ++count;
                 const R vj = (R)S.vol[j];
@@ -145,10 +149,11 @@ int op_neighbour(Ctx* c) {
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
         k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
-                                                          c->pcell, c->nbr, c->gwf, c->cnt, c->d_flag);
+                                                          c->pcell, c->nbr, c->gw, c->gwf, c->cnt, c->d_flag);
     else
         k_neighbour<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count,
-                                                           c->sorted, c->pcell, c->nbr, c->gw, c->cnt, c->d_flag);
+                                                           c->sorted, c->pcell, c->nbr, c->gw, nullptr, c->cnt,
+                                                           c->d_flag);
     BSC_LAUNCH(c);
     c->have_lists = true;
     return BSC_OK;
@@ -467,6 +472,59 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel(int64_t n, State S, KPara
     }
 }
 
+// Mixed path.  The pressure force is a sum of terms ~p/h that cancel down to
+// ~rho g (a factor ~200 in a hydrostatic column), so FP32 there costs ~5e-5
+// in the velocity.  The term is split exactly:
+//   fluid j: (p_j q_i + p_i q_j)/(q_i+q_j) = p_i + q_i (p_j - p_i)/(q_i+q_j)
+//   wall j:  p_j + p_i = 2 p_i + (p_j - p_i)
+// so a_i = c0 [ 2 p_i sum_j V_j g_j  +  sum_j w_j (p_j - p_i) g_j ]; the first
+// (cancelling) sum runs in FP64, the second (difference) sum in FP32.
+__global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S, KParams K,
+                                                              const int32_t* __restrict__ nbr,
+                                                              const double2* __restrict__ gw,
+                                                              const float2* __restrict__ gwf,
+                                                              const int32_t* __restrict__ cnt,
+                                                              const double* __restrict__ q, double dt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint8_t fi = S.flags[i];
+    if (S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD))) {
+        const double L0 = S.L0[i], L1 = S.L1[i], L2 = S.L2[i], L3 = S.L3[i];
+        const float L0f = (float)L0, L1f = (float)L1, L2f = (float)L2, L3f = (float)L3;
+        const double pi = S.p[i];
+        const float qi = (float)q[i];
+        double sx = 0.0, sy = 0.0;
+        float ax = 0.f, ay = 0.f;
+        const int m = cnt[i];
+        for (int k = 0; k < m; ++k) {
+            const int64_t e = ell(i, k, K.kmax);
+            const int j = nbr[e];
+            const double2 g = gw[e];
+            const float2 gf = gwf[e];
+            const double vj = S.vol[j];
+            sx += vj * (L0 * g.x + L1 * g.y);
+            sy += vj * (L2 * g.x + L3 * g.y);
+            const float w = (S.tid[j] == BSC_TID_FLUID) ? 2.f * (float)vj * qi / (qi + (float)q[j]) : (float)vj;
+            const float dp = (float)(S.p[j] - pi);
+            ax += w * dp * (L0f * gf.x + L1f * gf.y);
+            ay += w * dp * (L2f * gf.x + L3f * gf.y);
+        }
+        const double ni = S.por[i], c0 = ni * ni / S.rho[i];
+        const double vx = S.vxs[i] - dt * c0 * (2.0 * pi * sx + (double)ax);
+        const double vy = S.vys[i] - dt * c0 * (2.0 * pi * sy + (double)ay);
+        S.vx[i] = vx;
+        S.vy[i] = vy;
+        S.vel[i] = sqrt(vx * vx + vy * vy) / ni;
+    }
+    if (fi & BSC_FLAG_BUFFER) {
+        S.vx[i] = S.vxs[i];
+        S.vy[i] = 0.0;
+    }
+    if ((fi & BSC_FLAG_DEAD) && !(fi & BSC_FLAG_BUFFER)) {
+        S.vx[i] = 0.0; S.vy[i] = 0.0; S.vxs[i] = 0.0; S.vys[i] = 0.0;
+    }
+}
+
 int op_comp_vel(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "comp_vel before neighbour");
     double* q = c->r;
@@ -474,7 +532,7 @@ int op_comp_vel(Ctx* c) {
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
-        k_comp_vel<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, q, c->dt);
+        k_comp_vel_mixed<<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->gwf, c->cnt, q, c->dt);
     else
         k_comp_vel<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, q, c->dt);
     BSC_LAUNCH(c);

@@ -21,6 +21,7 @@
 // relative residual to the requested tolerance.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <vector>
 
 #include "bsc_internal.cuh"
@@ -34,6 +35,7 @@ template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                         const typename Vec2<R>::type* __restrict__ gw,
                                                         const int32_t* __restrict__ cnt, R* __restrict__ aval,
+                                                        float* __restrict__ avalf,
                                                         double* __restrict__ b, const double* __restrict__ q,
                                                         const double* __restrict__ usx, const double* __restrict__ usy,
                                                         double dt) {
@@ -104,14 +106,19 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
     const double d = (double)dia;
     if (d == 0.0 || !isfinite(d)) {
         // zero-neighbour guard: identity row, b = 0 (the reference divides by 0)
-        for (int k = 0; k < m; ++k) aval[ell(i, k, K.kmax)] = 0;
+        for (int k = 0; k < m; ++k) {
+            aval[ell(i, k, K.kmax)] = 0;
+            if (avalf) avalf[ell(i, k, K.kmax)] = 0.f;
+        }
         b[i] = 0.0;
         return;
     }
     const R inv = (R)(1.0 / d);
     for (int k = 0; k < m; ++k) {
         const int64_t e = ell(i, k, K.kmax);
-        aval[e] = aval[e] * inv;
+        const R v = aval[e] * inv;
+        aval[e] = v;
+        if (avalf) avalf[e] = (float)v;  // the mixed path's inner-sweep copy
     }
     b[i] = ((double)fv / dt) / d;
 }
@@ -132,12 +139,11 @@ int op_ppe_assemble(Ctx* c) {
     k_vs_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, q, ux, uy);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
-    if (c->mixed)
-        k_assemble<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, c->avalf, c->b, q,
-                                                         ux, uy, c->dt);
-    else
-        k_assemble<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval, c->b, q,
-                                                          ux, uy, c->dt);
+    // FP64 assembly in both paths: the PPE coefficients are sums whose FP32
+    // rounding moves the pressure by ~5e-6 (relative) at 1e-8 residual; the
+    // mixed path keeps an FP32 copy for its inner sweeps
+    k_assemble<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
+                                                      c->mixed ? c->avalf : nullptr, c->b, q, ux, uy, c->dt);
     BSC_LAUNCH(c);
     c->have_csr = true;
     return BSC_OK;
@@ -152,12 +158,27 @@ struct EllOp {
     const int32_t* nbr;
     const int32_t* cnt;
     int kmax;
+    const void* key() const { return aval; }
+    // four entries per round so four gathers are in flight per thread; the
+    // column stride of the ELL layout is 32 slots
     template <typename X, typename A>
     __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
         A s = (A)x[i];
         const int m = cnt[i];
-        for (int k = 0; k < m; ++k) {
-            const int64_t e = ell(i, k, kmax);
+        const int64_t e0 = ell(i, 0, kmax);
+        int k = 0;
+        for (; k + 4 <= m; k += 4) {
+            const int64_t e = e0 + (int64_t)k * 32;
+            const int j0 = nbr[e], j1 = nbr[e + 32], j2 = nbr[e + 64], j3 = nbr[e + 96];
+            const T a0 = aval[e], a1 = aval[e + 32], a2 = aval[e + 64], a3 = aval[e + 96];
+            const X x0 = x[j0], x1 = x[j1], x2 = x[j2], x3 = x[j3];
+            s += (A)a0 * (A)x0;
+            s += (A)a1 * (A)x1;
+            s += (A)a2 * (A)x2;
+            s += (A)a3 * (A)x3;
+        }
+        for (; k < m; ++k) {
+            const int64_t e = e0 + (int64_t)k * 32;
             s += (A)aval[e] * (A)x[nbr[e]];
         }
         return s;
@@ -168,6 +189,7 @@ struct CsrOp {
     const int32_t* rp;
     const int32_t* col;
     const double* val;
+    const void* key() const { return val; }
     template <typename X, typename A>
     __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
         A s = 0;
@@ -286,11 +308,11 @@ __global__ void __launch_bounds__(RED_BLOCK) k_bicg_1(int64_t n, Op A, const T* 
 template <typename T>
 __global__ void __launch_bounds__(RED_BLOCK) k_bicg_2(int64_t n, const T* __restrict__ r, const T* __restrict__ v,
                                                        T* __restrict__ s, const double* __restrict__ part,
-                                                       Scalars* sc, int par) {
+                                                       Scalars* sc) {
     if (sc->done | sc->breakdown) return;
     double d[1];
     reduce_partials<1>(part, d);
-    const double rho = sc->rhob[par];
+    const double rho = sc->rhob[sc->it & 1];  // `it` was last written by the previous k_bicg_5
     if (d[0] == 0.0 || rho == 0.0) {
         if (blockIdx.x == 0 && threadIdx.x == 0) sc->tmp[0] = 0.0;
         return;
@@ -331,7 +353,10 @@ __global__ void __launch_bounds__(RED_BLOCK) k_bicg_4(int64_t n, T* __restrict__
         return;
     }
     const double omega = (d[1] == 0.0) ? 0.0 : d[0] / d[1];
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->tmp[1] = omega;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        sc->tmp[1] = omega;
+        sc->it_copy = sc->it;  // k_bicg_5 reads the copy while its block 0 advances `it`
+    }
     const T a = (T)alpha, w = (T)omega;
     double acc[2] = {0.0, 0.0};
     GRID_LOOP(i, n) {
@@ -354,13 +379,14 @@ __global__ void __launch_bounds__(RED_BLOCK) k_bicg_4(int64_t n, T* __restrict__
 template <typename T>
 __global__ void __launch_bounds__(RED_BLOCK) k_bicg_5(int64_t n, T* __restrict__ p, const T* __restrict__ r,
                                                        const T* __restrict__ v, const double* __restrict__ part,
-                                                       Scalars* sc, int par, int it_next, const T* __restrict__ x,
+                                                       Scalars* sc, const T* __restrict__ x,
                                                        T* __restrict__ xbest, double blowup) {
     if (sc->done | sc->breakdown) return;
     double d[2];
     reduce_partials<2>(part + 4 * RED_GRID, d);
     // every block derives the same scalars; block 0 publishes them for the
     // next kernels (rho and best go to the other parity slot, never read here)
+    const int g = sc->it_copy, par = g & 1;
     const double alpha = sc->tmp[0], omega = sc->tmp[1], rho = sc->rhob[par], best = sc->bestb[par];
     const double rn = sqrt(d[0]);
     const bool conv = rn <= sc->target;
@@ -372,7 +398,7 @@ __global__ void __launch_bounds__(RED_BLOCK) k_bicg_5(int64_t n, T* __restrict__
         sc->rr = d[0];
         sc->rhob[par ^ 1] = d[1];
         sc->bestb[par ^ 1] = improved ? rn : best;
-        sc->it = it_next;
+        sc->it = g + 1;
         sc->done = (conv || stop) ? 1 : 0;
         sc->breakdown = brk ? 1 : 0;
     }
@@ -603,7 +629,31 @@ int fetch_scalars(Ctx* c) {
     return BSC_OK;
 }
 
-constexpr int BATCH = 8;
+// Iterations queued between two convergence checks.  A batch is captured
+// once as a CUDA graph and replayed; kernels of iterations past convergence
+// return at their first instruction.
+inline int batch_for(int64_t n) { return n > 200000 ? 16 : 8; }
+
+// a cached graph for `body`, captured on the context stream
+template <typename F>
+int batch_graph(Ctx* c, const void* k0, const void* k1, const void* k2, int64_t n, F body, cudaGraphExec_t* out) {
+    for (auto& g : c->graphs)
+        if (g.k0 == k0 && g.k1 == k1 && g.k2 == k2 && g.n == n) {
+            *out = g.exec;
+            return BSC_OK;
+        }
+    cudaGraph_t graph = nullptr;
+    BSC_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    body();
+    BSC_CUDA(c, cudaStreamEndCapture(c->stream, &graph));
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaGraphInstantiate");
+    c->graphs.push_back({k0, k1, k2, n, exec});
+    *out = exec;
+    return BSC_OK;
+}
 
 // `xbest` (optional): keep the minimum-residual iterate there and stop a
 // diverging solve; *rr_out is then the squared best residual
@@ -616,22 +666,32 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
     k_bicg_setup<<<1, B, 0, c->stream>>>(c->part, c->sc, tol, rel_r0);
     BSC_LAUNCH(c);
     if (xbest) BSC_CUDA(c, cudaMemcpyAsync(xbest, w.x, sizeof(T) * n, cudaMemcpyDeviceToDevice, c->stream));
+    auto one = [&]() {
+        k_bicg_1<Op, T><<<G, B, 0, c->stream>>>(n, A, w.p, w.v, w.rh, c->part, c->sc);
+        k_bicg_2<T><<<G, B, 0, c->stream>>>(n, w.r, w.v, w.s, c->part, c->sc);
+        k_bicg_3<Op, T><<<G, B, 0, c->stream>>>(n, A, w.s, w.t, c->part, c->sc);
+        k_bicg_4<T><<<G, B, 0, c->stream>>>(n, w.x, w.p, w.s, w.t, w.r, w.rh, c->part, c->sc);
+        k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->part, c->sc, w.x, xbest, 1e3);
+    };
+    const int batch = batch_for(n);
     int launched = 0;
     for (;;) {
         int rc = fetch_scalars(c);
         if (rc) return rc;
         const Scalars& h = *c->h_sc;
         if (h.done || h.breakdown || h.it >= maxit || launched >= maxit) break;
-        const int nb = std::min(BATCH, maxit - h.it);
-        for (int q = 0; q < nb; ++q) {
-            const int g = h.it + q, par = g & 1;  // iterations run in order until done
-            k_bicg_1<Op, T><<<G, B, 0, c->stream>>>(n, A, w.p, w.v, w.rh, c->part, c->sc);
-            k_bicg_2<T><<<G, B, 0, c->stream>>>(n, w.r, w.v, w.s, c->part, c->sc, par);
-            k_bicg_3<Op, T><<<G, B, 0, c->stream>>>(n, A, w.s, w.t, c->part, c->sc);
-            k_bicg_4<T><<<G, B, 0, c->stream>>>(n, w.x, w.p, w.s, w.t, w.r, w.rh, c->part, c->sc);
-            k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->part, c->sc, par, g + 1, w.x, xbest, 1e3);
-            c->launches += 5;
+        const int nb = std::min(batch, maxit - h.it);
+        if (c->use_graphs && nb == batch) {
+            cudaGraphExec_t ge = nullptr;
+            rc = batch_graph(c, A.key(), (const void*)w.x, (const void*)xbest, n, [&]() {
+                for (int q = 0; q < batch; ++q) one();
+            }, &ge);
+            if (rc) return rc;
+            BSC_CUDA(c, cudaGraphLaunch(ge, c->stream));
+        } else {
+            for (int q = 0; q < nb; ++q) one();
         }
+        c->launches += 5 * nb;
         launched += nb;
         BSC_CUDA(c, cudaGetLastError());
     }
@@ -691,7 +751,7 @@ int run_fgmres(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_r0
 }
 
 // FP64 true residual of the FP32-valued unit-diagonal matrix: r = b - A x
-__global__ void __launch_bounds__(RED_BLOCK) k_ir_resid(int64_t n, EllOp<float> A, const double* __restrict__ x,
+__global__ void __launch_bounds__(RED_BLOCK) k_ir_resid(int64_t n, EllOp<double> A, const double* __restrict__ x,
                                                          const double* __restrict__ b, double* __restrict__ r,
                                                          float* __restrict__ rf, double* __restrict__ part) {
     double acc[2] = {0.0, 0.0};
@@ -775,7 +835,7 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
     int outer = 0, total = 0, st = BSC_OK;
     bool conv = false;
     for (;;) {
-        k_ir_resid<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, Af, x, c->b, r64, c->rf, c->part);
+        k_ir_resid<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, EllOp<double>{c->aval, c->nbr, c->cnt, c->K.kmax}, x, c->b, r64, c->rf, c->part);
         BSC_LAUNCH(c);
         k_ir_norms<<<1, RED_BLOCK, 0, c->stream>>>(c->part, norms);
         BSC_LAUNCH(c);
@@ -807,6 +867,9 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
         total += it;
         if (rc2 == BSC_E_BREAKDOWN && it == 0) { st = BSC_E_BREAKDOWN; break; }
         if (!std::isfinite(rri)) { st = BSC_E_BREAKDOWN; break; }  // keep x: the correction is unusable
+        if (c->debug)
+            std::fprintf(stderr, "[bsc] refinement sweep %d: |r|/|b| %.3e, inner iterations %d, inner |r|^2 ratio %.3e\n",
+                         outer, rn / bn, it, rri / ((double)rn * rn));
         if (!(rri < (double)rn * rn)) { st = BSC_E_NOT_CONVERGED; break; }  // the sweep made no progress
         k_ir_add<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, x, gm ? c->xf : c->xbf);
         BSC_LAUNCH(c);
