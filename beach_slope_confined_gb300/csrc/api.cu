@@ -364,6 +364,8 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
         return BSC_E_CUDA;
     }
     for (int k = 0; k < 2 * Ctx::EVPOOL; ++k) cudaEventCreate(&c->evs[k]);
+    cudaEventCreate(&c->ev_spmv[0]);
+    cudaEventCreate(&c->ev_spmv[1]);
     if (const char* e = std::getenv("BSC_GRAPHS")) c->use_graphs = e[0] != '0';
     if (const char* e = std::getenv("BSC_DEBUG")) c->debug = e[0] == '1';
     *out = c;
@@ -378,6 +380,8 @@ int bsc_destroy(bsc_ctx* c) {
     c->pallocs.clear();
     for (int k = 0; k < 2 * Ctx::EVPOOL; ++k)
         if (c->evs[k]) cudaEventDestroy(c->evs[k]);
+    for (int k = 0; k < 2; ++k)
+        if (c->ev_spmv[k]) cudaEventDestroy(c->ev_spmv[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return BSC_OK;
@@ -795,6 +799,7 @@ int bsc_csr_solve(const bsc_params* p, int32_t n, const int32_t* rowptr, const i
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BSC_E_NOT_BUILT;
     Ctx c;
     c.P = *p;
+    c.timing = false;  // no event pool on this temporary context
     if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess) return BSC_E_CUDA;
     const int64_t nnz = rowptr[n];
     int rc = alloc_solver_work(&c, n, true, false);

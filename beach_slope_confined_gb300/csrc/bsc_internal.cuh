@@ -190,6 +190,7 @@ struct Ctx {
     double ms[BSC_TIMING_SLOTS] = {0};
     int64_t calls[BSC_TIMING_SLOTS] = {0};
     bool timing = true;
+    cudaEvent_t ev_spmv[2] = {};  // around one SpMV per Krylov batch
     double* stepsc = nullptr;     // device: umax, numax (timestep reductions)
 };
 

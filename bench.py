@@ -1,0 +1,397 @@
+"""Benchmark of the ISPH step: particle-steps/s on the ~1M-particle wave tank.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the 4.0 m x 0.6 m tank at dx = 1.2 mm (833,250 fluid particles plus
+walls; per-cell porosity 0.4 +/- 0.05 in the slope), Wendland C2 with
+h = 1.3 dx, BiCGSTAB PPE to relative residual 1e-8, fixed dt = 1e-4 s.  A step
+is the whole main.f90:41-65 sequence (two neighbour searches, porosity,
+eddy viscosity, predictor, PPE assembly + solve, projection, shifting).
+The headline `value` is the mixed-precision path (FP32 pair sums and inner
+Krylov sweeps, FP64 refinement); the plain FP64 path is reported beside it.
+
+`--impl reference` times the reference algorithm on the host cores instead:
+the C++ OpenMP restatement of the Fortran routines (the Fortran itself needs
+gfortran and Intel MKL, neither present on this machine), on a bounded sample of
+the same workload.
+
+With `--gpus N` under torchrun every rank runs an independent replica of the
+tank on its own GPU (the step does not shard across GPUs here); value = the
+particle-steps of all ranks / the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "particle-steps/s at 1M (mixed vs FP64, PPE res 1e-8); adjoint/forward time"
+CONFIG = "c3"
+T_STEP, T_PPE_SOLVE, T_SPMV = 15, 8, 16
+
+
+# --------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# --------------------------------------------------------------------------
+class Dist:
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+
+            backend = os.environ.get("BSC_DIST_BACKEND", "nccl")
+            if backend == "nccl":
+                import torch
+
+                torch.cuda.set_device(self.local)
+            dist.init_process_group(backend=backend)
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, v: float) -> float:
+        if not self.pg:
+            return v
+        import torch
+
+        dev = "cuda" if os.environ.get("BSC_DIST_BACKEND", "nccl") == "nccl" else "cpu"
+        t = torch.tensor([v], dtype=torch.float64, device=dev)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+def aggregate(per_rank_seconds: float, units_per_rank: float, dist: Dist):
+    """Whole-job throughput: all ranks' units / the slowest rank's time."""
+    tmax = dist.max(per_rank_seconds)
+    return units_per_rank * dist.world / tmax, tmax
+
+
+# --------------------------------------------------------------------------
+# clocks during the timed region
+# --------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax = max(smax, float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# --------------------------------------------------------------------------
+# our arm
+# --------------------------------------------------------------------------
+def measured_peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def spmv_bytes(nnz: int, n: int, fp32: bool) -> int:
+    """Algorithmic bytes of one SpMV launch (k_bicg_1): per stored entry the
+    value and the column; per row the count, x_i, the result and the shadow
+    residual of the fused dot.  Neighbour values x_j come from cache."""
+    if fp32:
+        return 8 * nnz + 16 * n
+    return 12 * nnz + 28 * n
+
+
+def traffic_per_row(kind: str):
+    """DRAM bytes per row of one SpMV launch from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "spmv_dram_traffic.json")) as fh:
+            return float(json.load(fh)[kind]["dram_bytes_per_row"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def run_ours(args, dist: Dist):
+    from beach_slope_confined_gb300 import Solver, measure_peaks, scenario as sc, setup_tank
+
+    spec = sc.config_spec(args.config)
+    scen = sc.build(spec)
+    nf = scen.n_fluid
+    results = {}
+    states = {}
+    for prec in ("mixed", "fp64"):
+        if prec == "fp64" and args.no_fp64:
+            continue
+        P = sc.make_params(spec, scen.bounds, precision=prec, solver=args.solver, tol=1e-8, maxit=40000,
+                           inner_tol=args.inner_tol, max_outer=60)
+        g = Solver(P)
+        setup_tank(g, scen)
+        for _ in range(args.warmup):
+            g.step(1)
+        off, _ = g.get_neighbors()
+        nnz = int(off[-1])
+        g.synchronize()
+        g.reset_timings()
+        dist.barrier()
+        iters = []
+        with ClockSampler(dist.local) as clk:
+            t0 = time.perf_counter()
+            for _ in range(args.steps):
+                info = g.step(1)
+                iters.append((info.iterations, info.outer, info.rel_residual))
+            g.synchronize()
+            wall = time.perf_counter() - t0
+        t = g.timings()
+        dev_s = t.ms[T_STEP] / 1e3
+        value, tmax = aggregate(dev_s, nf * args.steps, dist)
+        spmv_ms = t.ms[T_SPMV] / max(1, t.calls[T_SPMV])
+        results[prec] = dict(value=value, ms_per_step=tmax / args.steps * 1e3, wall_s=wall, nnz=nnz,
+                             iters=iters, spmv_ms=spmv_ms, spmv_calls=int(t.calls[T_SPMV]),
+                             solve_ms=t.ms[T_PPE_SOLVE] / args.steps, launches=int(t.kernel_launches),
+                             clocks=clk.summary(), n=scen.n)
+        states[prec] = g.download_state()
+        # e2e through the C ABI with host buffers: upload, step, download
+        if prec == "mixed":
+            host = g.download_state()
+            up = {k: np.ascontiguousarray(v.reshape(-1)) for k, v in host.items()}
+            h2d = sum(a.nbytes for a in up.values())
+            g.upload_state(up)
+            g.step(1)
+            g.synchronize()
+            dist.barrier()
+            t0 = time.perf_counter()
+            ke = max(1, min(args.steps, 3))
+            for _ in range(ke):
+                g.upload_state(up)
+                g.step(1)
+                out = g.download_state()
+            e2e_s = time.perf_counter() - t0
+            d2h = sum(np.asarray(a).nbytes for a in out.values())
+            ev, _ = aggregate(e2e_s, nf * ke, dist)
+            results[prec]["e2e"] = dict(value=ev, unit="particle-steps/s", h2d_bytes_per_step=int(h2d),
+                                        d2h_bytes_per_step=int(d2h), steps=ke)
+        g.close()
+    errs = None
+    if "fp64" in states:
+        a, b = states["mixed"], states["fp64"]
+        errs = {f: float(np.linalg.norm(a[f] - b[f]) / max(np.linalg.norm(b[f]), 1e-300))
+                for f in ("x", "y", "vx", "vy", "p", "porosity", "nut")}
+    peaks = measure_peaks() if dist.rank == 0 else None
+    return scen, results, errs, peaks
+
+
+def cpu_sample(scen, spec, threads: int, gpu_iters: float, solver: str):
+    """Bounded sample of the reference algorithm on the host cores: one step
+    of the CPU restatement with the PPE solve capped at 20 iterations; the
+    solve time is scaled to `gpu_iters` iterations (the FP64 GPU solve of the
+    same workload).  Returns (particle-steps/s, description)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from beach_slope_confined_gb300 import scenario as sc
+    from beach_slope_confined_gb300.binding import setup_tank
+
+    oracle.set_threads(threads)
+    cap = 20
+    P = sc.make_params(spec, scen.bounds, solver=solver, tol=1e-8, maxit=cap)
+    o = oracle.context(P)
+    setup_tank(o, scen)
+    tm = {}
+
+    def timed(name, fn):
+        t0 = time.perf_counter()
+        fn()
+        tm[name] = tm.get(name, 0.0) + time.perf_counter() - t0
+
+    o.set_time(spec.dt, spec.dt)
+    for nm in ("piston", "projection", "cellshift", "resetid", "neighbour", "effpor", "eddyvis", "int_vel"):
+        timed(nm, getattr(o, nm))
+    P0 = sc.make_params(spec, scen.bounds, solver=solver, tol=1e-8, maxit=0)
+    o0 = oracle.context(P0)
+    t0 = time.perf_counter()
+    o.ppesolve(check=False)
+    t_solve_cap = time.perf_counter() - t0
+    # assembly-only cost: the same system with no iterations
+    setup_tank(o0, scen)
+    for nm in ("piston", "projection", "cellshift", "resetid", "neighbour", "effpor", "eddyvis", "int_vel"):
+        getattr(o0, nm)()
+    t0 = time.perf_counter()
+    o0.ppesolve(check=False)
+    t_asm = time.perf_counter() - t0
+    for nm in ("comp_vel", "comp_pos"):
+        timed(nm, getattr(o, nm))
+    timed("cellshift", lambda: o.cellshift(True))
+    for nm in ("neighbour", "freesurf", "effpor", "opt2_shift", "timestep"):
+        timed(nm, getattr(o, nm))
+    t_iter = max(t_solve_cap - t_asm, 0.0) / cap
+    t_step = sum(tm.values()) + t_asm + gpu_iters * t_iter
+    desc = (f"one step of the C++ OpenMP restatement on {scen.n_fluid} fluid particles, PPE {solver} capped at "
+            f"{cap} iterations ({t_iter*1e3:.2f} ms/iteration) and scaled to {gpu_iters:.0f} iterations; "
+            f"non-solver routines {sum(tm.values()):.2f} s, assembly {t_asm:.2f} s")
+    return scen.n_fluid / t_step, desc, t_step
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
+    ap.add_argument("--config", default=CONFIG)
+    ap.add_argument("--solver", default="bicgstab", choices=("bicgstab", "fgmres"))
+    ap.add_argument("--inner-tol", type=float, default=3e-2)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-iters", type=float, default=1850.0,
+                    help="PPE iterations per step the reference arm's sample is scaled to")
+    args = ap.parse_args()
+    dist = Dist()
+    from beach_slope_confined_gb300 import scenario as sc
+
+    threads = os.cpu_count() or 1
+    if args.impl == "reference":
+        if dist.rank == 0:
+            spec = sc.config_spec(args.config)
+            scen = sc.build(spec)
+            vals = []
+            for _ in range(args.warmup):
+                pass  # the sample has no warm state to build
+            for _ in range(max(1, args.steps)):
+                v, desc, t_step = cpu_sample(scen, spec, threads, args.cpu_iters, args.solver)
+                vals.append(v)
+            value = statistics.median(vals)
+            line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
+                    "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                    "ms_per_step": 1e3 * scen.n_fluid / value, "higher_is_better": True, "scaling": "weak",
+                    "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded wave tank)",
+                    "config": {"workload": f"{args.config} wave tank, dx={spec.dx} m, {scen.n_fluid} fluid "
+                                           f"particles, BiCGSTAB to 1e-8"},
+                    "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
+                                     "kind": "port", "sample": desc},
+                    "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                            "d2h_bytes_per_step": 0}}
+            print(json.dumps(line), flush=True)
+        dist.close()
+        return
+
+    scen, res, errs, peaks = run_ours(args, dist)
+    if dist.rank != 0:
+        dist.close()
+        return
+    spec = sc.config_spec(args.config)
+    m = res["mixed"]
+    hbm, peak_kind = measured_peak_hbm()
+    byts = spmv_bytes(m["nnz"], m["n"], fp32=True)
+    achieved = byts / (m["spmv_ms"] * 1e-3) / 1e9 if m["spmv_ms"] > 0 else None
+    tpr = traffic_per_row("fp32")
+    roofline = {"bound": "hbm", "kernel": "k_bicg_1<EllOp<float>,float> (FP32 ELL SpMV + dot)",
+                "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": (achieved / hbm) if achieved else None,
+                "traffic": (tpr * m["n"]) if tpr else None,
+                "algorithmic_bytes_per_launch": byts, "avg_launch_ms": m["spmv_ms"],
+                "launches_timed": m["spmv_calls"], "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs"}
+    fp64 = None
+    if "fp64" in res:
+        f = res["fp64"]
+        b64 = spmv_bytes(f["nnz"], f["n"], fp32=False)
+        a64 = b64 / (f["spmv_ms"] * 1e-3) / 1e9 if f["spmv_ms"] > 0 else None
+        t64 = traffic_per_row("fp64")
+        fp64 = {"value": f["value"], "ms_per_step": f["ms_per_step"], "ppe_iterations": [i[0] for i in f["iters"]],
+                "solve_ms_per_step": f["solve_ms"],
+                "roofline": {"bound": "hbm", "kernel": "k_bicg_1<EllOp<double>,double>", "achieved": a64,
+                             "peak": hbm, "unit": "GB/s", "frac": (a64 / hbm) if a64 else None,
+                             "traffic": (t64 * f["n"]) if t64 else None}}
+    cpu = None
+    if not args.no_cpu:
+        gpu_iters = statistics.mean(i[0] for i in res["fp64"]["iters"]) if "fp64" in res else args.cpu_iters
+        v, desc, _ = cpu_sample(scen, spec, threads, gpu_iters, args.solver)
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port", "sample": desc}
+    line = {
+        "metric": METRIC, "value": m["value"], "unit": "particle-steps/s", "n_gpus": dist.world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32/f64 (mixed)",
+        "data": "synthetic (seeded wave tank, no dataset)",
+        "config": {"workload": f"{args.config} wave tank 4.0x0.6 m, depth 0.30 m, dx={spec.dx} m, "
+                               f"{scen.n_fluid} fluid + {scen.n - scen.n_fluid} wall particles, Wendland C2 h=1.3dx, "
+                               f"{args.solver} PPE to rel-res 1e-8, dt={spec.dt} s",
+                   "fluid_particles": scen.n_fluid, "precision": "mixed (FP32 sweeps, FP64 refinement)",
+                   "l2": "inputs larger than L2 (particle state ~170 MB + neighbour lists ~0.9 GB)",
+                   "parallelism": f"replicas x{dist.world}"},
+        "ppe": {"iterations": [i[0] for i in m["iters"]], "refinement_sweeps": [i[1] for i in m["iters"]],
+                "rel_residual": [i[2] for i in m["iters"]]},
+        "fp64": fp64,
+        "mixed_vs_fp64_rel_l2": errs,
+        "roofline": roofline,
+        "cpu_baseline": cpu,
+        "e2e": m.get("e2e"),
+        "clocks": m["clocks"],
+        "gpu_launches": m["launches"],
+        "measured_peaks": {"fp64_gflops": peaks[0], "fp32_gflops": peaks[1], "copy_gbs": peaks[2]} if peaks else None,
+        "wcsph_adjoint_forward_ratio": None,
+    }
+    print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()
