@@ -128,17 +128,20 @@ static int alloc_solver_work(Ctx* c, int64_t n, bool fp64, bool fp32) {
     if (c->P.solver == BSC_SOLVER_FGMRES && fp64)
         if ((rc = dalloc(c, &c->V, (int64_t)(m + 1) * n))) return rc;
     if (fp32) {
+        // FGMRES-IR: FP64 outer basis V, FP32 preconditioned vectors Z, and
+        // the FP32 BiCGSTAB sweep vectors
+        c->ir_m = std::max(1, std::min(c->P.max_outer, 40));
+        if ((rc = dalloc(c, &c->V, (int64_t)(c->ir_m + 1) * n))) return rc;
+        if ((rc = dalloc(c, &c->Zf, (int64_t)c->ir_m * n))) return rc;
         if ((rc = dalloc(c, &c->xf, 9 * n))) return rc;
         c->rf = c->xf + n; c->sf = c->xf + 2 * n; c->rhf = c->xf + 3 * n; c->pf = c->xf + 4 * n;
         c->vf = c->xf + 5 * n; c->tf = c->xf + 6 * n; c->bf = c->xf + 7 * n; c->xbf = c->xf + 8 * n;
-        if (c->P.solver == BSC_SOLVER_FGMRES)
-            if ((rc = dalloc(c, &c->Vf, (int64_t)(m + 1) * n))) return rc;
     }
-    if ((rc = dalloc(c, &c->Hd, fg_layout_size(m)))) return rc;
+    if ((rc = dalloc(c, &c->Hd, fg_layout_size(64)))) return rc;
     if ((rc = dalloc(c, &c->part, (int64_t)RED_GRID * 64))) return rc;
-    if ((rc = dalloc(c, &c->sc, 1))) return rc;
-    if (!c->h_sc) BSC_CUDA(c, cudaMallocHost((void**)&c->h_sc, sizeof(Scalars)));
-    std::memset(c->h_sc, 0, sizeof(Scalars));
+    if ((rc = dalloc(c, &c->sc, 1)) || (rc = dalloc(c, &c->sc2, 1))) return rc;
+    if (!c->h_sc) BSC_CUDA(c, cudaMallocHost((void**)&c->h_sc, 2 * sizeof(Scalars)));
+    std::memset(c->h_sc, 0, 2 * sizeof(Scalars));
     return BSC_OK;
 }
 
@@ -368,6 +371,9 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
     cudaEventCreate(&c->ev_spmv[1]);
     if (const char* e = std::getenv("BSC_GRAPHS")) c->use_graphs = e[0] != '0';
     if (const char* e = std::getenv("BSC_DEBUG")) c->debug = e[0] == '1';
+    if (const char* e = std::getenv("BSC_SPMV_UNROLL")) c->spmv_unroll = e[0] == '1';
+    if (const char* e = std::getenv("BSC_PROFILE_ITER")) c->prof_iter = e[0] == '1';
+    for (int k = 0; k < 6; ++k) cudaEventCreate(&c->ev_it[k]);
     *out = c;
     return BSC_OK;
 }

@@ -162,6 +162,9 @@ struct Ctx {
     double *r = nullptr, *rh = nullptr, *pd = nullptr, *v = nullptr, *s = nullptr, *tv = nullptr, *xw = nullptr;
     float *rf = nullptr, *rhf = nullptr, *pf = nullptr, *vf = nullptr, *sf = nullptr, *tf = nullptr, *xf = nullptr;
     float* xbf = nullptr;         // best inner iterate (mixed)
+    float* Zf = nullptr;          // FGMRES-IR preconditioned vectors, ir_m x cap (mixed)
+    Scalars* sc2 = nullptr;       // FGMRES-IR outer scalars (h_sc[1] mirrors them)
+    int ir_m = 0;
     // instantiated CUDA graphs of one batch of Krylov iterations, keyed by
     // the operator and vectors they were captured with
     struct GraphEntry {
@@ -174,6 +177,9 @@ struct Ctx {
     std::vector<GraphEntry> graphs;
     bool use_graphs = true;
     bool debug = false;           // BSC_DEBUG=1: per-sweep solver trace on stderr
+    int spmv_unroll = 0;          // BSC_SPMV_UNROLL=1: four ELL entries per round
+    bool prof_iter = false;       // BSC_PROFILE_ITER=1: events around each Krylov kernel
+    cudaEvent_t ev_it[6] = {};
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64
     float* Vf = nullptr;          // FGMRES basis FP32 (mixed)
     double* Hd = nullptr;         // Hessenberg + Givens + y on device

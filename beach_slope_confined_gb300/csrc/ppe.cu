@@ -158,16 +158,16 @@ struct EllOp {
     const int32_t* nbr;
     const int32_t* cnt;
     int kmax;
+    int unroll = 0;  // 1: four entries per round (four gathers in flight)
     const void* key() const { return aval; }
-    // four entries per round so four gathers are in flight per thread; the
-    // column stride of the ELL layout is 32 slots
+    // the column stride of the ELL layout is 32 slots
     template <typename X, typename A>
     __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
         A s = (A)x[i];
         const int m = cnt[i];
         const int64_t e0 = ell(i, 0, kmax);
         int k = 0;
-        for (; k + 4 <= m; k += 4) {
+        for (; unroll && k + 4 <= m; k += 4) {
             const int64_t e = e0 + (int64_t)k * 32;
             const int j0 = nbr[e], j1 = nbr[e + 32], j2 = nbr[e + 64], j3 = nbr[e + 96];
             const T a0 = aval[e], a1 = aval[e + 32], a2 = aval[e + 64], a3 = aval[e + 96];
@@ -670,14 +670,19 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
     // graph too) so the dominant kernel's duration is measured in place
     bool first = true;
     auto one = [&]() {
+        const bool pr = first && c->prof_iter;
         if (first && c->timing) cudaEventRecord(c->ev_spmv[0], c->stream);
         k_bicg_1<Op, T><<<G, B, 0, c->stream>>>(n, A, w.p, w.v, w.rh, c->part, c->sc);
         if (first && c->timing) cudaEventRecord(c->ev_spmv[1], c->stream);
         first = false;
         k_bicg_2<T><<<G, B, 0, c->stream>>>(n, w.r, w.v, w.s, c->part, c->sc);
+        if (pr) cudaEventRecord(c->ev_it[2], c->stream);
         k_bicg_3<Op, T><<<G, B, 0, c->stream>>>(n, A, w.s, w.t, c->part, c->sc);
+        if (pr) cudaEventRecord(c->ev_it[3], c->stream);
         k_bicg_4<T><<<G, B, 0, c->stream>>>(n, w.x, w.p, w.s, w.t, w.r, w.rh, c->part, c->sc);
+        if (pr) cudaEventRecord(c->ev_it[4], c->stream);
         k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->part, c->sc, w.x, xbest, 1e3);
+        if (pr) cudaEventRecord(c->ev_it[5], c->stream);
     };
     const int batch = batch_for(n);
     int launched = 0;
@@ -692,6 +697,15 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
             if (cudaEventElapsedTime(&ms, c->ev_spmv[0], c->ev_spmv[1]) == cudaSuccess) {
                 c->ms[BSC_T_SPMV] += ms;
                 c->calls[BSC_T_SPMV]++;
+            }
+            if (c->prof_iter) {
+                const cudaEvent_t ev[6] = {c->ev_spmv[0], c->ev_spmv[1], c->ev_it[2], c->ev_it[3], c->ev_it[4],
+                                           c->ev_it[5]};
+                for (int k = 0; k < 5; ++k)
+                    if (cudaEventElapsedTime(&ms, ev[k], ev[k + 1]) == cudaSuccess) {
+                        c->ms[BSC_T_BICG_1 + k] += ms;
+                        c->calls[BSC_T_BICG_1 + k]++;
+                    }
             }
         }
         first = true;
@@ -796,6 +810,122 @@ __global__ void k_copy_f64(int64_t n, const double* __restrict__ a, double* __re
     GRID_LOOP(i, n) b[i] = a[i];
 }
 
+// ---- FGMRES-IR pieces (mixed path) ----------------------------------------------
+__global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+    GRID_LOOP(i, n) b[i] = (float)a[i];
+}
+
+// w = A z with the FP64 operator and an FP32 preconditioned vector
+__global__ void __launch_bounds__(RED_BLOCK) k_spmv_z(int64_t n, EllOp<double> A, const float* __restrict__ z,
+                                                       double* __restrict__ w, const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    GRID_LOOP(i, n) w[i] = A.template row<float, double>(i, z);
+}
+
+// x += sum_i y_i z_i, z_i the FP32 preconditioned vectors of the cycle
+__global__ void k_fg_update_z(int64_t n, double* __restrict__ x, const float* __restrict__ Z,
+                              const double* __restrict__ Hd, FgLayout F, const Scalars* __restrict__ sc) {
+    if (sc->done) return;
+    __shared__ double y[FG_MAXM];
+    const int k = (int)sc->tmp[1];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) y[i] = Hd[F.y(i)];
+    __syncthreads();
+    GRID_LOOP(q, n) {
+        double s = x[q];
+        for (int i = 0; i < k; ++i) s += y[i] * (double)Z[(int64_t)i * n + q];
+        x[q] = s;
+    }
+}
+
+int fetch_outer(Ctx* c) {
+    BSC_CUDA(c, cudaMemcpyAsync(c->h_sc + 1, c->sc2, sizeof(Scalars), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BSC_OK;
+}
+
+// Flexible GMRES in FP64 on the FP64 operator (outer), right-preconditioned
+// by an FP32 BiCGSTAB sweep on the FP32 copy of the operator (inner, minimum-
+// residual iterate, FP64 dot products).  The outer iteration minimises the
+// true FP64 residual over all corrections found so far, so a poor sweep only
+// costs its iterations; x converges to the FP64 system's solution.
+int run_fgmres_ir(Ctx* c, int64_t n, bsc_solve_info* si) {
+    const bsc_params& P = c->P;
+    const int G = RED_GRID, B = RED_BLOCK;
+    const int rel_r0 = P.tol_mode == BSC_TOL_REL_R0;
+    const int m = c->ir_m;
+    const FgLayout F{m};
+    const EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+    const EllOp<float> Af{c->avalf, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+    double* x = c->S.p;
+    double* w = c->tv;
+    const int budget = std::max(50, std::min(1000, P.maxit / std::max(1, P.max_outer)));
+    int first = 1, outer = 0, inner = 0;
+    for (;;) {
+        k_resid<EllOp<double>, double><<<G, B, 0, c->stream>>>(n, A, x, c->b, c->r, c->part);
+        BSC_LAUNCH(c);
+        k_fg_start<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, first, P.tol, rel_r0);
+        BSC_LAUNCH(c);
+        first = 0;
+        int rc = fetch_outer(c);
+        if (rc) return rc;
+        if (c->h_sc[1].done || outer >= P.max_outer || inner >= P.maxit) break;
+        k_fg_v0<double><<<G, B, 0, c->stream>>>(n, c->r, c->V, c->sc2);
+        BSC_LAUNCH(c);
+        for (int j = 0; j < m && outer < P.max_outer && inner < P.maxit; ++j) {
+            float* zj = c->Zf + (int64_t)j * n;
+            k_d2f<<<G, B, 0, c->stream>>>(n, c->V + (int64_t)j * n, c->rf);
+            BSC_CUDA(c, cudaMemsetAsync(c->xf, 0, sizeof(float) * n, c->stream));
+            Work<float> wk{c->xf, c->rf, c->sf, c->rhf, c->pf, c->vf, c->tf, c->bf, nullptr};
+            int it = 0;
+            double rri = 0.0;
+            rc = run_bicgstab<EllOp<float>, float>(c, n, Af, wk, P.inner_tol, 0, std::min(budget, P.maxit - inner),
+                                                   &it, &rri, zj);
+            if (rc && rc != BSC_E_BREAKDOWN) return rc;
+            inner += it;
+            ++outer;
+            // |v_j| = 1: a sweep that did not reduce it falls back to z_j = v_j
+            if (!(rri < 1.0) || !std::isfinite(rri)) k_d2f<<<G, B, 0, c->stream>>>(n, c->V + (int64_t)j * n, zj);
+            if (c->debug) std::fprintf(stderr, "[bsc] FGMRES-IR outer %d: sweep %d iterations, |r_inner|/|v| %.3e\n",
+                                       outer, it, std::sqrt(rri));
+            k_spmv_z<<<G, B, 0, c->stream>>>(n, A, zj, w, c->sc2);
+            for (int pass = 0; pass < 2; ++pass) {
+                k_fg_mdot<double><<<G, B, 0, c->stream>>>(n, c->V, w, j, c->part, c->sc2);
+                k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc2);
+                k_fg_maxpy<double><<<G, B, 0, c->stream>>>(n, c->V, w, j, c->Hd, F, pass, c->part, c->sc2);
+            }
+            k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, j);
+            k_fg_next<double><<<G, B, 0, c->stream>>>(n, w, c->V, j, c->sc2);
+            c->launches += 11;
+            BSC_CUDA(c, cudaGetLastError());
+            if ((rc = fetch_outer(c))) return rc;
+            if (c->h_sc[1].tmp[2] != 0.0) break;
+        }
+        k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc2, c->Hd, F);
+        k_fg_update_z<<<G, B, 0, c->stream>>>(n, x, c->Zf, c->Hd, F, c->sc2);
+        c->launches += 2;
+        BSC_CUDA(c, cudaGetLastError());
+        if (c->h_sc[1].breakdown && c->h_sc[1].tmp[1] == 0.0) break;
+    }
+    // true residual of the returned pressure
+    double* norms = c->Hd + F.size();
+    k_resid<EllOp<double>, double><<<G, B, 0, c->stream>>>(n, A, x, c->b, c->r, c->part);
+    BSC_LAUNCH(c);
+    k_ir_norms<<<1, B, 0, c->stream>>>(c->part, norms);
+    BSC_LAUNCH(c);
+    double nrm[2];
+    BSC_CUDA(c, cudaMemcpyAsync(nrm, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    si->iterations = inner;
+    si->outer = outer;
+    si->b_norm = c->h_sc[1].bnorm;
+    si->r0_norm = c->h_sc[1].r0norm;
+    si->rel_residual = nrm[1] > 0 ? nrm[0] / nrm[1] : nrm[0];
+    const double ref = rel_r0 ? si->r0_norm : si->b_norm;
+    si->converged = nrm[0] <= P.tol * ref ? 1 : 0;
+    si->status = si->converged ? BSC_OK : BSC_E_NOT_CONVERGED;
+    return si->status;
+}
+
 int solve_status(bsc_solve_info* info, int rc) {
     if (rc != BSC_OK) return rc;
     return info->converged ? BSC_OK : BSC_E_NOT_CONVERGED;
@@ -813,7 +943,7 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
     int rc = BSC_OK, iters = 0;
     double rr = 0.0;
     if (!c->mixed) {
-        EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax};
+        EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
         Work<double> w{c->S.p, c->b, c->r, c->rh, c->pd, c->v, c->s, c->tv, c->V};
         if (P.solver == BSC_SOLVER_FGMRES)
             rc = run_fgmres<EllOp<double>, double>(c, n, A, w, P.tol, rel_r0, P.maxit, c->fg_m, &iters, &rr);
@@ -840,62 +970,8 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
                      : (si->converged ? BSC_OK : BSC_E_NOT_CONVERGED);
         return si->status;
     }
-    // ---- mixed: FP64 iterative refinement around an FP32 inner solve
-    EllOp<float> Af{c->avalf, c->nbr, c->cnt, c->K.kmax};
-    double* x = c->S.p;
-    double* r64 = c->r;
-    double* norms = c->Hd + FgLayout{c->fg_m}.size();
-    double r0 = -1.0, bn = 0.0, rn = 0.0;
-    int outer = 0, total = 0, st = BSC_OK;
-    bool conv = false;
-    for (;;) {
-        k_ir_resid<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, EllOp<double>{c->aval, c->nbr, c->cnt, c->K.kmax}, x, c->b, r64, c->rf, c->part);
-        BSC_LAUNCH(c);
-        k_ir_norms<<<1, RED_BLOCK, 0, c->stream>>>(c->part, norms);
-        BSC_LAUNCH(c);
-        double nrm[2];
-        BSC_CUDA(c, cudaMemcpyAsync(nrm, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
-        rn = nrm[0];
-        bn = nrm[1];
-        if (r0 < 0) r0 = rn;
-        const double target = P.tol * (rel_r0 ? r0 : bn);
-        if (rn <= target) { conv = true; break; }
-        if (outer >= P.max_outer || total >= P.maxit) break;
-        ++outer;
-        // inner: A d = r (FP32), d0 = 0, relative tolerance inner_tol
-        BSC_CUDA(c, cudaMemsetAsync(c->xf, 0, sizeof(float) * n, c->stream));
-        // FP32 work: x = correction, b = residual, then r, rhat, p, v, s, t
-        Work<float> w{c->xf, c->rf, c->sf, c->rhf, c->pf, c->vf, c->tf, c->bf, c->Vf};
-        int it = 0;
-        double rri = 0;
-        // an FP32 Krylov solve stagnates near its attainable accuracy, so
-        // each sweep gets a bounded share of the iteration budget
-        const int share = std::max(50, P.maxit / std::max(1, P.max_outer));
-        const int budget = std::min(share, P.maxit - total);
-        // FGMRES minimises the residual (its iterate is the best one); the
-        // BiCGSTAB sweep returns its minimum-residual iterate
-        const bool gm = P.solver == BSC_SOLVER_FGMRES;
-        int rc2 = gm ? run_fgmres<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, c->fg_m, &it, &rri)
-                     : run_bicgstab<EllOp<float>, float>(c, n, Af, w, P.inner_tol, 0, budget, &it, &rri, c->xbf);
-        total += it;
-        if (rc2 == BSC_E_BREAKDOWN && it == 0) { st = BSC_E_BREAKDOWN; break; }
-        if (!std::isfinite(rri)) { st = BSC_E_BREAKDOWN; break; }  // keep x: the correction is unusable
-        if (c->debug)
-            std::fprintf(stderr, "[bsc] refinement sweep %d: |r|/|b| %.3e, inner iterations %d, inner |r|^2 ratio %.3e\n",
-                         outer, rn / bn, it, rri / ((double)rn * rn));
-        if (!(rri < (double)rn * rn)) { st = BSC_E_NOT_CONVERGED; break; }  // the sweep made no progress
-        k_ir_add<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(n, x, gm ? c->xf : c->xbf);
-        BSC_LAUNCH(c);
-    }
-    si->iterations = total;
-    si->outer = outer;
-    si->converged = conv ? 1 : 0;
-    si->b_norm = bn;
-    si->r0_norm = r0;
-    si->rel_residual = bn > 0 ? rn / bn : rn;
-    si->status = conv ? BSC_OK : (st != BSC_OK ? st : BSC_E_NOT_CONVERGED);
-    return si->status;
+    // ---- mixed: FGMRES-IR (FP64 outer, FP32 BiCGSTAB sweeps)
+    return run_fgmres_ir(c, n, si);
 }
 
 // ---- standalone CSR solve (device buffers allocated by the caller context) ----

@@ -299,7 +299,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--config", default=CONFIG)
     ap.add_argument("--solver", default="bicgstab", choices=("bicgstab", "fgmres"))
-    ap.add_argument("--inner-tol", type=float, default=3e-2)
+    ap.add_argument("--inner-tol", type=float, default=0.1)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-iters", type=float, default=1850.0,
