@@ -669,20 +669,22 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
     // the first SpMV of every batch is bracketed by events (recorded into the
     // graph too) so the dominant kernel's duration is measured in place
     bool first = true;
+    // external event nodes when captured into a graph, so they stay timeable
+    auto rec = [&](cudaEvent_t e) { cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal); };
     auto one = [&]() {
         const bool pr = first && c->prof_iter;
-        if (first && c->timing) cudaEventRecord(c->ev_spmv[0], c->stream);
+        if (first && c->timing) rec(c->ev_spmv[0]);
         k_bicg_1<Op, T><<<G, B, 0, c->stream>>>(n, A, w.p, w.v, w.rh, c->part, c->sc);
-        if (first && c->timing) cudaEventRecord(c->ev_spmv[1], c->stream);
+        if (first && c->timing) rec(c->ev_spmv[1]);
         first = false;
         k_bicg_2<T><<<G, B, 0, c->stream>>>(n, w.r, w.v, w.s, c->part, c->sc);
-        if (pr) cudaEventRecord(c->ev_it[2], c->stream);
+        if (pr) rec(c->ev_it[2]);
         k_bicg_3<Op, T><<<G, B, 0, c->stream>>>(n, A, w.s, w.t, c->part, c->sc);
-        if (pr) cudaEventRecord(c->ev_it[3], c->stream);
+        if (pr) rec(c->ev_it[3]);
         k_bicg_4<T><<<G, B, 0, c->stream>>>(n, w.x, w.p, w.s, w.t, w.r, w.rh, c->part, c->sc);
-        if (pr) cudaEventRecord(c->ev_it[4], c->stream);
+        if (pr) rec(c->ev_it[4]);
         k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->part, c->sc, w.x, xbest, 1e3);
-        if (pr) cudaEventRecord(c->ev_it[5], c->stream);
+        if (pr) rec(c->ev_it[5]);
     };
     const int batch = batch_for(n);
     int launched = 0;
@@ -707,6 +709,7 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
                         c->calls[BSC_T_BICG_1 + k]++;
                     }
             }
+            (void)cudaGetLastError();  // a failed diagnostic query must not fail the solve
         }
         first = true;
         if (c->use_graphs && nb == batch) {
