@@ -140,6 +140,8 @@ static int alloc_solver_work(Ctx* c, int64_t n, bool fp64, bool fp32) {
     if ((rc = dalloc(c, &c->Hd, fg_layout_size(64)))) return rc;
     if ((rc = dalloc(c, &c->part, (int64_t)RED_GRID * 64))) return rc;
     if ((rc = dalloc(c, &c->sc, 1)) || (rc = dalloc(c, &c->sc2, 1))) return rc;
+    if ((rc = dalloc(c, &c->ticket, 1))) return rc;
+    BSC_CUDA(c, cudaMemsetAsync(c->ticket, 0, sizeof(unsigned), c->stream));
     if (!c->h_sc) BSC_CUDA(c, cudaMallocHost((void**)&c->h_sc, 2 * sizeof(Scalars)));
     std::memset(c->h_sc, 0, 2 * sizeof(Scalars));
     return BSC_OK;

@@ -52,7 +52,7 @@ struct Scalars {
     double rho, alpha, omega, beta;
     double rr, bnorm, r0norm, target;
     double tmp[8];
-    int32_t done, breakdown, it, it_copy;  // it_copy: `it` as seen by the update kernel
+    int32_t done, breakdown, it, k5;  // k5: work of the last kernel of a BiCGSTAB iteration
 };
 
 // ---- kernel constants --------------------------------------------------------
@@ -164,6 +164,7 @@ struct Ctx {
     float* xbf = nullptr;         // best inner iterate (mixed)
     float* Zf = nullptr;          // FGMRES-IR preconditioned vectors, ir_m x cap (mixed)
     Scalars* sc2 = nullptr;       // FGMRES-IR outer scalars (h_sc[1] mirrors them)
+    unsigned* ticket = nullptr;   // last-block counter of the Krylov reductions (kept at 0 between launches)
     int ir_m = 0;
     // instantiated CUDA graphs of one batch of Krylov iterations, keyed by
     // the operator and vectors they were captured with
@@ -177,7 +178,7 @@ struct Ctx {
     std::vector<GraphEntry> graphs;
     bool use_graphs = true;
     bool debug = false;           // BSC_DEBUG=1: per-sweep solver trace on stderr
-    int spmv_unroll = 0;          // BSC_SPMV_UNROLL=1: four ELL entries per round
+    int spmv_unroll = 1;          // four ELL entries per round (BSC_SPMV_UNROLL=0: one)
     bool prof_iter = false;       // BSC_PROFILE_ITER=1: events around each Krylov kernel
     cudaEvent_t ev_it[6] = {};
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64

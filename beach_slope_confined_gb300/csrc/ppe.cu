@@ -232,7 +232,7 @@ __device__ __forceinline__ void reduce_partials(const double* __restrict__ part,
 #pragma unroll
     for (int d = 0; d < D; ++d) {
         double x = 0.0;
-        for (int k = threadIdx.x; k < RED_GRID; k += blockDim.x) x += part[d * RED_GRID + k];
+        for (int k = threadIdx.x; k < RED_GRID; k += blockDim.x) x += __ldcg(part + d * RED_GRID + k);
         for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
         if (lane == 0) sh[d][w] = x;
     }
@@ -277,8 +277,9 @@ __global__ void k_bicg_setup(const double* __restrict__ part, Scalars* sc, doubl
     reduce_partials<2>(part, v);
     if (threadIdx.x == 0) {
         sc->rr = v[0];
-        sc->rhob[0] = v[0];
+        sc->rho = v[0];
         sc->bestb[0] = sqrt(v[0]);
+        sc->k5 = 0;
         sc->bnorm = sqrt(v[1]);
         sc->r0norm = sqrt(v[0]);
         sc->target = tol * (rel_r0 ? sc->r0norm : sc->bnorm);
@@ -289,76 +290,88 @@ __global__ void k_bicg_setup(const double* __restrict__ part, Scalars* sc, doubl
     }
 }
 
-// v = A p; partial (rhat . v)
+// Every block writes its partial sums; the block that finishes last (ticket
+// taken after a fence) reduces them in block order and returns true, so one
+// block publishes each scalar and the consumer kernels stream without any
+// reduction of their own.  The ticket is reset by that block.
+template <int D>
+__device__ __forceinline__ bool finish_partials(double (&v)[D], double* __restrict__ part,
+                                                unsigned* __restrict__ ticket, double (&tot)[D]) {
+    block_partials<D>(v, part);
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return false;
+    __threadfence();
+    reduce_partials<D>(part, tot);
+    if (threadIdx.x == 0) *ticket = 0u;
+    return true;
+}
+
+// v = A p; alpha = rho / (rhat . v)
 template <typename Op, typename T>
 __global__ void __launch_bounds__(RED_BLOCK) k_bicg_1(int64_t n, Op A, const T* __restrict__ p, T* __restrict__ v,
                                                        const T* __restrict__ rh, double* __restrict__ part,
-                                                       const Scalars* __restrict__ sc) {
+                                                       Scalars* sc, unsigned* __restrict__ ticket) {
     if (sc->done | sc->breakdown) return;
-    double acc[1] = {0.0};
+    double acc[1] = {0.0}, d[1];
     GRID_LOOP(i, n) {
         const T vi = (T)A.template row<T, T>(i, p);
         v[i] = vi;
         acc[0] += (double)rh[i] * (double)vi;
     }
-    block_partials<1>(acc, part);
+    if (finish_partials<1>(acc, part, ticket, d) && threadIdx.x == 0) {
+        const double rho = sc->rho;
+        if (d[0] == 0.0 || rho == 0.0) sc->breakdown = 1;
+        else sc->tmp[0] = rho / d[0];
+    }
 }
 
-// alpha = rho / (rhat.v); s = r - alpha v
+// s = r - alpha v
 template <typename T>
 __global__ void __launch_bounds__(RED_BLOCK) k_bicg_2(int64_t n, const T* __restrict__ r, const T* __restrict__ v,
-                                                       T* __restrict__ s, const double* __restrict__ part,
-                                                       Scalars* sc) {
+                                                       T* __restrict__ s, const Scalars* __restrict__ sc) {
     if (sc->done | sc->breakdown) return;
-    double d[1];
-    reduce_partials<1>(part, d);
-    const double rho = sc->rhob[sc->it & 1];  // `it` was last written by the previous k_bicg_5
-    if (d[0] == 0.0 || rho == 0.0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) sc->tmp[0] = 0.0;
-        return;
-    }
-    const double alpha = rho / d[0];
-    if (blockIdx.x == 0 && threadIdx.x == 0) sc->tmp[0] = alpha;
-    const T a = (T)alpha;
+    const T a = (T)sc->tmp[0];
     GRID_LOOP(i, n) s[i] = r[i] - a * v[i];
 }
 
-// t = A s; partials (t.s, t.t)
+// t = A s; omega = (t.s)/(t.t)
 template <typename Op, typename T>
 __global__ void __launch_bounds__(RED_BLOCK) k_bicg_3(int64_t n, Op A, const T* __restrict__ s, T* __restrict__ t,
-                                                       double* __restrict__ part, const Scalars* __restrict__ sc) {
+                                                       double* __restrict__ part, Scalars* sc,
+                                                       unsigned* __restrict__ ticket) {
     if (sc->done | sc->breakdown) return;
-    double acc[2] = {0.0, 0.0};
+    double acc[2] = {0.0, 0.0}, d[2];
     GRID_LOOP(i, n) {
         const T ti = (T)A.template row<T, T>(i, s);
         t[i] = ti;
         acc[0] += (double)ti * (double)s[i];
         acc[1] += (double)ti * (double)ti;
     }
-    block_partials<2>(acc, part + 2 * RED_GRID);
+    if (finish_partials<2>(acc, part + 2 * RED_GRID, ticket, d) && threadIdx.x == 0)
+        sc->tmp[1] = (d[1] == 0.0) ? 0.0 : d[0] / d[1];
 }
 
-// omega = (t.s)/(t.t); x += alpha p + omega s; r = s - omega t; partials (r.r, rhat.r)
+// x += alpha p + omega s; r = s - omega t; then (last block) the residual
+// test, rho, beta and what k_bicg_5 has to do.  With `track` (the FP32 sweeps
+// of the mixed path) the minimum-residual iterate is kept and a sweep whose
+// residual grows past `blowup` times that minimum stops: BiCGSTAB's residual
+// is not monotone, and in FP32 on this operator it can diverge.
 template <typename T>
 __global__ void __launch_bounds__(RED_BLOCK) k_bicg_4(int64_t n, T* __restrict__ x, const T* __restrict__ p,
                                                        const T* __restrict__ s, const T* __restrict__ t,
                                                        T* __restrict__ r, const T* __restrict__ rh,
-                                                       double* __restrict__ part, Scalars* sc) {
+                                                       double* __restrict__ part, Scalars* sc,
+                                                       unsigned* __restrict__ ticket, int track, double blowup) {
     if (sc->done | sc->breakdown) return;
-    double d[2];
-    reduce_partials<2>(part + 2 * RED_GRID, d);
-    const double alpha = sc->tmp[0];
-    if (alpha == 0.0) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) sc->breakdown = 1;
-        return;
-    }
-    const double omega = (d[1] == 0.0) ? 0.0 : d[0] / d[1];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        sc->tmp[1] = omega;
-        sc->it_copy = sc->it;  // k_bicg_5 reads the copy while its block 0 advances `it`
-    }
+    const double alpha = sc->tmp[0], omega = sc->tmp[1];
     const T a = (T)alpha, w = (T)omega;
-    double acc[2] = {0.0, 0.0};
+    double acc[2] = {0.0, 0.0}, d[2];
     GRID_LOOP(i, n) {
         const T si = s[i];
         x[i] = x[i] + a * p[i] + w * si;
@@ -367,47 +380,45 @@ __global__ void __launch_bounds__(RED_BLOCK) k_bicg_4(int64_t n, T* __restrict__
         acc[0] += (double)ri * (double)ri;
         acc[1] += (double)rh[i] * (double)ri;
     }
-    block_partials<2>(acc, part + 4 * RED_GRID);
-}
-
-// convergence, beta, p = r + beta (p - omega v)
-// With `xbest` set (the FP32 inner solve of the mixed path) the iterate of
-// smallest residual is kept and a sweep whose residual grows past `blowup`
-// times that minimum stops: BiCGSTAB's residual is not monotone, and in FP32
-// on this operator it can diverge, while refinement needs a correction that
-// does not increase the residual.
-template <typename T>
-__global__ void __launch_bounds__(RED_BLOCK) k_bicg_5(int64_t n, T* __restrict__ p, const T* __restrict__ r,
-                                                       const T* __restrict__ v, const double* __restrict__ part,
-                                                       Scalars* sc, const T* __restrict__ x,
-                                                       T* __restrict__ xbest, double blowup) {
-    if (sc->done | sc->breakdown) return;
-    double d[2];
-    reduce_partials<2>(part + 4 * RED_GRID, d);
-    // every block derives the same scalars; block 0 publishes them for the
-    // next kernels (rho and best go to the other parity slot, never read here)
-    const int g = sc->it_copy, par = g & 1;
-    const double alpha = sc->tmp[0], omega = sc->tmp[1], rho = sc->rhob[par], best = sc->bestb[par];
-    const double rn = sqrt(d[0]);
-    const bool conv = rn <= sc->target;
-    const bool improved = rn < best;
-    const bool stop = xbest && !conv && (!(rn == rn) || rn > blowup * best);
-    const bool brk = !conv && !stop && (omega == 0.0 || d[1] == 0.0);
-    const double beta = brk || conv || stop ? 0.0 : (d[1] / rho) * (alpha / omega);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (finish_partials<2>(acc, part + 4 * RED_GRID, ticket, d) && threadIdx.x == 0) {
+        const double rn = sqrt(d[0]), best = sc->bestb[0], rho = sc->rho;
+        const bool conv = rn <= sc->target;
+        const bool improved = rn < best;
+        const bool stop = track && !conv && (!(rn == rn) || rn > blowup * best);
+        const bool brk = !conv && !stop && (omega == 0.0 || d[1] == 0.0);
+        sc->tmp[2] = (conv || stop || brk) ? 0.0 : (d[1] / rho) * (alpha / omega);
         sc->rr = d[0];
-        sc->rhob[par ^ 1] = d[1];
-        sc->bestb[par ^ 1] = improved ? rn : best;
-        sc->it = g + 1;
+        sc->rho = d[1];
+        if (improved) sc->bestb[0] = rn;
+        sc->it += 1;
         sc->done = (conv || stop) ? 1 : 0;
         sc->breakdown = brk ? 1 : 0;
+        sc->k5 = ((track && improved) ? 1 : 0) | ((conv || stop || brk) ? 0 : 2);
     }
-    if (xbest && improved) {
+}
+
+// bit 1: keep x as the best iterate; bit 2: p = r + beta (p - omega v)
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_bicg_5(int64_t n, T* __restrict__ p, const T* __restrict__ r,
+                                                       const T* __restrict__ v, Scalars* sc, const T* __restrict__ x,
+                                                       T* __restrict__ xbest, unsigned* __restrict__ ticket) {
+    const int mode = sc->k5;
+    if (mode == 0) return;
+    if ((mode & 1) && xbest) {
         GRID_LOOP(i, n) xbest[i] = x[i];
     }
-    if (conv || brk || stop) return;
-    const T bt = (T)beta, w = (T)omega;
-    GRID_LOOP(i, n) p[i] = r[i] + bt * (p[i] - w * v[i]);
+    if (mode & 2) {
+        const T bt = (T)sc->tmp[2], w = (T)sc->tmp[1];
+        GRID_LOOP(i, n) p[i] = r[i] + bt * (p[i] - w * v[i]);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(ticket, 1u) == gridDim.x - 1) {  // every block has read `mode`
+            sc->k5 = 0;
+            *ticket = 0u;
+        }
+    }
 }
 
 // ============================================================================
@@ -674,16 +685,17 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
     auto one = [&]() {
         const bool pr = first && c->prof_iter;
         if (first && c->timing) rec(c->ev_spmv[0]);
-        k_bicg_1<Op, T><<<G, B, 0, c->stream>>>(n, A, w.p, w.v, w.rh, c->part, c->sc);
+        k_bicg_1<Op, T><<<G, B, 0, c->stream>>>(n, A, w.p, w.v, w.rh, c->part, c->sc, c->ticket);
         if (first && c->timing) rec(c->ev_spmv[1]);
         first = false;
-        k_bicg_2<T><<<G, B, 0, c->stream>>>(n, w.r, w.v, w.s, c->part, c->sc);
+        k_bicg_2<T><<<G, B, 0, c->stream>>>(n, w.r, w.v, w.s, c->sc);
         if (pr) rec(c->ev_it[2]);
-        k_bicg_3<Op, T><<<G, B, 0, c->stream>>>(n, A, w.s, w.t, c->part, c->sc);
+        k_bicg_3<Op, T><<<G, B, 0, c->stream>>>(n, A, w.s, w.t, c->part, c->sc, c->ticket);
         if (pr) rec(c->ev_it[3]);
-        k_bicg_4<T><<<G, B, 0, c->stream>>>(n, w.x, w.p, w.s, w.t, w.r, w.rh, c->part, c->sc);
+        k_bicg_4<T><<<G, B, 0, c->stream>>>(n, w.x, w.p, w.s, w.t, w.r, w.rh, c->part, c->sc, c->ticket,
+                                            xbest != nullptr, 1e3);
         if (pr) rec(c->ev_it[4]);
-        k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->part, c->sc, w.x, xbest, 1e3);
+        k_bicg_5<T><<<G, B, 0, c->stream>>>(n, w.p, w.r, w.v, c->sc, w.x, xbest, c->ticket);
         if (pr) rec(c->ev_it[5]);
     };
     const int batch = batch_for(n);
@@ -728,7 +740,7 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
     }
     *iters = c->h_sc->it;
     if (xbest) {
-        const double b = c->h_sc->bestb[c->h_sc->it & 1];
+        const double b = c->h_sc->bestb[0];
         *rr_out = b * b;
     } else {
         *rr_out = c->h_sc->rr;
