@@ -15,10 +15,11 @@
 // host can queue a batch of iterations and test convergence once per batch.
 // Reductions are two-stage with a fixed grid, hence deterministic.
 //
-// Mixed precision: the pair sums of the assembly run in FP32, the inner
-// Krylov solve runs in FP32 with FP64 dot products and norms, and an FP64
-// iterative-refinement loop (true residual b - A x in FP64) drives the
-// relative residual to the requested tolerance.
+// Mixed precision: the matrix is assembled in FP64 in both paths and the
+// mixed path keeps an FP32 copy of it.  Its solve is FGMRES-IR: a flexible
+// GMRES outer loop in FP64 (true residual b - A x in FP64) whose
+// preconditioner is a short FP32 BiCGSTAB sweep with FP64 dot products; a
+// breakdown of BiCGSTAB restarts it from the current iterate.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -287,6 +288,20 @@ __global__ void k_bicg_setup(const double* __restrict__ part, Scalars* sc, doubl
         sc->breakdown = 0;
         sc->it = 0;
         sc->alpha = sc->omega = 1.0;
+    }
+}
+
+// restart after a breakdown: k_bicg_init has set r = rhat = p = b - A x from
+// the current iterate; the target, iteration count and best residual carry on
+__global__ void k_bicg_restart(const double* __restrict__ part, Scalars* sc) {
+    double v[2];
+    reduce_partials<2>(part, v);
+    if (threadIdx.x == 0) {
+        sc->rr = v[0];
+        sc->rho = v[0];
+        sc->k5 = 0;
+        sc->done = (sqrt(v[0]) <= sc->target) ? 1 : 0;
+        sc->breakdown = (v[0] == 0.0 && !sc->done) ? 1 : 0;
     }
 }
 
@@ -680,8 +695,13 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
     // the first SpMV of every batch is bracketed by events (recorded into the
     // graph too) so the dominant kernel's duration is measured in place
     bool first = true;
-    // external event nodes when captured into a graph, so they stay timeable
-    auto rec = [&](cudaEvent_t e) { cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal); };
+    // external event nodes when captured into a graph, so they stay
+    // timeable; a plain record on the uncaptured tail batch
+    bool capturing = false;
+    auto rec = [&](cudaEvent_t e) {
+        if (capturing) cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal);
+        else cudaEventRecord(e, c->stream);
+    };
     auto one = [&]() {
         const bool pr = first && c->prof_iter;
         if (first && c->timing) rec(c->ev_spmv[0]);
@@ -699,11 +719,22 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
         if (pr) rec(c->ev_it[5]);
     };
     const int batch = batch_for(n);
-    int launched = 0;
+    constexpr int kMaxRestarts = 8;
+    int launched = 0, restarts = 0;
     for (;;) {
         int rc = fetch_scalars(c);
         if (rc) return rc;
         const Scalars& h = *c->h_sc;
+        if (h.breakdown && !h.done && h.it < maxit && restarts < kMaxRestarts) {
+            // rho or omega vanished: restart from x with a fresh shadow residual
+            ++restarts;
+            k_bicg_init<Op, T><<<G, B, 0, c->stream>>>(n, A, w.x, w.b, w.r, w.rh, w.p, c->part);
+            BSC_LAUNCH(c);
+            k_bicg_restart<<<1, B, 0, c->stream>>>(c->part, c->sc);
+            BSC_LAUNCH(c);
+            c->launches += 2;
+            continue;
+        }
         if (h.done || h.breakdown || h.it >= maxit || launched >= maxit) break;
         const int nb = std::min(batch, maxit - h.it);
         if (launched > 0 && c->timing) {  // the previous batch has completed (fetch_scalars synced)
@@ -727,7 +758,9 @@ int run_bicgstab(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_
         if (c->use_graphs && nb == batch) {
             cudaGraphExec_t ge = nullptr;
             rc = batch_graph(c, A.key(), (const void*)w.x, (const void*)xbest, n, [&]() {
+                capturing = true;
                 for (int q = 0; q < batch; ++q) one();
+                capturing = false;
             }, &ge);
             if (rc) return rc;
             BSC_CUDA(c, cudaGraphLaunch(ge, c->stream));

@@ -253,9 +253,13 @@ def build(spec: TankSpec) -> Scenario:
 
     scen_stub = Scenario(spec, *([np.empty(0)] * 15), por_grid, por_origin, por_step, ())
 
-    # ---- porous solid lattice below the slope line
-    si, sj = np.meshgrid(np.arange(int(round(spec.toe_x / dx)), nx),
-                         np.arange(int(math.ceil(top / dx)) + 1), indexing="ij")
+    # ---- porous solid lattice below the slope line.  Like the soil lattice of
+    # boundary.f90:532-533 (which starts three spacings inside the walls) it
+    # runs under the bottom wall and behind the right wall for a full kernel
+    # support, so the smoothed porosity of effpor has no wall deficit.
+    ext = int(math.ceil(2.0 * h / dx))
+    si, sj = np.meshgrid(np.arange(int(round(spec.toe_x / dx)), nx + ext),
+                         np.arange(-ext, int(math.ceil(top / dx)) + 1), indexing="ij")
     sx = (si.ravel() + 0.5) * dx
     sy = (sj.ravel() + 0.5) * dx
     keep = below_slope(sx, sy)
@@ -278,7 +282,9 @@ def build(spec: TankSpec) -> Scenario:
         xs = (np.arange(i_left, i_right) + 0.5) * dx
         walls.append((xs, np.full(xs.size, -(k + 0.5) * dx), tid, 0))
         ys = (np.arange(nyw) + 0.5) * dx
-        walls.append((np.full(ys.size, spec.length + (k + 0.5) * dx), ys, tid, 0))
+        # the right wall closes the fluid lattice at nx * dx, so the wall gap
+        # stays one spacing when length / dx is not a whole number
+        walls.append((np.full(ys.size, (nx + k + 0.5) * dx), ys, tid, 0))
         walls.append((np.full(ys.size, -(k + 0.5) * dx), ys, tid, FLAG_PISTON))
     wx = np.concatenate([w[0] for w in walls])
     wy = np.concatenate([w[1] for w in walls])

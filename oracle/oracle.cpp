@@ -319,13 +319,23 @@ int bicgstab(const bsc_params& P, const std::vector<int64_t>& rp, const std::vec
     const double r0n = std::sqrt(dot(rs, rs));
     info->b_norm = bn;
     info->r0_norm = r0n;
-    int it = 0, status = BSC_OK, conv = tol_met(P, r0n, bn, r0n) ? 1 : 0;
+    int it = 0, status = BSC_OK, conv = tol_met(P, r0n, bn, r0n) ? 1 : 0, restarts = 0;
     while (!conv && it < P.maxit) {
+        if (status == BSC_E_BREAKDOWN) {
+            // rho or omega vanished: restart from x with a fresh shadow residual
+            if (restarts == 8) break;
+            ++restarts;
+            status = BSC_OK;
+            spmv(rp, cl, vl, x, mm1);
+#pragma omp parallel for schedule(static)
+            for (int64_t k = 0; k < n; ++k) { rs[k] = b[k] - mm1[k]; p[k] = rs[k]; res[k] = rs[k]; }
+            if (tol_met(P, std::sqrt(dot(rs, rs)), bn, r0n)) { conv = 1; break; }
+        }
         ++it;
         spmv(rp, cl, vl, p, mm1);
         double prevr = dot(res, rs);
         double den = dot(mm1, res);
-        if (prevr == 0.0 || den == 0.0) { status = BSC_E_BREAKDOWN; break; }
+        if (prevr == 0.0 || den == 0.0) { status = BSC_E_BREAKDOWN; --it; continue; }
         double alpha = prevr / den;
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n; ++k) si[k] = rs[k] - alpha * mm1[k];
@@ -339,7 +349,7 @@ int bicgstab(const bsc_params& P, const std::vector<int64_t>& rp, const std::vec
         }
         double rn = std::sqrt(dot(rs, rs));
         if (tol_met(P, rn, bn, r0n)) { conv = 1; break; }
-        if (wi == 0.0) { status = BSC_E_BREAKDOWN; break; }
+        if (wi == 0.0) { status = BSC_E_BREAKDOWN; continue; }
         double betas = (dot(rs, res) / prevr) * (alpha / wi);
 #pragma omp parallel for schedule(static)
         for (int64_t k = 0; k < n; ++k) p[k] = rs[k] + betas * (p[k] - wi * mm1[k]);
