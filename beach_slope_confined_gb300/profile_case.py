@@ -1,0 +1,45 @@
+"""A short, bounded run of the ISPH step for kernel profiling.
+
+    python -m beach_slope_confined_gb300.profile_case c3 mixed 10
+
+builds the named wave-tank case, uploads it and runs ``steps`` (default 1)
+full steps with every PPE solve capped at ``maxit`` Krylov iterations, so a
+profiler sees a few launches of each kernel of the step on the full-size
+state.  A capped solve reports BSC_E_NOT_CONVERGED, which is expected here
+and ignored; any other error raises.  Prints ``ok`` and the particle count.
+"""
+from __future__ import annotations
+
+import argparse
+
+from . import BscError, Solver, scenario as sc, setup_tank
+
+NOT_CONVERGED = -5
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("config", nargs="?", default="c3")
+    ap.add_argument("precision", nargs="?", default="mixed", choices=("mixed", "fp64"))
+    ap.add_argument("maxit", nargs="?", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=1)
+    args = ap.parse_args(argv)
+    spec = sc.config_spec(args.config)
+    scen = sc.build(spec)
+    P = sc.make_params(spec, scen.bounds, precision=args.precision, tol=1e-8, maxit=args.maxit,
+                       inner_tol=0.1, max_outer=4)
+    g = Solver(P)
+    setup_tank(g, scen)
+    for _ in range(args.steps):
+        try:
+            g.step(1)
+        except BscError as e:
+            if e.code != NOT_CONVERGED:
+                raise
+    g.synchronize()
+    g.close()
+    print("ok", scen.n)
+
+
+if __name__ == "__main__":
+    main()
