@@ -47,6 +47,22 @@ def solve_csr(params: Params, rowptr, col, val, b, x0):
     return csr_solve(lib(), "bsc_", params, rowptr, col, val, b, x0)
 
 
+def solve_csr_noalloc(params: Params, n: int, rowptr_ptr: int, col_ptr: int, val_ptr: int, b_ptr: int,
+                      x_ptr: int, stream: int = 0):
+    """bsc_csr_solve_noalloc: BiCGSTAB on a CSR matrix already in device
+    memory, for hosts that may not allocate on the device.  The arguments are
+    raw device addresses (int32 rowptr[n+1], int32 col, float64 val, b, x) and
+    a cudaStream_t as an integer (0: the legacy default stream).  x is solved
+    in place.  Returns (status, SolveInfo)."""
+    f = lib().bsc_csr_solve_noalloc
+    f.argtypes = [ctypes.POINTER(Params), ctypes.c_int32] + [ctypes.c_void_p] * 6 + [ctypes.POINTER(SolveInfo)]
+    f.restype = ctypes.c_int
+    info = SolveInfo()
+    rc = f(ctypes.byref(params), int(n), rowptr_ptr, col_ptr, val_ptr, b_ptr, x_ptr, stream or None,
+           ctypes.byref(info))
+    return rc, info
+
+
 def default_params(dl: float) -> Params:
     p = Params()
     rc = lib().bsc_default_params(ctypes.byref(p), dl)

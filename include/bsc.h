@@ -239,6 +239,27 @@ int bsc_csr_solve(const bsc_params* p, int32_t n, const int32_t* rowptr,
                   const int32_t* col, const double* val, const double* b,
                   double* x, bsc_solve_info* info);
 
+/* The same BiCGSTAB solve for callers that may not allocate device memory:
+ * a program whose own pool or caching allocator holds the GPU's memory, where
+ * a library's cudaMalloc could fail and its cudaFree would stall the device.
+ * No counterpart in the reference: it exists for such hosts only.
+ *  - rowptr, col, val, b, x are DEVICE pointers owned by the caller; x holds
+ *    the initial guess on entry and the solution on return.  Work is queued
+ *    on `stream` (NULL: the legacy default stream) and the call returns once
+ *    it has finished.
+ *  - Nothing is allocated: the work vectors live in a fixed device array of
+ *    the library sized for n <= BSC_NOALLOC_MAX_ROWS rows (about 6.3 MB).
+ *    Larger n returns BSC_E_CAPACITY; host pointers, a solver other than
+ *    BSC_SOLVER_BICGSTAB, or n <= 0 return BSC_E_INVALID.
+ *  - The first call on each device looks up that array's device address;
+ *    make it before any stream capture begins.
+ *  - All calls share the array: calls whose work overlaps on the GPU (other
+ *    streams, other host threads) race and must be serialised by the caller. */
+#define BSC_NOALLOC_MAX_ROWS 131072
+int bsc_csr_solve_noalloc(const bsc_params* p, int32_t n, const int32_t* rowptr,
+                          const int32_t* col, const double* val, const double* b,
+                          double* x, void* stream, bsc_solve_info* info);
+
 /* ---- hardware probes ---------------------------------------------------- */
 /* Measured FP64 and FP32 FMA throughput (GFLOP/s, 2 flops per FMA) and a
  * device-to-device copy bandwidth (GB/s, read+write) on the current device. */
