@@ -100,6 +100,7 @@ static void free_all(Ctx* c) {
     c->graphs.clear();
     for (void* p : c->allocs) cudaFree(p);
     c->allocs.clear();
+    mg_free(c);
     if (c->h_sc) cudaFreeHost(c->h_sc);
     if (c->h_flag) cudaFreeHost(c->h_flag);
     c->h_sc = nullptr;
@@ -343,6 +344,11 @@ int bsc_default_params(bsc_params* p, double dl) {
     p->inner_tol = 1e-4;
     p->max_neighbors = 64;
     p->reorder_every = 20;
+    p->precond = BSC_PRECOND_NONE;
+    p->mg_omega = 0.8;
+    p->mg_scale = 1.5;
+    p->mg_sweeps = 2;
+    p->mg_coarse_max = MG_COARSE_MAX;
     return BSC_OK;
 }
 
@@ -353,7 +359,11 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
         !(p->tol > 0) || (p->solver != BSC_SOLVER_BICGSTAB && p->solver != BSC_SOLVER_FGMRES) ||
         (p->precision != BSC_PREC_FP64 && p->precision != BSC_PREC_MIXED) ||
         (p->kernel != BSC_KERNEL_HYBRID && p->kernel != BSC_KERNEL_WENDLAND_C2) || p->piston_modes < 0 ||
-        p->piston_modes > BSC_MAX_PISTON_MODES)
+        p->piston_modes > BSC_MAX_PISTON_MODES || (p->precond != BSC_PRECOND_NONE && p->precond != BSC_PRECOND_MG))
+        return BSC_E_INVALID;
+    if (p->precond == BSC_PRECOND_MG &&
+        (!(p->mg_omega > 0 && p->mg_omega < 2) || !(p->mg_scale > 0) || p->mg_sweeps < 1 || p->mg_sweeps > 8 ||
+         p->mg_coarse_max < 4 || p->mg_coarse_max > MG_COARSE_MAX))
         return BSC_E_INVALID;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BSC_E_NOT_BUILT;

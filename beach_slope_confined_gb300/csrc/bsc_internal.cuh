@@ -114,6 +114,35 @@ template <> struct Vec2<float> { using type = float2; };
 inline unsigned blocks_for(int64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
 // ---- the context ---------------------------------------------------------------
+// ---- cell-aggregation multigrid (mg.cu) -------------------------------------
+// Level 0 is the PPE in the neighbour-list layout; level 1 aggregates the
+// particles of each neighbour-search cell; every further level merges 2x2
+// cells.  Levels >= 1 are structured grids with 9-point stencils.
+constexpr int MG_MAX_LEVELS = 24;
+constexpr int MG_COARSE_MAX = 128;  // cells of the coarsest level (dense inverse)
+struct MgLevel {
+    int nx = 0, ny = 0;            // cells; index cx * ny + cy
+    int64_t nc = 0;
+    double* A = nullptr;           // 9 x nc, stencil-major: A[s * nc + c], s = (dx+1)*3 + (dy+1)
+    double* dinv = nullptr;        // 1 / centre coefficient, 0 on empty cells
+    float* Af = nullptr;           // FP32 copies (mixed path)
+    float* dinvf = nullptr;
+    void *b = nullptr, *x = nullptr, *y = nullptr, *t = nullptr;  // V-cycle vectors (FP64 or FP32)
+};
+struct Mg {
+    int nlev = 0;                  // levels 1..nlev are structured; nlev is solved densely
+    MgLevel L[MG_MAX_LEVELS + 1];
+    double* cinv = nullptr;        // inverse of the coarsest level, FP64, row-major
+    int64_t n = 0;                 // rows the buffers are sized for
+    int gx = 0, gy = 0;            // level-1 grid they are sized for
+    int m = 0;                     // FGMRES restart length
+    bool f32 = false;
+    void *r0 = nullptr, *y0 = nullptr, *t0 = nullptr;  // fine-level V-cycle vectors
+    double* V = nullptr;           // FGMRES basis (m+1) x n
+    void* Z = nullptr;             // preconditioned vectors m x n (FP64 or FP32)
+    std::vector<void*> allocs;
+};
+
 struct Ctx {
     bsc_params P{};
     KParams K{};
@@ -199,6 +228,7 @@ struct Ctx {
     bool timing = true;
     cudaEvent_t ev_spmv[2] = {};  // around one SpMV per Krylov batch
     double* stepsc = nullptr;     // device: umax, numax (timestep reductions)
+    Mg mg;                        // multigrid preconditioner of the PPE (mg.cu)
 };
 
 void timing_flush(Ctx* c);
@@ -239,6 +269,12 @@ int op_probe_eta(Ctx* c, int np, const double* xp, double depth, double* eta);
 // ppe.cu
 int op_ppe_assemble(Ctx* c);
 int op_ppe_solve(Ctx* c, bsc_solve_info* info);
+// multigrid: build the hierarchy for the assembled PPE; apply one V-cycle
+// z = M v to an FP64 vector (FP64 or FP32 arithmetic); release the buffers
+int mg_setup(Ctx* c);
+int mg_vcycle_f64(Ctx* c, const double* v, double* z);
+int mg_vcycle_f32(Ctx* c, const double* v, float* z);
+void mg_free(Ctx* c);
 int fg_layout_size(int m);
 int csr_solve_device(Ctx* c, int32_t n, const int32_t* rp, const int32_t* col, const double* val,
                      const double* b, double* x, bsc_solve_info* info);

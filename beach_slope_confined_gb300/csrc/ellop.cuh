@@ -1,0 +1,47 @@
+// ellop.cuh -- the PPE operator in the neighbour-list (ELL) layout, shared by
+// the Krylov solvers (ppe.cu) and the multigrid preconditioner (mg.cu).
+#pragma once
+#include "bsc_internal.cuh"
+
+namespace bsc {
+
+// grid-stride loop over [0, n)
+#define GRID_LOOP(i, n) \
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
+
+// The Jacobi-scaled PPE matrix I + N: unit diagonal (not stored), the
+// off-diagonals N in the slots of the neighbour lists.
+template <typename T>
+struct EllOp {
+    const T* aval;
+    const int32_t* nbr;
+    const int32_t* cnt;
+    int kmax;
+    int unroll = 0;  // 1: four entries per round (four gathers in flight)
+    const void* key() const { return aval; }
+    // the column stride of the ELL layout is 32 slots
+    template <typename X, typename A>
+    __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
+        A s = (A)x[i];
+        const int m = cnt[i];
+        const int64_t e0 = ell(i, 0, kmax);
+        int k = 0;
+        for (; unroll && k + 4 <= m; k += 4) {
+            const int64_t e = e0 + (int64_t)k * 32;
+            const int j0 = nbr[e], j1 = nbr[e + 32], j2 = nbr[e + 64], j3 = nbr[e + 96];
+            const T a0 = aval[e], a1 = aval[e + 32], a2 = aval[e + 64], a3 = aval[e + 96];
+            const X x0 = x[j0], x1 = x[j1], x2 = x[j2], x3 = x[j3];
+            s += (A)a0 * (A)x0;
+            s += (A)a1 * (A)x1;
+            s += (A)a2 * (A)x2;
+            s += (A)a3 * (A)x3;
+        }
+        for (; k < m; ++k) {
+            const int64_t e = e0 + (int64_t)k * 32;
+            s += (A)aval[e] * (A)x[nbr[e]];
+        }
+        return s;
+    }
+};
+
+}  // namespace bsc

@@ -1,0 +1,561 @@
+// mg.cu -- cell-aggregation multigrid preconditioner for the PPE.
+//
+// The reference solves the PPE with unpreconditioned Krylov methods (MKL
+// dfgmres, solver.f90:306-347; BiCGSTAB, solver.f90:129-254), whose iteration
+// count grows with the resolution (about 1400 BiCGSTAB iterations at 0.85 M
+// particles).  This preconditioner keeps the same matrix and the same
+// stopping test and only changes how fast the Krylov method gets there.
+//
+// Hierarchy (rebuilt for every assembled matrix):
+//  - level 0: the Jacobi-scaled PPE I + N in the neighbour-list layout;
+//  - level 1: one unknown per neighbour-search cell (side >= 2h), the sum of
+//    its particles' unknowns (piecewise-constant aggregation).  Every
+//    neighbour of a particle lies in the 3x3 cells around it, so the Galerkin
+//    operator P^T A P is a 9-point stencil on the cell grid;
+//  - level l+1: 2x2 blocks of level-l cells, again a 9-point stencil;
+//  - the coarsest level (<= mg_coarse_max cells) is inverted densely.
+// Every coarse operator is summed by one thread per coarse cell in a fixed
+// order, so the hierarchy is deterministic.
+//
+// V-cycle: mg_sweeps damped-Jacobi sweeps before and after the coarse
+// correction on every level (weight mg_omega), the correction prolonged by
+// injection and scaled by mg_scale (plain aggregation under-corrects smooth
+// error; a factor of about 1.5 restores it).  The first pre-sweep from a
+// zero guess and the prolongation are folded into the neighbouring sweep.
+#include <algorithm>
+#include <cmath>
+
+#include "bsc_internal.cuh"
+#include "ellop.cuh"
+
+namespace bsc {
+
+namespace {
+
+constexpr int MG_BLOCK = 256;
+
+__device__ __forceinline__ int stencil_slot(int dx, int dy) { return (dx + 1) * 3 + (dy + 1); }
+
+// ---- hierarchy ----------------------------------------------------------------
+// level 1 from the fine matrix: thread per cell, its particles in the cell
+// list's (id-sorted) order, each particle's row in neighbour-list order
+__global__ void k_mg_galerkin0(int nx, int ny, const int32_t* __restrict__ cell_start,
+                               const int32_t* __restrict__ cell_count, const int32_t* __restrict__ sorted,
+                               const int32_t* __restrict__ pcell, EllOp<double> A, double* __restrict__ Ac,
+                               double* __restrict__ dinv) {
+    const int64_t nc = (int64_t)nx * ny;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int cx = (int)(c / ny), cy = (int)(c % ny);
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int q0 = cell_start[c], qn = cell_count[c];
+    for (int q = q0; q < q0 + qn; ++q) {
+        const int i = sorted[q];
+        acc[4] += 1.0;  // the unit diagonal
+        const int m = A.cnt[i];
+        const int64_t e0 = ell(i, 0, A.kmax);
+        for (int k = 0; k < m; ++k) {
+            const int64_t e = e0 + (int64_t)k * 32;
+            const int cj = pcell[A.nbr[e]];
+            const int dx = cj / ny - cx, dy = cj % ny - cy;
+            if (dx < -1 || dx > 1 || dy < -1 || dy > 1) continue;  // cannot happen: lists come from the 3x3 cells
+            acc[stencil_slot(dx, dy)] += A.aval[e];
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 9; ++s) Ac[s * nc + c] = acc[s];
+    dinv[c] = acc[4] != 0.0 ? 1.0 / acc[4] : 0.0;
+}
+
+// level l -> l+1 over 2x2 blocks
+__global__ void k_mg_galerkin(int nxf, int nyf, const double* __restrict__ Af, int nxc, int nyc,
+                              double* __restrict__ Ac, double* __restrict__ dinv) {
+    const int64_t ncc = (int64_t)nxc * nyc, ncf = (int64_t)nxf * nyf;
+    const int64_t C = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (C >= ncc) return;
+    const int CX = (int)(C / nyc), CY = (int)(C % nyc);
+    double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    for (int a = 0; a < 2; ++a) {
+        const int fx = 2 * CX + a;
+        if (fx >= nxf) continue;
+        for (int b = 0; b < 2; ++b) {
+            const int fy = 2 * CY + b;
+            if (fy >= nyf) continue;
+            const int64_t f = (int64_t)fx * nyf + fy;
+            for (int s = 0; s < 9; ++s) {
+                const double v = Af[s * ncf + f];
+                if (v == 0.0) continue;
+                const int gx = fx + s / 3 - 1, gy = fy + s % 3 - 1;
+                if (gx < 0 || gx >= nxf || gy < 0 || gy >= nyf) continue;
+                acc[stencil_slot((gx >> 1) - CX, (gy >> 1) - CY)] += v;
+            }
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < 9; ++s) Ac[s * ncc + C] = acc[s];
+    dinv[C] = acc[4] != 0.0 ? 1.0 / acc[4] : 0.0;
+}
+
+// Dense inverse of the coarsest level by Gauss-Jordan elimination with
+// partial (row) pivoting, in place in shared memory, one CTA.  Empty cells
+// (all-zero rows) become identity rows.  A zero pivot is replaced by a tiny
+// one: the preconditioner then loses that direction but stays finite.
+__global__ void __launch_bounds__(1024) k_mg_dense_inverse(int nx, int ny, const double* __restrict__ A,
+                                                            double* __restrict__ cinv) {
+    extern __shared__ double M[];  // n x n, row-major
+    __shared__ int perm[MG_COARSE_MAX];
+    __shared__ double fcol[MG_COARSE_MAX];
+    __shared__ int piv_row;
+    __shared__ double piv_inv;
+    const int n = nx * ny;
+    const int t = threadIdx.x, T = blockDim.x;
+    for (int q = t; q < n * n; q += T) M[q] = 0.0;
+    __syncthreads();
+    for (int c = t; c < n; c += T) {
+        const int cx = c / ny, cy = c % ny;
+        bool any = false;
+        for (int s = 0; s < 9; ++s) {
+            const double v = A[(int64_t)s * n + c];
+            const int gx = cx + s / 3 - 1, gy = cy + s % 3 - 1;
+            if (v == 0.0 || gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
+            M[c * n + gx * ny + gy] += v;
+            any = true;
+        }
+        if (!any) M[c * n + c] = 1.0;
+    }
+    __syncthreads();
+    for (int k = 0; k < n; ++k) {
+        // pivot: the largest |M[i][k]| over i >= k (warp 0)
+        if (t < 32) {
+            double best = -1.0;
+            int bi = k;
+            for (int i = k + t; i < n; i += 32) {
+                const double a = fabs(M[i * n + k]);
+                if (a > best) { best = a; bi = i; }
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                const double ob = __shfl_down_sync(0xffffffffu, best, o);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (t == 0) { piv_row = bi; perm[k] = bi; }
+        }
+        __syncthreads();
+        const int p = piv_row;
+        if (p != k)
+            for (int j = t; j < n; j += T) {
+                const double a = M[k * n + j];
+                M[k * n + j] = M[p * n + j];
+                M[p * n + j] = a;
+            }
+        __syncthreads();
+        if (t == 0) {
+            double pv = M[k * n + k];
+            if (pv == 0.0) pv = 1e-300;
+            piv_inv = 1.0 / pv;
+            M[k * n + k] = 1.0;
+        }
+        __syncthreads();
+        for (int j = t; j < n; j += T) M[k * n + j] *= piv_inv;
+        for (int i = t; i < n; i += T) fcol[i] = (i == k) ? 0.0 : M[i * n + k];
+        __syncthreads();
+        for (int i = t; i < n; i += T)
+            if (i != k) M[i * n + k] = 0.0;
+        __syncthreads();
+        for (int q = t; q < n * n; q += T) {
+            const int i = q / n, j = q % n;
+            if (i != k) M[q] -= fcol[i] * M[k * n + j];
+        }
+        __syncthreads();
+    }
+    // undo the row interchanges as column interchanges, last first
+    for (int k = n - 1; k >= 0; --k) {
+        const int p = perm[k];
+        if (p != k)
+            for (int i = t; i < n; i += T) {
+                const double a = M[i * n + k];
+                M[i * n + k] = M[i * n + p];
+                M[i * n + p] = a;
+            }
+        __syncthreads();
+    }
+    for (int q = t; q < n * n; q += T) cinv[q] = M[q];
+}
+
+__global__ void k_mg_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
+    GRID_LOOP(i, n) b[i] = (float)a[i];
+}
+
+// ---- V-cycle, structured levels (l >= 1) -------------------------------------------
+// x_out = x + w D^-1 (b - A x) where the input x is
+//   MODE 0: xin;
+//   MODE 1: w D^-1 b (the first sweep from a zero guess, folded in);
+//   MODE 2: xin + scale * xc[parent] (the prolonged coarse correction, folded in).
+template <typename T, int MODE>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg_smooth(int nx, int ny, const T* __restrict__ A,
+                                                         const T* __restrict__ dinv, const T* __restrict__ b,
+                                                         const T* __restrict__ xin, const T* __restrict__ xc, int nyc,
+                                                         T scale, T w, T* __restrict__ xout) {
+    const int64_t nc = (int64_t)nx * ny;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= nc) return;
+    const int cx = (int)(c / ny), cy = (int)(c % ny);
+    auto xv = [&](int gx, int gy) -> T {
+        const int64_t g = (int64_t)gx * ny + gy;
+        if (MODE == 1) return w * dinv[g] * b[g];
+        if (MODE == 2) return xin[g] + scale * xc[(int64_t)(gx >> 1) * nyc + (gy >> 1)];
+        return xin[g];
+    };
+    T ax = 0;
+#pragma unroll
+    for (int s = 0; s < 9; ++s) {
+        const int gx = cx + s / 3 - 1, gy = cy + s % 3 - 1;
+        if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
+        const T a = A[s * nc + c];
+        if (a != (T)0) ax += a * xv(gx, gy);
+    }
+    xout[c] = xv(cx, cy) + w * dinv[c] * (b[c] - ax);
+}
+
+// one sweep from a zero guess: x = w D^-1 b
+template <typename T>
+__global__ void k_mg_jacobi0(int64_t nc, const T* __restrict__ dinv, const T* __restrict__ b, T w, T* __restrict__ x) {
+    GRID_LOOP(c, nc) x[c] = w * dinv[c] * b[c];
+}
+
+// b_c = sum over the 2x2 children of the residual b - A x
+template <typename T>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const T* __restrict__ A,
+                                                           const T* __restrict__ b, const T* __restrict__ x, int nxc,
+                                                           int nyc, T* __restrict__ bc) {
+    const int64_t ncc = (int64_t)nxc * nyc, nc = (int64_t)nx * ny;
+    const int64_t C = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (C >= ncc) return;
+    const int CX = (int)(C / nyc), CY = (int)(C % nyc);
+    T sum = 0;
+    for (int a = 0; a < 2; ++a) {
+        const int fx = 2 * CX + a;
+        if (fx >= nx) continue;
+        for (int bb = 0; bb < 2; ++bb) {
+            const int fy = 2 * CY + bb;
+            if (fy >= ny) continue;
+            const int64_t f = (int64_t)fx * ny + fy;
+            T ax = 0;
+#pragma unroll
+            for (int s = 0; s < 9; ++s) {
+                const int gx = fx + s / 3 - 1, gy = fy + s % 3 - 1;
+                if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
+                const T av = A[s * nc + f];
+                if (av != (T)0) ax += av * x[(int64_t)gx * ny + gy];
+            }
+            sum += b[f] - ax;
+        }
+    }
+    bc[C] = sum;
+}
+
+// coarsest level: x = C^-1 b
+template <typename T>
+__global__ void k_mg_dense_apply(int n, const double* __restrict__ cinv, const T* __restrict__ b, T* __restrict__ x) {
+    for (int r = threadIdx.x; r < n; r += blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < n; ++c) s += cinv[r * n + c] * (double)b[c];
+        x[r] = (T)s;
+    }
+}
+
+// ---- V-cycle, level 0 (the PPE, unit diagonal) ---------------------------------------
+// two sweeps from a zero guess: x1 = w v; x2 = x1 + w (v - A x1)
+template <typename T>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<T> A, const double* __restrict__ v, T w,
+                                                        T* __restrict__ x) {
+    GRID_LOOP(i, n) {
+        const T Av = A.template row<double, T>(i, v);
+        const T vi = (T)v[i];
+        x[i] = w * vi + w * (vi - w * Av);
+    }
+}
+
+__global__ void k_mg0_scale_f64(int64_t n, const double* __restrict__ v, double w, double* __restrict__ x) {
+    GRID_LOOP(i, n) x[i] = w * v[i];
+}
+__global__ void k_mg0_scale_f32(int64_t n, const double* __restrict__ v, float w, float* __restrict__ x) {
+    GRID_LOOP(i, n) x[i] = w * (float)v[i];
+}
+
+// x_out = x + w (v - A x)
+template <typename T>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<T> A, const double* __restrict__ v,
+                                                         const T* __restrict__ x, T w, T* __restrict__ xout) {
+    GRID_LOOP(i, n) xout[i] = x[i] + w * ((T)v[i] - A.template row<T, T>(i, x));
+}
+
+// r = v - A x
+template <typename T>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_resid(int64_t n, EllOp<T> A, const double* __restrict__ v,
+                                                         const T* __restrict__ x, T* __restrict__ r) {
+    GRID_LOOP(i, n) r[i] = (T)v[i] - A.template row<T, T>(i, x);
+}
+
+// level-1 right-hand side: the residual summed over each cell's particles
+template <typename T>
+__global__ void k_mg0_restrict(int64_t nc, const int32_t* __restrict__ cell_start, const int32_t* __restrict__ cell_count,
+                               const int32_t* __restrict__ sorted, const T* __restrict__ r, T* __restrict__ b1) {
+    GRID_LOOP(c, nc) {
+        const int q0 = cell_start[c], qn = cell_count[c];
+        T s = 0;
+        for (int q = q0; q < q0 + qn; ++q) s += r[sorted[q]];
+        b1[c] = s;
+    }
+}
+
+// first post-sweep with the prolonged level-1 correction folded in:
+// y = x + scale * x1[cell]; x_out = y + w (v - A y)
+template <typename T>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_post(int64_t n, EllOp<T> A, const double* __restrict__ v,
+                                                        const T* __restrict__ x, const T* __restrict__ x1,
+                                                        const int32_t* __restrict__ pcell, T scale, T w,
+                                                        T* __restrict__ xout) {
+    GRID_LOOP(i, n) {
+        const T yi = x[i] + scale * x1[pcell[i]];
+        T Ay = yi;
+        const int m = A.cnt[i];
+        const int64_t e0 = ell(i, 0, A.kmax);
+        for (int k = 0; k < m; ++k) {
+            const int64_t e = e0 + (int64_t)k * 32;
+            const int j = A.nbr[e];
+            Ay += A.aval[e] * (x[j] + scale * x1[pcell[j]]);
+        }
+        xout[i] = yi + w * ((T)v[i] - Ay);
+    }
+}
+
+template <typename T>
+struct Lv {
+    const T* A;
+    const T* dinv;
+    T *b, *x, *y, *t;
+};
+
+template <typename T>
+Lv<T> level_view(const MgLevel& L) {
+    if constexpr (sizeof(T) == 4)
+        return {L.Af, L.dinvf, (T*)L.b, (T*)L.x, (T*)L.y, (T*)L.t};
+    else
+        return {L.A, L.dinv, (T*)L.b, (T*)L.x, (T*)L.y, (T*)L.t};
+}
+
+template <typename T>
+EllOp<T> fine_op(Ctx* c);
+template <>
+EllOp<double> fine_op<double>(Ctx* c) {
+    return EllOp<double>{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+}
+template <>
+EllOp<float> fine_op<float>(Ctx* c) {
+    return EllOp<float>{c->avalf, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+}
+
+// approximate solve of level l >= 1 (b_l -> x_l)
+template <typename T>
+int cycle_level(Ctx* c, int l) {
+    Mg& mg = c->mg;
+    const MgLevel& L = mg.L[l];
+    Lv<T> v = level_view<T>(L);
+    const unsigned g = blocks_for(L.nc, MG_BLOCK);
+    if (l == mg.nlev) {
+        k_mg_dense_apply<T><<<1, MG_COARSE_MAX, 0, c->stream>>>((int)L.nc, mg.cinv, v.b, v.x);
+        BSC_LAUNCH(c);
+        return BSC_OK;
+    }
+    const T w = (T)c->P.mg_omega, sc = (T)c->P.mg_scale;
+    const int nu = c->P.mg_sweeps;
+    // pre-smoothing from a zero guess: one sweep is x = w D^-1 b; with two or
+    // more, the first is folded into the second
+    T* cur = v.y;
+    if (nu == 1)
+        k_mg_jacobi0<T><<<g, MG_BLOCK, 0, c->stream>>>(L.nc, v.dinv, v.b, w, cur);
+    else
+        k_mg_smooth<T, 1><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, nullptr, nullptr, 0, sc, w, cur);
+    BSC_LAUNCH(c);
+    for (int k = 2; k < nu; ++k) {
+        T* out = cur == v.y ? v.t : v.y;
+        k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w, out);
+        BSC_LAUNCH(c);
+        cur = out;
+    }
+    const MgLevel& Lc = mg.L[l + 1];
+    Lv<T> vc = level_view<T>(Lc);
+    k_mg_restrict<T><<<blocks_for(Lc.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.b, cur, Lc.nx, Lc.ny,
+                                                                             vc.b);
+    BSC_LAUNCH(c);
+    if (int rc = cycle_level<T>(c, l + 1)) return rc;
+    // post-smoothing: the prolongation folded into the first sweep; the last
+    // sweep writes x_l
+    for (int k = 0; k < nu; ++k) {
+        T* out = (k == nu - 1) ? v.x : (cur == v.y ? v.t : v.y);
+        if (k == 0)
+            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w,
+                                                             out);
+        else
+            k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w,
+                                                             out);
+        BSC_LAUNCH(c);
+        cur = out;
+    }
+    return BSC_OK;
+}
+
+template <typename T>
+int vcycle(Ctx* c, const double* vin, T* z) {
+    Mg& mg = c->mg;
+    const int64_t n = c->n;
+    const EllOp<T> A = fine_op<T>(c);
+    const T w = (T)c->P.mg_omega, sc = (T)c->P.mg_scale;
+    const int nu = c->P.mg_sweeps;
+    T *P0 = (T*)mg.y0, *Q0 = (T*)mg.t0, *R0 = (T*)mg.r0;
+    const int G = RED_GRID;
+    T* cur = P0;
+    if (nu == 1) {
+        if constexpr (sizeof(T) == 4)
+            k_mg0_scale_f32<<<G, MG_BLOCK, 0, c->stream>>>(n, vin, (float)w, (float*)cur);
+        else
+            k_mg0_scale_f64<<<G, MG_BLOCK, 0, c->stream>>>(n, vin, (double)w, (double*)cur);
+    } else {
+        k_mg0_pre2<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, cur);
+    }
+    BSC_LAUNCH(c);
+    for (int k = 2; k < nu; ++k) {
+        T* out = cur == P0 ? Q0 : P0;
+        k_mg0_sweep<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out);
+        BSC_LAUNCH(c);
+        cur = out;
+    }
+    k_mg0_resid<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, R0);
+    BSC_LAUNCH(c);
+    const MgLevel& L1 = mg.L[1];
+    Lv<T> v1 = level_view<T>(L1);
+    k_mg0_restrict<T><<<blocks_for(L1.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L1.nc, c->cell_start, c->cell_count,
+                                                                              c->sorted, R0, v1.b);
+    BSC_LAUNCH(c);
+    if (int rc = cycle_level<T>(c, 1)) return rc;
+    for (int k = 0; k < nu; ++k) {
+        T* out = (k == nu - 1) ? z : (cur == P0 ? Q0 : P0);
+        if (k == 0)
+            k_mg0_post<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, out);
+        else
+            k_mg0_sweep<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out);
+        BSC_LAUNCH(c);
+        cur = out;
+    }
+    return BSC_OK;
+}
+
+template <typename T>
+int mg_dalloc(Ctx* c, T** p, int64_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, (size_t)std::max<int64_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaMalloc (multigrid)");
+    c->mg.allocs.push_back(q);
+    *p = (T*)q;
+    return BSC_OK;
+}
+
+// buffers for the grid, the row count, the restart length and the precision
+int mg_alloc(Ctx* c) {
+    Mg& mg = c->mg;
+    const int64_t n = c->n;
+    const int m = std::max(1, std::min(c->P.restart, 64));
+    const bool f32 = c->mixed;
+    if (mg.n == n && mg.gx == c->K.nx && mg.gy == c->K.ny && mg.m == m && mg.f32 == f32 && !mg.allocs.empty())
+        return BSC_OK;
+    mg_free(c);
+    // the level dimensions
+    int nlev = 1;
+    mg.L[1].nx = c->K.nx;
+    mg.L[1].ny = c->K.ny;
+    const int64_t cmax = std::max(4, std::min(c->P.mg_coarse_max, MG_COARSE_MAX));
+    while ((int64_t)mg.L[nlev].nx * mg.L[nlev].ny > cmax) {
+        if (nlev == MG_MAX_LEVELS) return set_err(c, BSC_E_CAPACITY, "multigrid: too many levels");
+        mg.L[nlev + 1].nx = (mg.L[nlev].nx + 1) / 2;
+        mg.L[nlev + 1].ny = (mg.L[nlev].ny + 1) / 2;
+        ++nlev;
+    }
+    mg.nlev = nlev;
+    const size_t vs = f32 ? sizeof(float) : sizeof(double);
+    int rc;
+    for (int l = 1; l <= nlev; ++l) {
+        MgLevel& L = mg.L[l];
+        L.nc = (int64_t)L.nx * L.ny;
+        if ((rc = mg_dalloc(c, &L.A, 9 * L.nc)) || (rc = mg_dalloc(c, &L.dinv, L.nc))) return rc;
+        if (f32 && ((rc = mg_dalloc(c, &L.Af, 9 * L.nc)) || (rc = mg_dalloc(c, &L.dinvf, L.nc)))) return rc;
+        unsigned char* vec = nullptr;
+        if ((rc = mg_dalloc(c, &vec, (int64_t)(4 * L.nc) * (int64_t)vs))) return rc;
+        L.b = vec;
+        L.x = vec + L.nc * vs;
+        L.y = vec + 2 * L.nc * vs;
+        L.t = vec + 3 * L.nc * vs;
+    }
+    const int64_t nco = mg.L[nlev].nc;
+    if ((rc = mg_dalloc(c, &mg.cinv, nco * nco))) return rc;
+    unsigned char* fine = nullptr;
+    if ((rc = mg_dalloc(c, &fine, 3 * n * (int64_t)vs))) return rc;
+    mg.r0 = fine;
+    mg.y0 = fine + n * vs;
+    mg.t0 = fine + 2 * n * vs;
+    if ((rc = mg_dalloc(c, &mg.V, (int64_t)(m + 1) * n))) return rc;
+    unsigned char* z = nullptr;
+    if ((rc = mg_dalloc(c, &z, (int64_t)m * n * (int64_t)vs))) return rc;
+    mg.Z = z;
+    mg.n = n;
+    mg.gx = c->K.nx;
+    mg.gy = c->K.ny;
+    mg.m = m;
+    mg.f32 = f32;
+    return BSC_OK;
+}
+
+}  // namespace
+
+void mg_free(Ctx* c) {
+    Mg& mg = c->mg;
+    if (!mg.allocs.empty() && c->stream) cudaStreamSynchronize(c->stream);
+    for (void* p : mg.allocs) cudaFree(p);
+    mg.allocs.clear();
+    mg = Mg{};
+}
+
+int mg_setup(Ctx* c) {
+    if (!c->have_csr) return set_err(c, BSC_E_INVALID, "multigrid setup before assembly");
+    if (int rc = mg_alloc(c)) return rc;
+    Mg& mg = c->mg;
+    const EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, 0};
+    MgLevel& L1 = mg.L[1];
+    k_mg_galerkin0<<<blocks_for(L1.nc, 128), 128, 0, c->stream>>>(L1.nx, L1.ny, c->cell_start, c->cell_count,
+                                                                   c->sorted, c->pcell, A, L1.A, L1.dinv);
+    BSC_LAUNCH(c);
+    for (int l = 1; l < mg.nlev; ++l) {
+        const MgLevel &F = mg.L[l], &C = mg.L[l + 1];
+        k_mg_galerkin<<<blocks_for(C.nc, 128), 128, 0, c->stream>>>(F.nx, F.ny, F.A, C.nx, C.ny, C.A, C.dinv);
+        BSC_LAUNCH(c);
+    }
+    const MgLevel& Lc = mg.L[mg.nlev];
+    const int smem = (int)(Lc.nc * Lc.nc * sizeof(double));
+    BSC_CUDA(c, cudaFuncSetAttribute(k_mg_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     MG_COARSE_MAX * MG_COARSE_MAX * (int)sizeof(double)));
+    k_mg_dense_inverse<<<1, 1024, smem, c->stream>>>(Lc.nx, Lc.ny, Lc.A, mg.cinv);
+    BSC_LAUNCH(c);
+    if (mg.f32)
+        for (int l = 1; l <= mg.nlev; ++l) {
+            const MgLevel& L = mg.L[l];
+            k_mg_to_f32<<<blocks_for(9 * L.nc, 256), 256, 0, c->stream>>>(9 * L.nc, L.A, L.Af);
+            k_mg_to_f32<<<blocks_for(L.nc, 256), 256, 0, c->stream>>>(L.nc, L.dinv, L.dinvf);
+            c->launches += 2;
+        }
+    return BSC_OK;
+}
+
+int mg_vcycle_f64(Ctx* c, const double* v, double* z) { return vcycle<double>(c, v, z); }
+int mg_vcycle_f32(Ctx* c, const double* v, float* z) { return vcycle<float>(c, v, z); }
+
+}  // namespace bsc

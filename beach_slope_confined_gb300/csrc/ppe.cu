@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "bsc_internal.cuh"
+#include "ellop.cuh"
 
 namespace bsc {
 
@@ -153,39 +154,6 @@ int op_ppe_assemble(Ctx* c) {
 // ============================================================================
 // operators: unit-diagonal ELL (the PPE) and general CSR (standalone solve)
 // ============================================================================
-template <typename T>
-struct EllOp {
-    const T* aval;
-    const int32_t* nbr;
-    const int32_t* cnt;
-    int kmax;
-    int unroll = 0;  // 1: four entries per round (four gathers in flight)
-    const void* key() const { return aval; }
-    // the column stride of the ELL layout is 32 slots
-    template <typename X, typename A>
-    __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
-        A s = (A)x[i];
-        const int m = cnt[i];
-        const int64_t e0 = ell(i, 0, kmax);
-        int k = 0;
-        for (; unroll && k + 4 <= m; k += 4) {
-            const int64_t e = e0 + (int64_t)k * 32;
-            const int j0 = nbr[e], j1 = nbr[e + 32], j2 = nbr[e + 64], j3 = nbr[e + 96];
-            const T a0 = aval[e], a1 = aval[e + 32], a2 = aval[e + 64], a3 = aval[e + 96];
-            const X x0 = x[j0], x1 = x[j1], x2 = x[j2], x3 = x[j3];
-            s += (A)a0 * (A)x0;
-            s += (A)a1 * (A)x1;
-            s += (A)a2 * (A)x2;
-            s += (A)a3 * (A)x3;
-        }
-        for (; k < m; ++k) {
-            const int64_t e = e0 + (int64_t)k * 32;
-            s += (A)aval[e] * (A)x[nbr[e]];
-        }
-        return s;
-    }
-};
-
 struct CsrOp {
     const int32_t* rp;
     const int32_t* col;
@@ -251,7 +219,6 @@ __device__ __forceinline__ void reduce_partials(const double* __restrict__ part,
     for (int d = 0; d < D; ++d) out[d] = res[d];
 }
 
-#define GRID_LOOP(i, n) for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < (n); i += (int64_t)gridDim.x * blockDim.x)
 
 // ============================================================================
 // BiCGSTAB, value type T (double or float), dots accumulated in double
@@ -863,15 +830,17 @@ __global__ void k_d2f(int64_t n, const double* __restrict__ a, float* __restrict
     GRID_LOOP(i, n) b[i] = (float)a[i];
 }
 
-// w = A z with the FP64 operator and an FP32 preconditioned vector
-__global__ void __launch_bounds__(RED_BLOCK) k_spmv_z(int64_t n, EllOp<double> A, const float* __restrict__ z,
+// w = A z with the FP64 operator and a preconditioned vector (FP32 or FP64)
+template <typename ZT>
+__global__ void __launch_bounds__(RED_BLOCK) k_spmv_z(int64_t n, EllOp<double> A, const ZT* __restrict__ z,
                                                        double* __restrict__ w, const Scalars* __restrict__ sc) {
     if (fg_skip(sc)) return;
-    GRID_LOOP(i, n) w[i] = A.template row<float, double>(i, z);
+    GRID_LOOP(i, n) w[i] = A.template row<ZT, double>(i, z);
 }
 
-// x += sum_i y_i z_i, z_i the FP32 preconditioned vectors of the cycle
-__global__ void k_fg_update_z(int64_t n, double* __restrict__ x, const float* __restrict__ Z,
+// x += sum_i y_i z_i, z_i the preconditioned vectors of the cycle
+template <typename ZT>
+__global__ void k_fg_update_z(int64_t n, double* __restrict__ x, const ZT* __restrict__ Z,
                               const double* __restrict__ Hd, FgLayout F, const Scalars* __restrict__ sc) {
     if (sc->done) return;
     __shared__ double y[FG_MAXM];
@@ -974,6 +943,93 @@ int run_fgmres_ir(Ctx* c, int64_t n, bsc_solve_info* si) {
     return si->status;
 }
 
+// Flexible GMRES(m) in FP64 on the FP64 operator, right-preconditioned by
+// one multigrid V-cycle per iteration (mg.cu), in FP64 (ZT = double) or FP32
+// (ZT = float, the mixed path).  Stops on the Arnoldi residual estimate and
+// reports the true residual of the returned pressure.
+template <typename ZT>
+int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
+    const bsc_params& P = c->P;
+    const int G = RED_GRID, B = RED_BLOCK;
+    const int rel_r0 = P.tol_mode == BSC_TOL_REL_R0;
+    Mg& mg = c->mg;
+    const int m = mg.m;
+    const FgLayout F{m};
+    const EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+    double* x = c->S.p;
+    double* w = c->tv;
+    double* V = mg.V;
+    ZT* Z = (ZT*)mg.Z;
+    int first = 1, iters = 0, rc;
+    for (;;) {
+        k_resid<EllOp<double>, double><<<G, B, 0, c->stream>>>(n, A, x, c->b, c->r, c->part);
+        BSC_LAUNCH(c);
+        k_fg_start<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, first, P.tol, rel_r0);
+        BSC_LAUNCH(c);
+        first = 0;
+        if ((rc = fetch_outer(c))) return rc;
+        if (c->h_sc[1].done || iters >= P.maxit) break;
+        k_fg_v0<double><<<G, B, 0, c->stream>>>(n, c->r, V, c->sc2);
+        BSC_LAUNCH(c);
+        for (int j = 0; j < m && iters < P.maxit; ++j) {
+            ZT* zj = Z + (int64_t)j * n;
+            const double* vj = V + (int64_t)j * n;
+            if constexpr (sizeof(ZT) == 4)
+                rc = mg_vcycle_f32(c, vj, (float*)zj);
+            else
+                rc = mg_vcycle_f64(c, vj, (double*)zj);
+            if (rc) return rc;
+            // the FP64 SpMV w = A z_j is bracketed by events: the dominant
+            // HBM-bound kernel, timed in place
+            if (c->timing) cudaEventRecord(c->ev_spmv[0], c->stream);
+            k_spmv_z<ZT><<<G, B, 0, c->stream>>>(n, A, zj, w, c->sc2);
+            if (c->timing) cudaEventRecord(c->ev_spmv[1], c->stream);
+            for (int pass = 0; pass < 2; ++pass) {
+                k_fg_mdot<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc2);
+                k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc2);
+                k_fg_maxpy<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, pass, c->part, c->sc2);
+            }
+            k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, j);
+            k_fg_next<double><<<G, B, 0, c->stream>>>(n, w, V, j, c->sc2);
+            c->launches += 9;
+            BSC_CUDA(c, cudaGetLastError());
+            ++iters;
+            if ((rc = fetch_outer(c))) return rc;
+            if (c->timing) {  // the stream is idle after fetch_outer
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, c->ev_spmv[0], c->ev_spmv[1]) == cudaSuccess) {
+                    c->ms[BSC_T_SPMV] += ms;
+                    c->calls[BSC_T_SPMV]++;
+                }
+                (void)cudaGetLastError();
+            }
+            if (c->h_sc[1].tmp[2] != 0.0) break;
+        }
+        k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc2, c->Hd, F);
+        k_fg_update_z<ZT><<<G, B, 0, c->stream>>>(n, x, Z, c->Hd, F, c->sc2);
+        c->launches += 2;
+        BSC_CUDA(c, cudaGetLastError());
+        if (c->h_sc[1].breakdown && c->h_sc[1].tmp[1] == 0.0) break;
+    }
+    double* norms = c->Hd + F.size();
+    k_resid<EllOp<double>, double><<<G, B, 0, c->stream>>>(n, A, x, c->b, c->r, c->part);
+    BSC_LAUNCH(c);
+    k_ir_norms<<<1, B, 0, c->stream>>>(c->part, norms);
+    BSC_LAUNCH(c);
+    double nrm[2];
+    BSC_CUDA(c, cudaMemcpyAsync(nrm, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    si->iterations = iters;
+    si->outer = 1;
+    si->b_norm = c->h_sc[1].bnorm;
+    si->r0_norm = c->h_sc[1].r0norm;
+    si->rel_residual = nrm[1] > 0 ? nrm[0] / nrm[1] : nrm[0];
+    const double ref = rel_r0 ? si->r0_norm : si->b_norm;
+    si->converged = nrm[0] <= P.tol * ref ? 1 : 0;
+    si->status = si->converged ? BSC_OK : BSC_E_NOT_CONVERGED;
+    return si->status;
+}
+
 int solve_status(bsc_solve_info* info, int rc) {
     if (rc != BSC_OK) return rc;
     return info->converged ? BSC_OK : BSC_E_NOT_CONVERGED;
@@ -990,6 +1046,10 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
     *si = bsc_solve_info{};
     int rc = BSC_OK, iters = 0;
     double rr = 0.0;
+    if (P.precond == BSC_PRECOND_MG) {
+        if ((rc = mg_setup(c))) return rc;
+        return c->mixed ? run_fgmres_mg<float>(c, n, si) : run_fgmres_mg<double>(c, n, si);
+    }
     if (!c->mixed) {
         EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
         Work<double> w{c->S.p, c->b, c->r, c->rh, c->pd, c->v, c->s, c->tv, c->V};

@@ -23,11 +23,12 @@ def main(argv=None):
     ap.add_argument("precision", nargs="?", default="mixed", choices=("mixed", "fp64"))
     ap.add_argument("maxit", nargs="?", type=int, default=10)
     ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--precond", default="none", choices=("none", "mg"))
     args = ap.parse_args(argv)
     spec = sc.config_spec(args.config)
     scen = sc.build(spec)
     P = sc.make_params(spec, scen.bounds, precision=args.precision, tol=1e-8, maxit=args.maxit,
-                       inner_tol=0.1, max_outer=4)
+                       inner_tol=0.1, max_outer=4, precond=args.precond, restart=40)
     g = Solver(P)
     setup_tank(g, scen)
     for _ in range(args.steps):

@@ -335,9 +335,9 @@ class Params(ctypes.Structure):
         ("tschmidt", _D), ("diffusivity", _D), ("restart", _I), ("maxit", _I),
         ("tol_mode", _I), ("max_outer", _I), ("tol", _D), ("inner_tol", _D),
         ("max_neighbors", _I), ("reorder_every", _I), ("piston_modes", _I),
-        ("pad0", _I), ("piston_amp", _D * 8), ("piston_period", _D * 8),
+        ("precond", _I), ("piston_amp", _D * 8), ("piston_period", _D * 8),
         ("piston_phase", _D * 8), ("piston_ramp", _D), ("xmin", _D), ("xmax", _D), ("ymin", _D),
-        ("ymax", _D),
+        ("ymax", _D), ("mg_omega", _D), ("mg_scale", _D), ("mg_sweeps", _I), ("mg_coarse_max", _I),
     ]
 
 
@@ -364,13 +364,15 @@ STATE_FIELDS = ("x", "y", "vx", "vy", "xs", "ys", "vxs", "vys", "p", "rho", "ode
                 "xrest")
 
 SOLVERS = {"bicgstab": 0, "fgmres": 1}
+PRECONDS = {"none": 0, "mg": 1}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 
 
 def make_params(spec: TankSpec, bounds=None, *, precision="fp64", solver="bicgstab",
                 tol=1e-8, maxit=2000, restart=30, max_neighbors=48,
                 reorder_every=20, tol_mode=0, dt_mode=0, inner_tol=1e-4,
-                max_outer=20) -> Params:
+                max_outer=20, precond="none", mg_omega=0.8, mg_scale=1.5, mg_sweeps=2,
+                mg_coarse_max=128) -> Params:
     """bsc_params for a tank case (constants of initialize.f90:19-56 where the
     benchmark does not override them)."""
     p = Params()
@@ -413,6 +415,9 @@ def make_params(spec: TankSpec, bounds=None, *, precision="fp64", solver="bicgst
     p.piston_modes = len(spec.piston_amp)
     for k, (a, T, ph) in enumerate(zip(spec.piston_amp, spec.piston_period, spec.piston_phase)):
         p.piston_amp[k], p.piston_period[k], p.piston_phase[k] = a, T, ph
+    p.precond = PRECONDS[precond]
+    p.mg_omega, p.mg_scale = mg_omega, mg_scale
+    p.mg_sweeps, p.mg_coarse_max = mg_sweeps, mg_coarse_max
     if bounds is not None:
         p.xmin, p.xmax, p.ymin, p.ymax = bounds
     return p

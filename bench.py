@@ -163,6 +163,13 @@ def spmv_bytes(nnz: int, n: int, fp32: bool) -> int:
     return 12 * nnz + 28 * n
 
 
+def spmv_z_bytes(nnz: int, n: int, z_bytes: int) -> int:
+    """Algorithmic bytes of one k_spmv_z launch (w = A z, the FP64 operator
+    applied to a preconditioned vector of z_bytes per element): per stored
+    entry the FP64 value and the column; per row the count, z_i and w_i."""
+    return 12 * nnz + (4 + z_bytes + 8) * n
+
+
 def traffic_per_row(kind: str):
     """DRAM bytes per row of one SpMV launch from the committed ncu summary."""
     try:
@@ -184,7 +191,7 @@ def run_ours(args, dist: Dist):
         if prec == "fp64" and args.no_fp64:
             continue
         P = sc.make_params(spec, scen.bounds, precision=prec, solver=args.solver, tol=1e-8, maxit=40000,
-                           inner_tol=args.inner_tol, max_outer=60)
+                           inner_tol=args.inner_tol, max_outer=60, precond=args.precond, restart=args.restart)
         g = Solver(P)
         setup_tank(g, scen)
         for _ in range(args.warmup):
@@ -237,8 +244,17 @@ def run_ours(args, dist: Dist):
         a, b = states["mixed"], states["fp64"]
         errs = {f: float(np.linalg.norm(a[f] - b[f]) / max(np.linalg.norm(b[f]), 1e-300))
                 for f in ("x", "y", "vx", "vy", "p", "porosity", "nut")}
+    # iterations of the reference algorithm (unpreconditioned FP64 BiCGSTAB)
+    # on the first step, to scale the CPU sample of that algorithm
+    ref_iters = None
+    if args.precond != "none" and not args.no_cpu and dist.rank == 0:
+        P = sc.make_params(spec, scen.bounds, precision="fp64", solver="bicgstab", tol=1e-8, maxit=40000)
+        g = Solver(P)
+        setup_tank(g, scen)
+        ref_iters = g.step(1).iterations
+        g.close()
     peaks = measure_peaks() if dist.rank == 0 else None
-    return scen, results, errs, peaks
+    return scen, results, errs, peaks, ref_iters
 
 
 def cpu_sample(scen, spec, threads: int, gpu_iters: float, solver: str):
@@ -300,9 +316,12 @@ def main():
     ap.add_argument("--config", default=CONFIG)
     ap.add_argument("--solver", default="bicgstab", choices=("bicgstab", "fgmres"))
     ap.add_argument("--inner-tol", type=float, default=0.1)
+    ap.add_argument("--precond", default="mg", choices=("mg", "none"),
+                    help="PPE preconditioner: cell multigrid inside FGMRES, or none (the reference's solvers)")
+    ap.add_argument("--restart", type=int, default=40)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--cpu-iters", type=float, default=1850.0,
+    ap.add_argument("--cpu-iters", type=float, default=1350.0,
                     help="PPE iterations per step the reference arm's sample is scaled to")
     args = ap.parse_args()
     dist = Dist()
@@ -334,17 +353,24 @@ def main():
         dist.close()
         return
 
-    scen, res, errs, peaks = run_ours(args, dist)
+    scen, res, errs, peaks, ref_iters = run_ours(args, dist)
     if dist.rank != 0:
         dist.close()
         return
     spec = sc.config_spec(args.config)
     m = res["mixed"]
     hbm, peak_kind = measured_peak_hbm()
-    byts = spmv_bytes(m["nnz"], m["n"], fp32=True)
+    mg = args.precond == "mg"
+    if mg:
+        byts = spmv_z_bytes(m["nnz"], m["n"], 4)
+        kname = "k_spmv_z<float> (FP64 ELL SpMV of the FP32 preconditioned vector)"
+        tpr = traffic_per_row("spmv_z_fp32")
+    else:
+        byts = spmv_bytes(m["nnz"], m["n"], fp32=True)
+        kname = "k_bicg_1<EllOp<float>,float> (FP32 ELL SpMV + dot)"
+        tpr = traffic_per_row("fp32")
     achieved = byts / (m["spmv_ms"] * 1e-3) / 1e9 if m["spmv_ms"] > 0 else None
-    tpr = traffic_per_row("fp32")
-    roofline = {"bound": "hbm", "kernel": "k_bicg_1<EllOp<float>,float> (FP32 ELL SpMV + dot)",
+    roofline = {"bound": "hbm", "kernel": kname,
                 "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": (achieved / hbm) if achieved else None,
                 "traffic": (tpr * m["n"]) if tpr else None,
@@ -353,19 +379,27 @@ def main():
     fp64 = None
     if "fp64" in res:
         f = res["fp64"]
-        b64 = spmv_bytes(f["nnz"], f["n"], fp32=False)
+        b64 = spmv_z_bytes(f["nnz"], f["n"], 8) if mg else spmv_bytes(f["nnz"], f["n"], fp32=False)
         a64 = b64 / (f["spmv_ms"] * 1e-3) / 1e9 if f["spmv_ms"] > 0 else None
-        t64 = traffic_per_row("fp64")
+        t64 = traffic_per_row("spmv_z_fp64" if mg else "fp64")
         fp64 = {"value": f["value"], "ms_per_step": f["ms_per_step"], "ppe_iterations": [i[0] for i in f["iters"]],
                 "solve_ms_per_step": f["solve_ms"],
-                "roofline": {"bound": "hbm", "kernel": "k_bicg_1<EllOp<double>,double>", "achieved": a64,
+                "roofline": {"bound": "hbm",
+                             "kernel": "k_spmv_z<double>" if mg else "k_bicg_1<EllOp<double>,double>",
+                             "achieved": a64,
                              "peak": hbm, "unit": "GB/s", "frac": (a64 / hbm) if a64 else None,
                              "traffic": (t64 * f["n"]) if t64 else None}}
     cpu = None
     if not args.no_cpu:
-        gpu_iters = statistics.mean(i[0] for i in res["fp64"]["iters"]) if "fp64" in res else args.cpu_iters
-        v, desc, _ = cpu_sample(scen, spec, threads, gpu_iters, args.solver)
+        if ref_iters:
+            gpu_iters = float(ref_iters)
+        elif "fp64" in res and not mg:
+            gpu_iters = statistics.mean(i[0] for i in res["fp64"]["iters"])
+        else:
+            gpu_iters = args.cpu_iters
+        v, desc, _ = cpu_sample(scen, spec, threads, gpu_iters, "bicgstab")
         cpu = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port", "sample": desc}
+    solver_desc = f"FGMRES({args.restart}) + cell-multigrid V-cycle" if mg else args.solver
     line = {
         "metric": METRIC, "value": m["value"], "unit": "particle-steps/s", "n_gpus": dist.world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True,
@@ -373,8 +407,10 @@ def main():
         "data": "synthetic (seeded wave tank, no dataset)",
         "config": {"workload": f"{args.config} wave tank 4.0x0.6 m, depth 0.30 m, dx={spec.dx} m, "
                                f"{scen.n_fluid} fluid + {scen.n - scen.n_fluid} wall particles, Wendland C2 h=1.3dx, "
-                               f"{args.solver} PPE to rel-res 1e-8, dt={spec.dt} s",
-                   "fluid_particles": scen.n_fluid, "precision": "mixed (FP32 sweeps, FP64 refinement)",
+                               f"{solver_desc} PPE to rel-res 1e-8, dt={spec.dt} s",
+                   "fluid_particles": scen.n_fluid, "precond": args.precond,
+                   "precision": ("mixed (FP32 pair sums and V-cycle, FP64 assembly and FGMRES)" if mg
+                                 else "mixed (FP32 sweeps, FP64 refinement)"),
                    "l2": "inputs larger than L2 (particle state ~170 MB + neighbour lists ~0.9 GB)",
                    "parallelism": f"replicas x{dist.world}"},
         "ppe": {"iterations": [i[0] for i in m["iters"]], "refinement_sweeps": [i[1] for i in m["iters"]],

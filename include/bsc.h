@@ -55,6 +55,10 @@ enum { BSC_SOLVER_BICGSTAB = 0, BSC_SOLVER_FGMRES = 1 };
 /* stopping test: ||r|| <= tol*||b|| (relative residual), or
  * ||r|| <= tol*||r0|| (the MKL dfgmres test used by solver.f90:321-324) */
 enum { BSC_TOL_REL_B = 0, BSC_TOL_REL_R0 = 1 };
+/* PPE preconditioner: none (the reference's solvers), or a V-cycle of
+ * multigrid over the neighbour cells used by flexible GMRES(restart); the
+ * V-cycle runs in FP64 on the FP64 path and in FP32 on the mixed path. */
+enum { BSC_PRECOND_NONE = 0, BSC_PRECOND_MG = 1 };
 /* time step: fixed dt, or the CFL/viscous rule of integrator.f90:908-976 */
 enum { BSC_DT_FIXED = 0, BSC_DT_ADAPTIVE = 1 };
 
@@ -109,12 +113,17 @@ typedef struct bsc_params {
     int32_t max_neighbors;       /* neighbour-list capacity per particle           */
     int32_t reorder_every;       /* Morton reorder of the state every n cellshifts */
     int32_t piston_modes;        /* piston x_p(t) = sum a_k sin(2 pi t/T_k + phi_k)*/
-    int32_t pad0;
+    int32_t precond;             /* BSC_PRECOND_* for the PPE solve                */
     double  piston_amp[BSC_MAX_PISTON_MODES];
     double  piston_period[BSC_MAX_PISTON_MODES];
     double  piston_phase[BSC_MAX_PISTON_MODES];
     double  piston_ramp;         /* stroke scaled by (1-cos(pi t/ramp))/2 for t<ramp */
     double  xmin, xmax, ymin, ymax; /* cell-grid bounds; all 0 = derive at upload */
+    /* cell-aggregation multigrid (BSC_PRECOND_MG) */
+    double  mg_omega;            /* damped-Jacobi weight of the smoother           */
+    double  mg_scale;            /* scaling of the coarse-grid correction          */
+    int32_t mg_sweeps;           /* pre- and post-smoothing sweeps per level       */
+    int32_t mg_coarse_max;       /* cells of the coarsest level (dense solve)      */
 } bsc_params;
 
 /* Host-side particle state, structure of arrays, n entries each, id order.

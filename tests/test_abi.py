@@ -88,3 +88,14 @@ def test_no_gpu_means_no_context():
     with pytest.raises(BscError) as e:
         Solver(sc.make_params(sc.TankSpec()))
     assert e.value.code == -8
+
+
+@pytest.mark.parametrize("bad", [dict(mg_sweeps=0), dict(mg_omega=2.5), dict(mg_coarse_max=1000),
+                                 dict(mg_scale=0.0)])
+def test_multigrid_parameters_are_validated(bad):
+    """bsc_create rejects out-of-range multigrid settings before touching a GPU."""
+    from beach_slope_confined_gb300 import BscError, Solver
+
+    with pytest.raises(BscError) as e:
+        Solver(sc.make_params(sc.TankSpec(), precond="mg", **bad))
+    assert e.value.code == -1
