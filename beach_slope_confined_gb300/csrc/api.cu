@@ -153,6 +153,7 @@ static int alloc_for(Ctx* c, int64_t n) {
     int rc;
     if ((rc = alloc_state(c, c->S, n)) || (rc = alloc_state(c, c->S2, n))) return rc;
     if ((rc = dalloc(c, &c->pcell, n)) || (rc = dalloc(c, &c->pslot, n)) || (rc = dalloc(c, &c->sorted, n))) return rc;
+    if ((rc = dalloc(c, &c->posf, n))) return rc;
     const int64_t slots = ((n + 31) / 32) * 32 * (int64_t)c->K.kmax;
     if ((rc = dalloc(c, &c->nbr, slots)) || (rc = dalloc(c, &c->cnt, n))) return rc;
     // FP64 grad W and PPE values in both precisions; the mixed path adds FP32
@@ -501,7 +502,7 @@ int bsc_upload_solids(bsc_ctx* c, int64_t ns, const double* x, const double* y, 
     if (ns == 0) return BSC_OK;
     int rc;
     if ((rc = palloc(c, &c->sx, ns)) || (rc = palloc(c, &c->sy, ns)) || (rc = palloc(c, &c->svol, ns)) ||
-        (rc = palloc(c, &c->spor, ns)))
+        (rc = palloc(c, &c->spor, ns)) || (rc = palloc(c, &c->sposf, ns)))
         return rc;
     std::vector<double> vol(ns), sp(ns);
     const KParams& K = c->K;

@@ -166,6 +166,10 @@ struct Ctx {
     int32_t *cell_start = nullptr, *cell_count = nullptr, *cell_rank = nullptr, *cell_tmp = nullptr;
     int32_t *pcell = nullptr, *pslot = nullptr, *sorted = nullptr;
     int32_t *scan_part = nullptr;
+    // positions as float offsets from the origin of their own cell (the FP32
+    // pre-test of the pair searches); fluid/wall particles and solids
+    float2* posf = nullptr;
+    float2* sposf = nullptr;
     // solids: their own cell list, static after upload
     double *sx = nullptr, *sy = nullptr, *svol = nullptr, *spor = nullptr;
     int32_t *scell_start = nullptr, *scell_count = nullptr;

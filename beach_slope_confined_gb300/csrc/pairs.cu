@@ -66,6 +66,28 @@ __device__ __forceinline__ double porosity_at(const KParams& K, double x, double
     return K.pgrid[(int64_t)fy * K.pnx + (int64_t)fx];
 }
 
+// ---- FP32 pre-test of the pair searches -----------------------------------------------
+// Positions are kept as float offsets from the origin of their own cell, so
+// a candidate in the neighbouring cell (ax, ay) sits at its offset plus an
+// exact shift of 0 or +-cs.  With offsets below PRE_GUARD cells the float
+// estimate of r^2 is within ~1e-6 (relative) of the exact one, far inside
+// the 1e-5 margin: the pre-test only rejects candidates that the exact FP64
+// test would reject too.  Particles farther from their binned cell skip it.
+constexpr float PRE_GUARD = 4.0f;
+constexpr double PRE_MARGIN = 1e-5;
+
+__device__ __forceinline__ bool pre_ok(float2 p, float csf) {
+    return fabsf(p.x) < PRE_GUARD * csf && fabsf(p.y) < PRE_GUARD * csf;
+}
+
+__global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
+                       const int32_t* __restrict__ pcell, KParams K, float2* __restrict__ posf) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
+    posf[i] = make_float2((float)(x[i] - (K.gx0 + cx * K.cs)), (float)(y[i] - (K.gy0 + cy * K.cs)));
+}
+
 // ---- search.f90:13-399 neighbour / nsearch2 ----------------------------------------
 template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KParams K,
@@ -73,6 +95,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                                                          const int32_t* __restrict__ ccount,
                                                          const int32_t* __restrict__ sorted,
                                                          const int32_t* __restrict__ pcell,
+                                                         const float2* __restrict__ posf,
                                                          int32_t* __restrict__ nbr, double2* __restrict__ gw,
                                                          float2* __restrict__ gwf,
                                                          int32_t* __restrict__ cnt, int32_t* __restrict__ flag) {
@@ -80,21 +103,29 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
     if (i >= n) return;
     const double xi = S.x[i], yi = S.y[i];
     const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
-    const float H2f = (float)(K.H2 * (1.0 + 1e-5));
+    const float H2f = (float)(K.H2 * (1.0 + PRE_MARGIN));
+    const float csf = (float)K.cs;
+    const float2 pi = posf[i];
+    const bool pre_i = pre_ok(pi, csf);
     R m0 = 0, m1 = 0, m2 = 0, m3 = 0;
     int count = 0;
     for (int ax = cx - 1; ax <= cx + 1; ++ax) {
         if (ax < 0 || ax >= K.nx) continue;
+        const float shx = (float)(ax - cx) * csf;
         for (int ay = cy - 1; ay <= cy + 1; ++ay) {
             if (ay < 0 || ay >= K.ny) continue;
+            const float shy = (float)(ay - cy) * csf;
             const int cc = ax * K.ny + ay;
             const int s0 = cstart[cc], s1 = s0 + ccount[cc];
             for (int s = s0; s < s1; ++s) {
                 const int j = sorted[s];
                 if (j == (int)i) continue;  // (tid,matid) self test, search.f90:53-55
+                const float2 pj = posf[j];
+                if (pre_i && pre_ok(pj, csf)) {
+                    const float fdx = pi.x - (pj.x + shx), fdy = pi.y - (pj.y + shy);
+                    if (fdx * fdx + fdy * fdy > H2f) continue;
+                }
                 const double dx = xi - S.x[j], dy = yi - S.y[j];
-                const float fdx = (float)dx, fdy = (float)dy;
-                if (fdx * fdx + fdy * fdy > H2f) continue;
                 const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
                 if (!(r < K.H)) continue;
                 // grad W per pair in FP64 (stored in FP64, and in FP32 for the
@@ -146,14 +177,17 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
 }
 
 int op_neighbour(Ctx* c) {
+    k_posf<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S.x, c->S.y, c->pcell, c->K, c->posf);
+    BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
         k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
-                                                          c->pcell, c->nbr, c->gw, c->gwf, c->cnt, c->d_flag);
+                                                          c->pcell, c->posf, c->nbr, c->gw, c->gwf, c->cnt,
+                                                          c->d_flag);
     else
         k_neighbour<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count,
-                                                           c->sorted, c->pcell, c->nbr, c->gw, nullptr, c->cnt,
-                                                           c->d_flag);
+                                                           c->sorted, c->pcell, c->posf, c->nbr, c->gw, nullptr,
+                                                           c->cnt, c->d_flag);
     BSC_LAUNCH(c);
     c->have_lists = true;
     return BSC_OK;
@@ -187,6 +221,7 @@ template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams K, const int32_t* __restrict__ pcell,
                                                       const int32_t* __restrict__ scs, const int32_t* __restrict__ scc,
                                                       const double* __restrict__ sx, const double* __restrict__ sy,
+                                                      const float2* __restrict__ sposf,
                                                       const double* __restrict__ svol,
                                                       const double* __restrict__ spor) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -195,18 +230,26 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
     if (S.tid[i] != BSC_TID_FLUID) return;
     const double xi = S.x[i], yi = S.y[i];
     const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
-    const float H2f = (float)(K.H2 * (1.0 + 1e-5));
+    const float H2f = (float)(K.H2 * (1.0 + PRE_MARGIN));
+    const float csf = (float)K.cs;
+    const float2 pi = make_float2((float)(xi - (K.gx0 + cx * K.cs)), (float)(yi - (K.gy0 + cy * K.cs)));
+    const bool pre_i = pre_ok(pi, csf);
     R frac = 0;
     for (int ax = cx - 1; ax <= cx + 1; ++ax) {
         if (ax < 0 || ax >= K.nx) continue;
+        const float shx = (float)(ax - cx) * csf;
         for (int ay = cy - 1; ay <= cy + 1; ++ay) {
             if (ay < 0 || ay >= K.ny) continue;
+            const float shy = (float)(ay - cy) * csf;
             const int cc = ax * K.ny + ay;
             const int s0 = scs[cc], s1 = s0 + scc[cc];
             for (int s = s0; s < s1; ++s) {
+                const float2 ps = sposf[s];
+                if (pre_i && pre_ok(ps, csf)) {
+                    const float fdx = pi.x - (ps.x + shx), fdy = pi.y - (ps.y + shy);
+                    if (fdx * fdx + fdy * fdy > H2f) continue;
+                }
                 const double dx = xi - sx[s], dy = yi - sy[s];
-                const float fdx = (float)dx, fdy = (float)dy;
-                if (fdx * fdx + fdy * fdy > H2f) continue;
                 const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
                 if (!(r < K.H)) continue;
                 frac += ((R)1 - (R)spor[s]) * kern_w<R>(K, (R)r) * (R)svol[s];
@@ -235,10 +278,10 @@ int op_effpor(Ctx* c) {
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
         k_effpor<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
-                                                       c->sx, c->sy, c->svol, c->spor);
+                                                       c->sx, c->sy, c->sposf, c->svol, c->spor);
     else
         k_effpor<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
-                                                        c->sx, c->sy, c->svol, c->spor);
+                                                        c->sx, c->sy, c->sposf, c->svol, c->spor);
     BSC_LAUNCH(c);
     return BSC_OK;
 }
