@@ -131,6 +131,7 @@ struct MgLevel {
 };
 struct Mg {
     int nlev = 0;                  // levels 1..nlev are structured; nlev is solved densely
+    int tail_l0 = 0;               // levels tail_l0..nlev run in one single-CTA kernel
     MgLevel L[MG_MAX_LEVELS + 1];
     double* cinv = nullptr;        // inverse of the coarsest level, FP64, row-major
     int64_t n = 0;                 // rows the buffers are sized for
@@ -138,8 +139,10 @@ struct Mg {
     int m = 0;                     // FGMRES restart length
     bool f32 = false;
     void *r0 = nullptr, *y0 = nullptr, *t0 = nullptr;  // fine-level V-cycle vectors
-    double* V = nullptr;           // FGMRES basis (m+1) x n
-    void* Z = nullptr;             // preconditioned vectors m x n (FP64 or FP32)
+    double* V = nullptr;           // FGMRES basis (m+1) x n (FP64 path)
+    double* Z = nullptr;           // preconditioned vectors m x n (FP64 path)
+    float *Vf = nullptr, *Zf = nullptr;  // the same in FP32 (mixed path's inner solve)
+    float *wf = nullptr, *rf = nullptr;  // FP32 work vectors
     std::vector<void*> allocs;
 };
 
@@ -207,9 +210,11 @@ struct Ctx {
         const void* k2;
         int64_t n;
         cudaGraphExec_t exec;
+        int64_t kernels = 0;      // kernels in the graph (counted at capture)
     };
     std::vector<GraphEntry> graphs;
     bool use_graphs = true;
+    bool capturing = false;       // a graph capture of the context stream is open
     bool debug = false;           // BSC_DEBUG=1: per-sweep solver trace on stderr
     int spmv_unroll = 1;          // four ELL entries per round (BSC_SPMV_UNROLL=0: one)
     bool prof_iter = false;       // BSC_PROFILE_ITER=1: events around each Krylov kernel
@@ -236,6 +241,18 @@ struct Ctx {
 };
 
 void timing_flush(Ctx* c);
+
+// an event on the context stream; inside a graph capture it becomes an
+// external event node, so it is recorded on every replay and stays timeable
+inline void record_event(Ctx* c, cudaEvent_t e) {
+    if (c->capturing)
+        cudaEventRecordWithFlags(e, c->stream, cudaEventRecordExternal);
+    else
+        cudaEventRecord(e, c->stream);
+}
+
+// destroy the cached graphs (their kernels hold pointers that are about to change)
+void drop_graphs(Ctx* c);
 
 // ---- stage timer: a pair of CUDA events on the context stream -----------------
 struct StageTimer {
@@ -277,7 +294,7 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info);
 // z = M v to an FP64 vector (FP64 or FP32 arithmetic); release the buffers
 int mg_setup(Ctx* c);
 int mg_vcycle_f64(Ctx* c, const double* v, double* z);
-int mg_vcycle_f32(Ctx* c, const double* v, float* z);
+int mg_vcycle_f32(Ctx* c, const float* v, float* z);
 void mg_free(Ctx* c);
 int fg_layout_size(int m);
 int csr_solve_device(Ctx* c, int32_t n, const int32_t* rp, const int32_t* col, const double* val,

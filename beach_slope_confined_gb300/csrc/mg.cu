@@ -187,18 +187,15 @@ __global__ void k_mg_to_f32(int64_t n, const double* __restrict__ a, float* __re
 }
 
 // ---- V-cycle, structured levels (l >= 1) -------------------------------------------
-// x_out = x + w D^-1 (b - A x) where the input x is
+// One damped-Jacobi update of cell c: x + w D^-1 (b - A x), where the input x is
 //   MODE 0: xin;
 //   MODE 1: w D^-1 b (the first sweep from a zero guess, folded in);
 //   MODE 2: xin + scale * xc[parent] (the prolonged coarse correction, folded in).
 template <typename T, int MODE>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg_smooth(int nx, int ny, const T* __restrict__ A,
-                                                         const T* __restrict__ dinv, const T* __restrict__ b,
-                                                         const T* __restrict__ xin, const T* __restrict__ xc, int nyc,
-                                                         T scale, T w, T* __restrict__ xout) {
+__device__ __forceinline__ T smooth_at(int nx, int ny, int64_t c, const T* __restrict__ A,
+                                       const T* __restrict__ dinv, const T* __restrict__ b,
+                                       const T* __restrict__ xin, const T* __restrict__ xc, int nyc, T scale, T w) {
     const int64_t nc = (int64_t)nx * ny;
-    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (c >= nc) return;
     const int cx = (int)(c / ny), cy = (int)(c % ny);
     auto xv = [&](int gx, int gy) -> T {
         const int64_t g = (int64_t)gx * ny + gy;
@@ -214,23 +211,14 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg_smooth(int nx, int ny, const T*
         const T a = A[s * nc + c];
         if (a != (T)0) ax += a * xv(gx, gy);
     }
-    xout[c] = xv(cx, cy) + w * dinv[c] * (b[c] - ax);
+    return xv(cx, cy) + w * dinv[c] * (b[c] - ax);
 }
 
-// one sweep from a zero guess: x = w D^-1 b
+// the residual b - A x summed over the 2x2 children of coarse cell C
 template <typename T>
-__global__ void k_mg_jacobi0(int64_t nc, const T* __restrict__ dinv, const T* __restrict__ b, T w, T* __restrict__ x) {
-    GRID_LOOP(c, nc) x[c] = w * dinv[c] * b[c];
-}
-
-// b_c = sum over the 2x2 children of the residual b - A x
-template <typename T>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const T* __restrict__ A,
-                                                           const T* __restrict__ b, const T* __restrict__ x, int nxc,
-                                                           int nyc, T* __restrict__ bc) {
-    const int64_t ncc = (int64_t)nxc * nyc, nc = (int64_t)nx * ny;
-    const int64_t C = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (C >= ncc) return;
+__device__ __forceinline__ T restrict_at(int nx, int ny, const T* __restrict__ A, const T* __restrict__ b,
+                                         const T* __restrict__ x, int64_t C, int nyc) {
+    const int64_t nc = (int64_t)nx * ny;
     const int CX = (int)(C / nyc), CY = (int)(C % nyc);
     T sum = 0;
     for (int a = 0; a < 2; ++a) {
@@ -251,48 +239,139 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const 
             sum += b[f] - ax;
         }
     }
-    bc[C] = sum;
+    return sum;
 }
 
-// coarsest level: x = C^-1 b
+template <typename T, int MODE>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg_smooth(int nx, int ny, const T* __restrict__ A,
+                                                         const T* __restrict__ dinv, const T* __restrict__ b,
+                                                         const T* __restrict__ xin, const T* __restrict__ xc, int nyc,
+                                                         T scale, T w, T* __restrict__ xout) {
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= (int64_t)nx * ny) return;
+    xout[c] = smooth_at<T, MODE>(nx, ny, c, A, dinv, b, xin, xc, nyc, scale, w);
+}
+
+// one sweep from a zero guess: x = w D^-1 b
 template <typename T>
-__global__ void k_mg_dense_apply(int n, const double* __restrict__ cinv, const T* __restrict__ b, T* __restrict__ x) {
-    for (int r = threadIdx.x; r < n; r += blockDim.x) {
-        double s = 0.0;
-        for (int c = 0; c < n; ++c) s += cinv[r * n + c] * (double)b[c];
-        x[r] = (T)s;
+__global__ void k_mg_jacobi0(int64_t nc, const T* __restrict__ dinv, const T* __restrict__ b, T w, T* __restrict__ x) {
+    GRID_LOOP(c, nc) x[c] = w * dinv[c] * b[c];
+}
+
+template <typename T>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const T* __restrict__ A,
+                                                           const T* __restrict__ b, const T* __restrict__ x, int nxc,
+                                                           int nyc, T* __restrict__ bc) {
+    const int64_t C = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (C >= (int64_t)nxc * nyc) return;
+    bc[C] = restrict_at<T>(nx, ny, A, b, x, C, nyc);
+}
+
+// The small levels l0..nlev in one CTA: the same sweeps, restrictions, dense
+// solve and prolongations as the per-level kernels, phase by phase with a
+// block barrier between phases (each phase reads what the previous one
+// wrote).  Saves two to four launches per level where a level is too small
+// to fill the GPU.
+constexpr int MG_TAIL_CELLS = 8192;
+constexpr int MG_TAIL_THREADS = 1024;
+template <typename T>
+struct TailLevel {
+    int nx, ny;
+    const T* A;
+    const T* dinv;
+    T *b, *x, *y, *t;
+};
+template <typename T>
+struct TailArgs {
+    int l0, nlev, nu;
+    T w, scale;
+    const double* cinv;
+    TailLevel<T> L[MG_MAX_LEVELS + 1];
+};
+
+template <typename T>
+__global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
+    const int t = threadIdx.x, NT = blockDim.x;
+    const T w = P.w, sc = P.scale;
+    const int nu = P.nu;
+    T* cur[MG_MAX_LEVELS + 1];
+    for (int l = P.l0; l < P.nlev; ++l) {
+        const TailLevel<T>& L = P.L[l];
+        const int64_t nc = (int64_t)L.nx * L.ny;
+        T* c0 = L.y;
+        for (int64_t c = t; c < nc; c += NT)
+            c0[c] = nu == 1 ? w * L.dinv[c] * L.b[c]
+                            : smooth_at<T, 1>(L.nx, L.ny, c, L.A, L.dinv, L.b, nullptr, nullptr, 0, sc, w);
+        __syncthreads();
+        for (int k = 2; k < nu; ++k) {
+            T* out = c0 == L.y ? L.t : L.y;
+            for (int64_t c = t; c < nc; c += NT)
+                out[c] = smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w);
+            __syncthreads();
+            c0 = out;
+        }
+        cur[l] = c0;
+        const TailLevel<T>& C = P.L[l + 1];
+        const int64_t ncc = (int64_t)C.nx * C.ny;
+        for (int64_t q = t; q < ncc; q += NT) C.b[q] = restrict_at<T>(L.nx, L.ny, L.A, L.b, c0, q, C.ny);
+        __syncthreads();
+    }
+    {   // coarsest level: x = C^-1 b, a warp per row, lanes along the row
+        const TailLevel<T>& L = P.L[P.nlev];
+        const int n = L.nx * L.ny;
+        const int lane = t & 31;
+        for (int r = t >> 5; r < n; r += NT >> 5) {
+            double s = 0.0;
+            for (int q = lane; q < n; q += 32) s += P.cinv[r * n + q] * (double)L.b[q];
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0) L.x[r] = (T)s;
+        }
+        __syncthreads();
+    }
+    for (int l = P.nlev - 1; l >= P.l0; --l) {
+        const TailLevel<T>& L = P.L[l];
+        const TailLevel<T>& C = P.L[l + 1];
+        const int64_t nc = (int64_t)L.nx * L.ny;
+        T* c0 = cur[l];
+        for (int k = 0; k < nu; ++k) {
+            T* out = (k == nu - 1) ? L.x : (c0 == L.y ? L.t : L.y);
+            for (int64_t c = t; c < nc; c += NT)
+                out[c] = k == 0 ? smooth_at<T, 2>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, C.x, C.ny, sc, w)
+                                : smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w);
+            __syncthreads();
+            c0 = out;
+        }
     }
 }
 
 // ---- V-cycle, level 0 (the PPE, unit diagonal) ---------------------------------------
+// VI: type of the right-hand side v; O: type of the result z (the last sweep)
 // two sweeps from a zero guess: x1 = w v; x2 = x1 + w (v - A x1)
-template <typename T>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<T> A, const double* __restrict__ v, T w,
+template <typename T, typename VI>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<T> A, const VI* __restrict__ v, T w,
                                                         T* __restrict__ x) {
     GRID_LOOP(i, n) {
-        const T Av = A.template row<double, T>(i, v);
+        const T Av = A.template row<VI, T>(i, v);
         const T vi = (T)v[i];
         x[i] = w * vi + w * (vi - w * Av);
     }
 }
 
-__global__ void k_mg0_scale_f64(int64_t n, const double* __restrict__ v, double w, double* __restrict__ x) {
-    GRID_LOOP(i, n) x[i] = w * v[i];
-}
-__global__ void k_mg0_scale_f32(int64_t n, const double* __restrict__ v, float w, float* __restrict__ x) {
-    GRID_LOOP(i, n) x[i] = w * (float)v[i];
+template <typename T, typename VI>
+__global__ void k_mg0_scale(int64_t n, const VI* __restrict__ v, T w, T* __restrict__ x) {
+    GRID_LOOP(i, n) x[i] = w * (T)v[i];
 }
 
 // x_out = x + w (v - A x)
-template <typename T>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<T> A, const double* __restrict__ v,
-                                                         const T* __restrict__ x, T w, T* __restrict__ xout) {
-    GRID_LOOP(i, n) xout[i] = x[i] + w * ((T)v[i] - A.template row<T, T>(i, x));
+template <typename T, typename VI, typename O>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<T> A, const VI* __restrict__ v,
+                                                         const T* __restrict__ x, T w, O* __restrict__ xout) {
+    GRID_LOOP(i, n) xout[i] = (O)(x[i] + w * ((T)v[i] - A.template row<T, T>(i, x)));
 }
 
 // r = v - A x
-template <typename T>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_resid(int64_t n, EllOp<T> A, const double* __restrict__ v,
+template <typename T, typename VI>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_resid(int64_t n, EllOp<T> A, const VI* __restrict__ v,
                                                          const T* __restrict__ x, T* __restrict__ r) {
     GRID_LOOP(i, n) r[i] = (T)v[i] - A.template row<T, T>(i, x);
 }
@@ -311,11 +390,11 @@ __global__ void k_mg0_restrict(int64_t nc, const int32_t* __restrict__ cell_star
 
 // first post-sweep with the prolonged level-1 correction folded in:
 // y = x + scale * x1[cell]; x_out = y + w (v - A y)
-template <typename T>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_post(int64_t n, EllOp<T> A, const double* __restrict__ v,
+template <typename T, typename VI, typename O>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_post(int64_t n, EllOp<T> A, const VI* __restrict__ v,
                                                         const T* __restrict__ x, const T* __restrict__ x1,
                                                         const int32_t* __restrict__ pcell, T scale, T w,
-                                                        T* __restrict__ xout) {
+                                                        O* __restrict__ xout) {
     GRID_LOOP(i, n) {
         const T yi = x[i] + scale * x1[pcell[i]];
         T Ay = yi;
@@ -326,7 +405,7 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg0_post(int64_t n, EllOp<T> A, co
             const int j = A.nbr[e];
             Ay += A.aval[e] * (x[j] + scale * x1[pcell[j]]);
         }
-        xout[i] = yi + w * ((T)v[i] - Ay);
+        xout[i] = (O)(yi + w * ((T)v[i] - Ay));
     }
 }
 
@@ -363,13 +442,24 @@ int cycle_level(Ctx* c, int l) {
     const MgLevel& L = mg.L[l];
     Lv<T> v = level_view<T>(L);
     const unsigned g = blocks_for(L.nc, MG_BLOCK);
-    if (l == mg.nlev) {
-        k_mg_dense_apply<T><<<1, MG_COARSE_MAX, 0, c->stream>>>((int)L.nc, mg.cinv, v.b, v.x);
+    const T w = (T)c->P.mg_omega, sc = (T)c->P.mg_scale;
+    const int nu = c->P.mg_sweeps;
+    if (l >= mg.tail_l0) {  // this level and all coarser ones in one CTA
+        TailArgs<T> P{};
+        P.l0 = l;
+        P.nlev = mg.nlev;
+        P.nu = nu;
+        P.w = w;
+        P.scale = sc;
+        P.cinv = mg.cinv;
+        for (int q = l; q <= mg.nlev; ++q) {
+            Lv<T> u = level_view<T>(mg.L[q]);
+            P.L[q] = TailLevel<T>{mg.L[q].nx, mg.L[q].ny, u.A, u.dinv, u.b, u.x, u.y, u.t};
+        }
+        k_mg_tail<T><<<1, MG_TAIL_THREADS, 0, c->stream>>>(P);
         BSC_LAUNCH(c);
         return BSC_OK;
     }
-    const T w = (T)c->P.mg_omega, sc = (T)c->P.mg_scale;
-    const int nu = c->P.mg_sweeps;
     // pre-smoothing from a zero guess: one sweep is x = w D^-1 b; with two or
     // more, the first is folded into the second
     T* cur = v.y;
@@ -406,8 +496,9 @@ int cycle_level(Ctx* c, int l) {
     return BSC_OK;
 }
 
-template <typename T>
-int vcycle(Ctx* c, const double* vin, T* z) {
+// z = M v: V-cycle arithmetic in T, right-hand side in VI, result in O
+template <typename T, typename VI, typename O>
+int vcycle(Ctx* c, const VI* vin, O* z) {
     Mg& mg = c->mg;
     const int64_t n = c->n;
     const EllOp<T> A = fine_op<T>(c);
@@ -415,39 +506,45 @@ int vcycle(Ctx* c, const double* vin, T* z) {
     const int nu = c->P.mg_sweeps;
     T *P0 = (T*)mg.y0, *Q0 = (T*)mg.t0, *R0 = (T*)mg.r0;
     const int G = RED_GRID;
+    if (c->prof_iter) record_event(c, c->ev_it[0]);
     T* cur = P0;
-    if (nu == 1) {
-        if constexpr (sizeof(T) == 4)
-            k_mg0_scale_f32<<<G, MG_BLOCK, 0, c->stream>>>(n, vin, (float)w, (float*)cur);
-        else
-            k_mg0_scale_f64<<<G, MG_BLOCK, 0, c->stream>>>(n, vin, (double)w, (double*)cur);
-    } else {
-        k_mg0_pre2<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, cur);
-    }
+    if (nu == 1)
+        k_mg0_scale<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, vin, w, cur);
+    else
+        k_mg0_pre2<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, cur);
     BSC_LAUNCH(c);
     for (int k = 2; k < nu; ++k) {
         T* out = cur == P0 ? Q0 : P0;
-        k_mg0_sweep<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out);
+        k_mg0_sweep<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out);
         BSC_LAUNCH(c);
         cur = out;
     }
-    k_mg0_resid<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, R0);
+    k_mg0_resid<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, R0);
     BSC_LAUNCH(c);
     const MgLevel& L1 = mg.L[1];
     Lv<T> v1 = level_view<T>(L1);
     k_mg0_restrict<T><<<blocks_for(L1.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L1.nc, c->cell_start, c->cell_count,
                                                                               c->sorted, R0, v1.b);
     BSC_LAUNCH(c);
+    if (c->prof_iter) record_event(c, c->ev_it[1]);
     if (int rc = cycle_level<T>(c, 1)) return rc;
+    if (c->prof_iter) record_event(c, c->ev_it[2]);
+    // post-smoothing; the last sweep writes z
     for (int k = 0; k < nu; ++k) {
-        T* out = (k == nu - 1) ? z : (cur == P0 ? Q0 : P0);
-        if (k == 0)
-            k_mg0_post<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, out);
+        const bool last = k == nu - 1;
+        T* out = cur == P0 ? Q0 : P0;
+        if (k == 0 && last)
+            k_mg0_post<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, z);
+        else if (k == 0)
+            k_mg0_post<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, out);
+        else if (last)
+            k_mg0_sweep<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, z);
         else
-            k_mg0_sweep<T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out);
+            k_mg0_sweep<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out);
         BSC_LAUNCH(c);
         cur = out;
     }
+    if (c->prof_iter) record_event(c, c->ev_it[3]);
     return BSC_OK;
 }
 
@@ -469,6 +566,7 @@ int mg_alloc(Ctx* c) {
     const bool f32 = c->mixed;
     if (mg.n == n && mg.gx == c->K.nx && mg.gy == c->K.ny && mg.m == m && mg.f32 == f32 && !mg.allocs.empty())
         return BSC_OK;
+    drop_graphs(c);  // captured iterations point into the buffers replaced here
     mg_free(c);
     // the level dimensions
     int nlev = 1;
@@ -482,6 +580,12 @@ int mg_alloc(Ctx* c) {
         ++nlev;
     }
     mg.nlev = nlev;
+    // one SM runs the tail: FP32 levels up to MG_TAIL_CELLS cells, FP64 ones
+    // (a small fraction of the FP32 rate) up to an eighth of that
+    const int64_t tail_cells = f32 ? MG_TAIL_CELLS : MG_TAIL_CELLS / 8;
+    mg.tail_l0 = nlev;
+    while (mg.tail_l0 > 1 && (int64_t)mg.L[mg.tail_l0 - 1].nx * mg.L[mg.tail_l0 - 1].ny <= tail_cells)
+        --mg.tail_l0;
     const size_t vs = f32 ? sizeof(float) : sizeof(double);
     int rc;
     for (int l = 1; l <= nlev; ++l) {
@@ -503,10 +607,16 @@ int mg_alloc(Ctx* c) {
     mg.r0 = fine;
     mg.y0 = fine + n * vs;
     mg.t0 = fine + 2 * n * vs;
-    if ((rc = mg_dalloc(c, &mg.V, (int64_t)(m + 1) * n))) return rc;
-    unsigned char* z = nullptr;
-    if ((rc = mg_dalloc(c, &z, (int64_t)m * n * (int64_t)vs))) return rc;
-    mg.Z = z;
+    if (f32) {
+        // FP32 inner FGMRES of the iterative refinement: basis, preconditioned
+        // vectors, and the work vectors w, r
+        if ((rc = mg_dalloc(c, &mg.Vf, (int64_t)(m + 1) * n)) || (rc = mg_dalloc(c, &mg.Zf, (int64_t)m * n)) ||
+            (rc = mg_dalloc(c, &mg.wf, 2 * n)))
+            return rc;
+        mg.rf = mg.wf + n;
+    } else {
+        if ((rc = mg_dalloc(c, &mg.V, (int64_t)(m + 1) * n)) || (rc = mg_dalloc(c, &mg.Z, (int64_t)m * n))) return rc;
+    }
     mg.n = n;
     mg.gx = c->K.nx;
     mg.gy = c->K.ny;
@@ -555,7 +665,7 @@ int mg_setup(Ctx* c) {
     return BSC_OK;
 }
 
-int mg_vcycle_f64(Ctx* c, const double* v, double* z) { return vcycle<double>(c, v, z); }
-int mg_vcycle_f32(Ctx* c, const double* v, float* z) { return vcycle<float>(c, v, z); }
+int mg_vcycle_f64(Ctx* c, const double* v, double* z) { return vcycle<double, double, double>(c, v, z); }
+int mg_vcycle_f32(Ctx* c, const float* v, float* z) { return vcycle<float, float, float>(c, v, z); }
 
 }  // namespace bsc

@@ -648,6 +648,45 @@ int batch_graph(Ctx* c, const void* k0, const void* k1, const void* k2, int64_t 
     return BSC_OK;
 }
 
+void drop_graphs(Ctx* c) {
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+    c->graphs.clear();
+}
+
+// Run `body` (which returns a status) as a CUDA graph cached under the key
+// (k0, k1, k2, n): captured on first use, replayed after.  A failure inside
+// the capture ends it and returns the failure.
+template <typename F>
+int graph_run(Ctx* c, const void* k0, const void* k1, const void* k2, int64_t n, F body) {
+    if (!c->use_graphs) return body();
+    for (auto& g : c->graphs)
+        if (g.k0 == k0 && g.k1 == k1 && g.k2 == k2 && g.n == n) {
+            BSC_CUDA(c, cudaGraphLaunch(g.exec, c->stream));
+            c->launches += g.kernels;
+            return BSC_OK;
+        }
+    BSC_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = c->launches;
+    c->capturing = true;
+    const int rc = body();
+    c->capturing = false;
+    cudaGraph_t graph = nullptr;
+    cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+    if (rc || e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        (void)cudaGetLastError();
+        return rc ? rc : cuda_err(c, e, "cudaStreamEndCapture");
+    }
+    cudaGraphExec_t exec = nullptr;
+    e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return cuda_err(c, e, "cudaGraphInstantiate");
+    c->graphs.push_back({k0, k1, k2, n, exec, c->launches - l0});
+    BSC_CUDA(c, cudaGraphLaunch(exec, c->stream));
+    return BSC_OK;
+}
+
 // `xbest` (optional): keep the minimum-residual iterate there and stop a
 // diverging solve; *rr_out is then the squared best residual
 template <typename Op, typename T>
@@ -943,11 +982,35 @@ int run_fgmres_ir(Ctx* c, int64_t n, bsc_solve_info* si) {
     return si->status;
 }
 
+// with BSC_PROFILE_ITER: the phases of the last multigrid-FGMRES iteration
+// (events ev_it[0..5], the stream idle) into timing slots BICG_1..5
+void mg_iter_profile(Ctx* c) {
+    if (!c->prof_iter) return;
+    for (int k = 0; k < 5; ++k) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, c->ev_it[k], c->ev_it[k + 1]) == cudaSuccess) {
+            c->ms[BSC_T_BICG_1 + k] += ms;
+            c->calls[BSC_T_BICG_1 + k]++;
+        }
+    }
+    (void)cudaGetLastError();
+}
+
+// the SpMV bracketed by ev_spmv (the stream idle) into the SPMV slot
+void spmv_time(Ctx* c) {
+    if (!c->timing) return;
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, c->ev_spmv[0], c->ev_spmv[1]) == cudaSuccess) {
+        c->ms[BSC_T_SPMV] += ms;
+        c->calls[BSC_T_SPMV]++;
+    }
+    (void)cudaGetLastError();
+}
+
 // Flexible GMRES(m) in FP64 on the FP64 operator, right-preconditioned by
-// one multigrid V-cycle per iteration (mg.cu), in FP64 (ZT = double) or FP32
-// (ZT = float, the mixed path).  Stops on the Arnoldi residual estimate and
-// reports the true residual of the returned pressure.
-template <typename ZT>
+// one FP64 multigrid V-cycle per iteration (mg.cu).  Each iteration runs as a
+// cached CUDA graph, one per Krylov column.  Stops on the Arnoldi residual
+// estimate and reports the true residual of the returned pressure.
 int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
     const bsc_params& P = c->P;
     const int G = RED_GRID, B = RED_BLOCK;
@@ -959,7 +1022,7 @@ int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
     double* x = c->S.p;
     double* w = c->tv;
     double* V = mg.V;
-    ZT* Z = (ZT*)mg.Z;
+    double* Z = mg.Z;
     int first = 1, iters = 0, rc;
     for (;;) {
         k_resid<EllOp<double>, double><<<G, B, 0, c->stream>>>(n, A, x, c->b, c->r, c->part);
@@ -972,41 +1035,40 @@ int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
         k_fg_v0<double><<<G, B, 0, c->stream>>>(n, c->r, V, c->sc2);
         BSC_LAUNCH(c);
         for (int j = 0; j < m && iters < P.maxit; ++j) {
-            ZT* zj = Z + (int64_t)j * n;
+            double* zj = Z + (int64_t)j * n;
             const double* vj = V + (int64_t)j * n;
-            if constexpr (sizeof(ZT) == 4)
-                rc = mg_vcycle_f32(c, vj, (float*)zj);
-            else
-                rc = mg_vcycle_f64(c, vj, (double*)zj);
+            // one iteration (V-cycle, SpMV, CGS2, Givens) as a cached graph per
+            // column j, keyed by the cell map too, whose buffer a Morton
+            // reorder swaps
+            rc = graph_run(c, c->pcell, vj, zj, n, [&]() -> int {
+                if (int r = mg_vcycle_f64(c, vj, zj)) return r;
+                // the SpMV w = A z_j is bracketed by events: the dominant
+                // HBM-bound kernel, timed in place
+                if (c->timing) record_event(c, c->ev_spmv[0]);
+                k_spmv_z<double><<<G, B, 0, c->stream>>>(n, A, zj, w, c->sc2);
+                if (c->timing) record_event(c, c->ev_spmv[1]);
+                if (c->prof_iter) record_event(c, c->ev_it[4]);
+                for (int pass = 0; pass < 2; ++pass) {
+                    k_fg_mdot<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc2);
+                    k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc2);
+                    k_fg_maxpy<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, pass, c->part, c->sc2);
+                }
+                k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, j);
+                k_fg_next<double><<<G, B, 0, c->stream>>>(n, w, V, j, c->sc2);
+                if (c->prof_iter) record_event(c, c->ev_it[5]);
+                c->launches += 9;
+                BSC_CUDA(c, cudaGetLastError());
+                return BSC_OK;
+            });
             if (rc) return rc;
-            // the FP64 SpMV w = A z_j is bracketed by events: the dominant
-            // HBM-bound kernel, timed in place
-            if (c->timing) cudaEventRecord(c->ev_spmv[0], c->stream);
-            k_spmv_z<ZT><<<G, B, 0, c->stream>>>(n, A, zj, w, c->sc2);
-            if (c->timing) cudaEventRecord(c->ev_spmv[1], c->stream);
-            for (int pass = 0; pass < 2; ++pass) {
-                k_fg_mdot<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc2);
-                k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc2);
-                k_fg_maxpy<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, pass, c->part, c->sc2);
-            }
-            k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, j);
-            k_fg_next<double><<<G, B, 0, c->stream>>>(n, w, V, j, c->sc2);
-            c->launches += 9;
-            BSC_CUDA(c, cudaGetLastError());
             ++iters;
             if ((rc = fetch_outer(c))) return rc;
-            if (c->timing) {  // the stream is idle after fetch_outer
-                float ms = 0.f;
-                if (cudaEventElapsedTime(&ms, c->ev_spmv[0], c->ev_spmv[1]) == cudaSuccess) {
-                    c->ms[BSC_T_SPMV] += ms;
-                    c->calls[BSC_T_SPMV]++;
-                }
-                (void)cudaGetLastError();
-            }
+            mg_iter_profile(c);
+            spmv_time(c);
             if (c->h_sc[1].tmp[2] != 0.0) break;
         }
         k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc2, c->Hd, F);
-        k_fg_update_z<ZT><<<G, B, 0, c->stream>>>(n, x, Z, c->Hd, F, c->sc2);
+        k_fg_update_z<double><<<G, B, 0, c->stream>>>(n, x, Z, c->Hd, F, c->sc2);
         c->launches += 2;
         BSC_CUDA(c, cudaGetLastError());
         if (c->h_sc[1].breakdown && c->h_sc[1].tmp[1] == 0.0) break;
@@ -1021,6 +1083,187 @@ int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
     BSC_CUDA(c, cudaStreamSynchronize(c->stream));
     si->iterations = iters;
     si->outer = 1;
+    si->b_norm = c->h_sc[1].bnorm;
+    si->r0_norm = c->h_sc[1].r0norm;
+    si->rel_residual = nrm[1] > 0 ? nrm[0] / nrm[1] : nrm[0];
+    const double ref = rel_r0 ? si->r0_norm : si->b_norm;
+    si->converged = nrm[0] <= P.tol * ref ? 1 : 0;
+    si->status = si->converged ? BSC_OK : BSC_E_NOT_CONVERGED;
+    return si->status;
+}
+
+// ---- mixed path: FGMRES-IR with an FP32 inner FGMRES + FP32 V-cycle -------------
+// The inner Krylov method runs entirely in FP32 (basis, Gram-Schmidt, SpMV,
+// V-cycle); dot products are summed per thread in FP32 and across threads in
+// FP64.  The outer iteration recomputes the true residual in FP64 and adds
+// each FP32 correction to the FP64 pressure (iterative refinement).
+__global__ void __launch_bounds__(RED_BLOCK) k_norm2f(int64_t n, const float* __restrict__ r,
+                                                       double* __restrict__ part) {
+    float acc = 0.f;
+    GRID_LOOP(i, n) acc += r[i] * r[i];
+    double a[2] = {(double)acc, (double)acc};
+    block_partials<2>(a, part);
+}
+
+__global__ void k_fgf_v0(int64_t n, const float* __restrict__ r, float* __restrict__ V0,
+                         const Scalars* __restrict__ sc) {
+    if (sc->done) return;
+    const float inv = (float)(1.0 / sc->tmp[0]);
+    GRID_LOOP(i, n) V0[i] = r[i] * inv;
+}
+
+__global__ void k_fgf_next(int64_t n, const float* __restrict__ w, float* __restrict__ V, int j,
+                           const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    const float inv = (float)(1.0 / sc->tmp[3]);
+    float* vn = V + (int64_t)(j + 1) * n;
+    GRID_LOOP(i, n) vn[i] = w[i] * inv;
+}
+
+__global__ void __launch_bounds__(RED_BLOCK) k_spmv_f(int64_t n, EllOp<float> A, const float* __restrict__ z,
+                                                       float* __restrict__ w, const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    GRID_LOOP(i, n) w[i] = A.template row<float, float>(i, z);
+}
+
+// h_i = V_i . w for i <= j, 8 columns per pass
+__global__ void __launch_bounds__(RED_BLOCK) k_fgf_mdot(int64_t n, const float* __restrict__ V,
+                                                         const float* __restrict__ w, int j,
+                                                         double* __restrict__ part, const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    for (int i0 = 0; i0 <= j; i0 += 8) {
+        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        const int cntv = min(8, j + 1 - i0);
+        GRID_LOOP(k, n) {
+            const float wk = w[k];
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (q < cntv) acc[q] += V[(int64_t)(i0 + q) * n + k] * wk;
+        }
+        double accd[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) accd[q] = (double)acc[q];
+        block_partials<8>(accd, part + (int64_t)i0 * RED_GRID);
+        __syncthreads();
+    }
+}
+
+// w -= sum_i h_i V_i; partial (w.w) when `norm`
+__global__ void __launch_bounds__(RED_BLOCK) k_fgf_maxpy(int64_t n, const float* __restrict__ V, float* __restrict__ w,
+                                                          int j, const double* __restrict__ Hd, FgLayout F, int norm,
+                                                          double* __restrict__ part, const Scalars* __restrict__ sc) {
+    if (fg_skip(sc)) return;
+    __shared__ float h[FG_MAXM];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) h[i] = (float)Hd[F.hc(i)];
+    __syncthreads();
+    float acc = 0.f;
+    GRID_LOOP(k, n) {
+        float s = w[k];
+        for (int i = 0; i <= j; ++i) s -= h[i] * V[(int64_t)i * n + k];
+        w[k] = s;
+        acc += s * s;
+    }
+    double a[1] = {(double)acc};
+    if (norm) block_partials<1>(a, part);
+}
+
+// x += sum_i y_i z_i (FP64 pressure, FP32 preconditioned vectors)
+__global__ void k_ir_addz(int64_t n, double* __restrict__ x, const float* __restrict__ Z,
+                          const double* __restrict__ Hd, FgLayout F, const Scalars* __restrict__ sc) {
+    if (sc->done) return;
+    __shared__ double y[FG_MAXM];
+    const int k = (int)sc->tmp[1];
+    for (int i = threadIdx.x; i < k; i += blockDim.x) y[i] = Hd[F.y(i)];
+    __syncthreads();
+    GRID_LOOP(q, n) {
+        double s = x[q];
+        for (int i = 0; i < k; ++i) s += y[i] * (double)Z[(int64_t)i * n + q];
+        x[q] = s;
+    }
+}
+
+int run_fgmres_ir_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
+    const bsc_params& P = c->P;
+    const int G = RED_GRID, B = RED_BLOCK;
+    const int rel_r0 = P.tol_mode == BSC_TOL_REL_R0;
+    Mg& mg = c->mg;
+    const int m = mg.m;
+    const FgLayout F{m};
+    const EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+    const EllOp<float> Af{c->avalf, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+    double* x = c->S.p;
+    float *V = mg.Vf, *Z = mg.Zf, *w = mg.wf, *rf = mg.rf;
+    // each inner solve asks for the reduction still needed (with a margin),
+    // but for no more than inner_tol, the most the FP32 arithmetic is trusted
+    // to deliver; the FP64 outer loop compounds the reductions
+    const double floor_tol = std::min(std::max(P.inner_tol, 1e-7), 0.5);
+    int first = 1, outer = 0, inner = 0, rc;
+    for (;;) {
+        k_resid<EllOp<double>, double><<<G, B, 0, c->stream>>>(n, A, x, c->b, c->r, c->part);
+        BSC_LAUNCH(c);
+        k_fg_start<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, first, P.tol, rel_r0);
+        BSC_LAUNCH(c);
+        first = 0;
+        if ((rc = fetch_outer(c))) return rc;
+        if (c->h_sc[1].done || outer >= P.max_outer || inner >= P.maxit) break;
+        ++outer;
+        const double beta = c->h_sc[1].tmp[0], need = c->h_sc[1].target / beta;
+        const double inner_tol = std::min(std::max(floor_tol, 0.3 * need), 0.5);
+        // inner: A d = r in FP32 from d = 0, one FGMRES(m) cycle
+        k_d2f<<<G, B, 0, c->stream>>>(n, c->r, rf);
+        k_norm2f<<<G, B, 0, c->stream>>>(n, rf, c->part);
+        k_fg_start<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, 1, inner_tol, 1);
+        k_fgf_v0<<<G, B, 0, c->stream>>>(n, rf, V, c->sc);
+        c->launches += 4;
+        for (int j = 0; j < m && inner < P.maxit; ++j) {
+            float* zj = Z + (int64_t)j * n;
+            const float* vj = V + (int64_t)j * n;
+            // one inner iteration as a cached graph per column j (and cell map)
+            rc = graph_run(c, c->pcell, vj, zj, n, [&]() -> int {
+                if (int r = mg_vcycle_f32(c, vj, zj)) return r;
+                // the FP32 SpMV w = A z_j is bracketed by events (the
+                // dominant HBM-bound kernel, timed in place)
+                if (c->timing) record_event(c, c->ev_spmv[0]);
+                k_spmv_f<<<G, B, 0, c->stream>>>(n, Af, zj, w, c->sc);
+                if (c->timing) record_event(c, c->ev_spmv[1]);
+                if (c->prof_iter) record_event(c, c->ev_it[4]);
+                for (int pass = 0; pass < 2; ++pass) {
+                    k_fgf_mdot<<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc);
+                    k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc);
+                    k_fgf_maxpy<<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, pass, c->part, c->sc);
+                }
+                k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, j);
+                k_fgf_next<<<G, B, 0, c->stream>>>(n, w, V, j, c->sc);
+                if (c->prof_iter) record_event(c, c->ev_it[5]);
+                c->launches += 9;
+                BSC_CUDA(c, cudaGetLastError());
+                return BSC_OK;
+            });
+            if (rc) return rc;
+            ++inner;
+            if ((rc = fetch_scalars(c))) return rc;
+            mg_iter_profile(c);
+            spmv_time(c);
+            if (c->h_sc[0].tmp[2] != 0.0) break;
+        }
+        k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc, c->Hd, F);
+        k_ir_addz<<<G, B, 0, c->stream>>>(n, x, Z, c->Hd, F, c->sc);
+        c->launches += 2;
+        BSC_CUDA(c, cudaGetLastError());
+        if (c->debug)
+            std::fprintf(stderr, "[bsc] FGMRES-IR outer %d: |r|/target %.3e, inner tol %.1e, %d inner iterations\n",
+                         outer, beta / c->h_sc[1].target, inner_tol, inner);
+    }
+    double* norms = c->Hd + F.size();
+    k_resid<EllOp<double>, double><<<G, B, 0, c->stream>>>(n, A, x, c->b, c->r, c->part);
+    BSC_LAUNCH(c);
+    k_ir_norms<<<1, B, 0, c->stream>>>(c->part, norms);
+    BSC_LAUNCH(c);
+    double nrm[2];
+    BSC_CUDA(c, cudaMemcpyAsync(nrm, norms, 2 * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+    si->iterations = inner;
+    si->outer = outer;
     si->b_norm = c->h_sc[1].bnorm;
     si->r0_norm = c->h_sc[1].r0norm;
     si->rel_residual = nrm[1] > 0 ? nrm[0] / nrm[1] : nrm[0];
@@ -1048,7 +1291,7 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info) {
     double rr = 0.0;
     if (P.precond == BSC_PRECOND_MG) {
         if ((rc = mg_setup(c))) return rc;
-        return c->mixed ? run_fgmres_mg<float>(c, n, si) : run_fgmres_mg<double>(c, n, si);
+        return c->mixed ? run_fgmres_ir_mg(c, n, si) : run_fgmres_mg(c, n, si);
     }
     if (!c->mixed) {
         EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};

@@ -315,7 +315,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--config", default=CONFIG)
     ap.add_argument("--solver", default="bicgstab", choices=("bicgstab", "fgmres"))
-    ap.add_argument("--inner-tol", type=float, default=0.1)
+    ap.add_argument("--inner-tol", type=float, default=None,
+                    help="mixed path: relative tolerance of each FP32 inner solve (default 1e-5 with the "
+                         "multigrid preconditioner, 0.1 for the BiCGSTAB sweeps without it)")
     ap.add_argument("--precond", default="mg", choices=("mg", "none"),
                     help="PPE preconditioner: cell multigrid inside FGMRES, or none (the reference's solvers)")
     ap.add_argument("--restart", type=int, default=40)
@@ -324,6 +326,8 @@ def main():
     ap.add_argument("--cpu-iters", type=float, default=1350.0,
                     help="PPE iterations per step the reference arm's sample is scaled to")
     args = ap.parse_args()
+    if args.inner_tol is None:
+        args.inner_tol = 1e-5 if args.precond == "mg" else 0.1
     dist = Dist()
     from beach_slope_confined_gb300 import scenario as sc
 

@@ -169,8 +169,11 @@ enum {
     BSC_T_PPE_SOLVE, BSC_T_COMP_VEL, BSC_T_COMP_POS, BSC_T_FREESURF,
     BSC_T_SHIFT, BSC_T_TIMESTEP, BSC_T_PISTON, BSC_T_STEP,
     BSC_T_SPMV, BSC_T_UPLOAD, BSC_T_DOWNLOAD,
-    /* the five kernels of one BiCGSTAB iteration (one iteration per batch is
-     * bracketed when the BSC_PROFILE_ITER=1 environment variable is set) */
+    /* with the BSC_PROFILE_ITER=1 environment variable: the five kernels of
+     * one BiCGSTAB iteration per batch; with the multigrid preconditioner,
+     * the phases of every FGMRES iteration instead: fine-level pre-smoothing
+     * and restriction, coarse levels, fine-level post-smoothing, the SpMV,
+     * and the orthogonalisation */
     BSC_T_BICG_1, BSC_T_BICG_2, BSC_T_BICG_3, BSC_T_BICG_4, BSC_T_BICG_5
 };
 
