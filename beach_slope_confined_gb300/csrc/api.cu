@@ -386,6 +386,7 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
     if (const char* e = std::getenv("BSC_DEBUG")) c->debug = e[0] == '1';
     if (const char* e = std::getenv("BSC_SPMV_UNROLL")) c->spmv_unroll = e[0] == '1';
     if (const char* e = std::getenv("BSC_PROFILE_ITER")) c->prof_iter = e[0] == '1';
+    if (const char* e = std::getenv("BSC_MG_TAIL")) c->mg_tail_cells = std::atoi(e);
     for (int k = 0; k < 6; ++k) cudaEventCreate(&c->ev_it[k]);
     *out = c;
     return BSC_OK;

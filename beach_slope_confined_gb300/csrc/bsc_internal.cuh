@@ -218,6 +218,7 @@ struct Ctx {
     bool debug = false;           // BSC_DEBUG=1: per-sweep solver trace on stderr
     int spmv_unroll = 1;          // four ELL entries per round (BSC_SPMV_UNROLL=0: one)
     bool prof_iter = false;       // BSC_PROFILE_ITER=1: events around each Krylov kernel
+    int mg_tail_cells = -1;       // BSC_MG_TAIL=<cells>: largest level in the single-CTA tail
     cudaEvent_t ev_it[6] = {};
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64
     float* Vf = nullptr;          // FGMRES basis FP32 (mixed)
@@ -253,6 +254,7 @@ inline void record_event(Ctx* c, cudaEvent_t e) {
 
 // destroy the cached graphs (their kernels hold pointers that are about to change)
 void drop_graphs(Ctx* c);
+
 
 // ---- stage timer: a pair of CUDA events on the context stream -----------------
 struct StageTimer {

@@ -187,14 +187,18 @@ __global__ void k_mg_to_f32(int64_t n, const double* __restrict__ a, float* __re
 }
 
 // ---- V-cycle, structured levels (l >= 1) -------------------------------------------
+// The per-cell helpers take plain (not __restrict__) pointers: the tail
+// kernel reads, in later phases, vectors it wrote in earlier ones, so those
+// loads must stay on the coherent path (within one CTA, a block barrier makes
+// the writes visible).
+
 // One damped-Jacobi update of cell c: x + w D^-1 (b - A x), where the input x is
 //   MODE 0: xin;
 //   MODE 1: w D^-1 b (the first sweep from a zero guess, folded in);
 //   MODE 2: xin + scale * xc[parent] (the prolonged coarse correction, folded in).
 template <typename T, int MODE>
-__device__ __forceinline__ T smooth_at(int nx, int ny, int64_t c, const T* __restrict__ A,
-                                       const T* __restrict__ dinv, const T* __restrict__ b,
-                                       const T* __restrict__ xin, const T* __restrict__ xc, int nyc, T scale, T w) {
+__device__ __forceinline__ T smooth_at(int nx, int ny, int64_t c, const T* A, const T* dinv, const T* b,
+                                       const T* xin, const T* xc, int nyc, T scale, T w) {
     const int64_t nc = (int64_t)nx * ny;
     const int cx = (int)(c / ny), cy = (int)(c % ny);
     auto xv = [&](int gx, int gy) -> T {
@@ -216,8 +220,7 @@ __device__ __forceinline__ T smooth_at(int nx, int ny, int64_t c, const T* __res
 
 // the residual b - A x summed over the 2x2 children of coarse cell C
 template <typename T>
-__device__ __forceinline__ T restrict_at(int nx, int ny, const T* __restrict__ A, const T* __restrict__ b,
-                                         const T* __restrict__ x, int64_t C, int nyc) {
+__device__ __forceinline__ T restrict_at(int nx, int ny, const T* A, const T* b, const T* x, int64_t C, int nyc) {
     const int64_t nc = (int64_t)nx * ny;
     const int CX = (int)(C / nyc), CY = (int)(C % nyc);
     T sum = 0;
@@ -271,8 +274,11 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const 
 // solve and prolongations as the per-level kernels, phase by phase with a
 // block barrier between phases (each phase reads what the previous one
 // wrote).  Saves two to four launches per level where a level is too small
-// to fill the GPU.
-constexpr int MG_TAIL_CELLS = 8192;
+// to fill the GPU; the thresholds are measured (a single SM is latency-bound
+// above about a thousand FP32 cells, and FP64 runs at a small fraction of
+// the FP32 rate on this GPU).
+constexpr int MG_TAIL_CELLS = 1100;
+constexpr int MG_TAIL_CELLS_F64 = 300;
 constexpr int MG_TAIL_THREADS = 1024;
 template <typename T>
 struct TailLevel {
@@ -476,8 +482,7 @@ int cycle_level(Ctx* c, int l) {
     }
     const MgLevel& Lc = mg.L[l + 1];
     Lv<T> vc = level_view<T>(Lc);
-    k_mg_restrict<T><<<blocks_for(Lc.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.b, cur, Lc.nx, Lc.ny,
-                                                                             vc.b);
+    k_mg_restrict<T><<<blocks_for(Lc.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.b, cur, Lc.nx, Lc.ny, vc.b);
     BSC_LAUNCH(c);
     if (int rc = cycle_level<T>(c, l + 1)) return rc;
     // post-smoothing: the prolongation folded into the first sweep; the last
@@ -485,11 +490,9 @@ int cycle_level(Ctx* c, int l) {
     for (int k = 0; k < nu; ++k) {
         T* out = (k == nu - 1) ? v.x : (cur == v.y ? v.t : v.y);
         if (k == 0)
-            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w,
-                                                             out);
+            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w, out);
         else
-            k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w,
-                                                             out);
+            k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w, out);
         BSC_LAUNCH(c);
         cur = out;
     }
@@ -523,8 +526,7 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
     BSC_LAUNCH(c);
     const MgLevel& L1 = mg.L[1];
     Lv<T> v1 = level_view<T>(L1);
-    k_mg0_restrict<T><<<blocks_for(L1.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L1.nc, c->cell_start, c->cell_count,
-                                                                              c->sorted, R0, v1.b);
+    k_mg0_restrict<T><<<blocks_for(L1.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L1.nc, c->cell_start, c->cell_count, c->sorted, R0, v1.b);
     BSC_LAUNCH(c);
     if (c->prof_iter) record_event(c, c->ev_it[1]);
     if (int rc = cycle_level<T>(c, 1)) return rc;
@@ -581,8 +583,9 @@ int mg_alloc(Ctx* c) {
     }
     mg.nlev = nlev;
     // one SM runs the tail: FP32 levels up to MG_TAIL_CELLS cells, FP64 ones
-    // (a small fraction of the FP32 rate) up to an eighth of that
-    const int64_t tail_cells = f32 ? MG_TAIL_CELLS : MG_TAIL_CELLS / 8;
+    // up to MG_TAIL_CELLS_F64
+    int64_t tail_cells = f32 ? MG_TAIL_CELLS : MG_TAIL_CELLS_F64;
+    if (c->mg_tail_cells >= 0) tail_cells = c->mg_tail_cells;
     mg.tail_l0 = nlev;
     while (mg.tail_l0 > 1 && (int64_t)mg.L[mg.tail_l0 - 1].nx * mg.L[mg.tail_l0 - 1].ny <= tail_cells)
         --mg.tail_l0;
@@ -593,12 +596,14 @@ int mg_alloc(Ctx* c) {
         L.nc = (int64_t)L.nx * L.ny;
         if ((rc = mg_dalloc(c, &L.A, 9 * L.nc)) || (rc = mg_dalloc(c, &L.dinv, L.nc))) return rc;
         if (f32 && ((rc = mg_dalloc(c, &L.Af, 9 * L.nc)) || (rc = mg_dalloc(c, &L.dinvf, L.nc)))) return rc;
+        // four vectors, each on a 256-byte boundary (no cache line shared)
+        const int64_t stride = ((L.nc * (int64_t)vs + 255) / 256) * 256;
         unsigned char* vec = nullptr;
-        if ((rc = mg_dalloc(c, &vec, (int64_t)(4 * L.nc) * (int64_t)vs))) return rc;
+        if ((rc = mg_dalloc(c, &vec, 4 * stride))) return rc;
         L.b = vec;
-        L.x = vec + L.nc * vs;
-        L.y = vec + 2 * L.nc * vs;
-        L.t = vec + 3 * L.nc * vs;
+        L.x = vec + stride;
+        L.y = vec + 2 * stride;
+        L.t = vec + 3 * stride;
     }
     const int64_t nco = mg.L[nlev].nc;
     if ((rc = mg_dalloc(c, &mg.cinv, nco * nco))) return rc;

@@ -171,22 +171,42 @@ struct CsrOp {
 // reductions: RED_GRID blocks write partials; consumers reduce them in a
 // fixed order (deterministic for a given n)
 // ============================================================================
-template <int D>
-__device__ __forceinline__ void block_partials(double (&v)[D], double* __restrict__ part) {
+// Warp sum into lane 0.  Only the lanes that feed lane 0 add (16, 8, 4, 2, 1
+// of them): lane 0 does the same additions in the same order as a full
+// butterfly, with a fifth of the FP64 work, which is what GB300's FP64 pipe
+// is short of.
+__device__ __forceinline__ double warp_sum_to_lane0(double x) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double y = __shfl_down_sync(0xffffffffu, x, o);
+        if (lane < o) x += y;
+    }
+    return x;
+}
+__device__ __forceinline__ float warp_sum_to_lane0(float x) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+    return x;
+}
+
+// per-block partial sums of D values into part[d * RED_GRID + block]; the
+// values may be float (warp sums in FP32, block sum in FP64) or double
+template <int D, typename V>
+__device__ __forceinline__ void block_partials(V (&v)[D], double* __restrict__ part) {
     __shared__ double sh[D][RED_BLOCK / 32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
     for (int d = 0; d < D; ++d) {
-        double x = v[d];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
-        if (lane == 0) sh[d][w] = x;
+        const V x = warp_sum_to_lane0(v[d]);
+        if (lane == 0) sh[d][w] = (double)x;
     }
     __syncthreads();
     if (threadIdx.x < 32) {
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             double x = (lane < RED_BLOCK / 32) ? sh[d][lane] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            x = warp_sum_to_lane0(x);
             if (lane == 0) part[d * RED_GRID + blockIdx.x] = x;
         }
     }
@@ -202,7 +222,7 @@ __device__ __forceinline__ void reduce_partials(const double* __restrict__ part,
     for (int d = 0; d < D; ++d) {
         double x = 0.0;
         for (int k = threadIdx.x; k < RED_GRID; k += blockDim.x) x += __ldcg(part + d * RED_GRID + k);
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        x = warp_sum_to_lane0(x);
         if (lane == 0) sh[d][w] = x;
     }
     __syncthreads();
@@ -210,7 +230,7 @@ __device__ __forceinline__ void reduce_partials(const double* __restrict__ part,
 #pragma unroll
         for (int d = 0; d < D; ++d) {
             double x = (lane < RED_BLOCK / 32) ? sh[d][lane] : 0.0;
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+            x = warp_sum_to_lane0(x);
             if (lane == 0) res[d] = x;
         }
     }
@@ -508,7 +528,7 @@ __global__ void k_fg_hcol(const double* __restrict__ part, double* Hd, FgLayout 
     for (int i = w; i <= j; i += nw) {
         double x = 0.0;
         for (int k = lane; k < RED_GRID; k += 32) x += part[(int64_t)i * RED_GRID + k];
-        for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+        x = warp_sum_to_lane0(x);
         if (lane == 0) {
             Hd[F.hc(i)] = x;
             Hd[F.H(i, j)] = accumulate ? Hd[F.H(i, j)] + x : x;
@@ -1101,7 +1121,7 @@ __global__ void __launch_bounds__(RED_BLOCK) k_norm2f(int64_t n, const float* __
                                                        double* __restrict__ part) {
     float acc = 0.f;
     GRID_LOOP(i, n) acc += r[i] * r[i];
-    double a[2] = {(double)acc, (double)acc};
+    float a[2] = {acc, acc};
     block_partials<2>(a, part);
 }
 
@@ -1140,10 +1160,7 @@ __global__ void __launch_bounds__(RED_BLOCK) k_fgf_mdot(int64_t n, const float* 
             for (int q = 0; q < 8; ++q)
                 if (q < cntv) acc[q] += V[(int64_t)(i0 + q) * n + k] * wk;
         }
-        double accd[8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) accd[q] = (double)acc[q];
-        block_partials<8>(accd, part + (int64_t)i0 * RED_GRID);
+        block_partials<8>(acc, part + (int64_t)i0 * RED_GRID);
         __syncthreads();
     }
 }
@@ -1163,7 +1180,7 @@ __global__ void __launch_bounds__(RED_BLOCK) k_fgf_maxpy(int64_t n, const float*
         w[k] = s;
         acc += s * s;
     }
-    double a[1] = {(double)acc};
+    float a[1] = {acc};
     if (norm) block_partials<1>(a, part);
 }
 
