@@ -51,6 +51,13 @@ static void derive_kparams(Ctx* c) {
     K.h = h;
     K.H = 2 * h;
     K.H2 = K.H * K.H;
+    // the neighbour test sqrt((xi-xj)^2+(yi-yj)^2) < 2h (search.f90:59) as a
+    // test on d2: the correctly rounded square root is monotone, so the test
+    // holds exactly for d2 below the smallest double whose root reaches 2h
+    double t = K.H2;
+    while (t > 0.0 && std::sqrt(t) >= K.H) t = std::nextafter(t, 0.0);
+    while (std::sqrt(t) < K.H) t = std::nextafter(t, INFINITY);
+    K.H2x = t;
     K.lam = P.lam;
     K.dl = P.dl;
     K.rho0 = P.rho0;

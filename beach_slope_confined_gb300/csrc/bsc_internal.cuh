@@ -59,6 +59,7 @@ struct Scalars {
 struct KParams {
     int kernel;
     double h, H, H2, lam, dl, rho0, rel_den, g, csh, maxshift, free_thr;
+    double H2x;  // sqrt_rn(d2) < H exactly when d2 < H2x (the reference's neighbour test)
     double por, alpha, beta, d50;
     double eddy_cs, eddy_cv, eddy_ce, varts_ps;
     double bxmin, bxmax;

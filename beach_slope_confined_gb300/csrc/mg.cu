@@ -212,8 +212,7 @@ __device__ __forceinline__ T smooth_at(int nx, int ny, int64_t c, const T* A, co
     for (int s = 0; s < 9; ++s) {
         const int gx = cx + s / 3 - 1, gy = cy + s % 3 - 1;
         if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
-        const T a = A[s * nc + c];
-        if (a != (T)0) ax += a * xv(gx, gy);
+        ax += A[s * nc + c] * xv(gx, gy);  // no test on the loaded value: loads stay independent
     }
     return xv(cx, cy) + w * dinv[c] * (b[c] - ax);
 }
@@ -236,8 +235,7 @@ __device__ __forceinline__ T restrict_at(int nx, int ny, const T* A, const T* b,
             for (int s = 0; s < 9; ++s) {
                 const int gx = fx + s / 3 - 1, gy = fy + s % 3 - 1;
                 if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
-                const T av = A[s * nc + f];
-                if (av != (T)0) ax += av * x[(int64_t)gx * ny + gy];
+                ax += A[s * nc + f] * x[(int64_t)gx * ny + gy];
             }
             sum += b[f] - ax;
         }

@@ -126,8 +126,9 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                     if (fdx * fdx + fdy * fdy > H2f) continue;
                 }
                 const double dx = xi - S.x[j], dy = yi - S.y[j];
-                const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-                if (!(r < K.H)) continue;
+                const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+                if (!(d2 < K.H2x)) continue;  // exactly sqrt(d2) < 2h, no FMA contraction
+                const double r = __dsqrt_rn(d2);
                 // grad W per pair in FP64 (stored in FP64, and in FP32 for the
                 // FP32 pair sums of the mixed path); the M sum runs in R
                 const double F = grad_factor<double>(K, r);
@@ -250,9 +251,11 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
                     if (fdx * fdx + fdy * fdy > H2f) continue;
                 }
                 const double dx = xi - sx[s], dy = yi - sy[s];
-                const double r = __dsqrt_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)));
-                if (!(r < K.H)) continue;
-                frac += ((R)1 - (R)spor[s]) * kern_w<R>(K, (R)r) * (R)svol[s];
+                const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+                if (!(d2 < K.H2x)) continue;  // exactly sqrt(d2) < 2h
+                // W(r) in R: an FP32 root for the FP32 sum, the exact one for FP64
+                const R r = sizeof(R) == 4 ? (R)sqrtf((float)d2) : (R)__dsqrt_rn(d2);
+                frac += ((R)1 - (R)spor[s]) * kern_w<R>(K, r) * (R)svol[s];
             }
         }
     }

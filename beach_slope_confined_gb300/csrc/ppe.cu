@@ -46,11 +46,15 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
     const int tid_i = S.tid[i];
     const bool free_i = S.flags[i] & BSC_FLAG_FREE;
     const double xi = S.x[i], yi = S.y[i];
-    const R ni = (R)S.por[i], rhoi = (R)S.rho[i], qi = (R)q[i];
+    const R ni = (R)S.por[i], qi = (R)q[i];
     const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
     const double usxi = usx[i], usyi = usy[i];
     const R mi_over_rhoi = (R)(S.mass[i] / S.rho[i]);
     const R lamp_f = (R)(1.0 / (K.rho0 * K.rel_den));
+    // per-row quotients hoisted out of the pair loop (FP64 divisions are
+    // expensive on this GPU): 1/n_i, and v*_i/n_i for the fixed-wall rows
+    const R inv_ni = (R)1 / ni;
+    const double vxi_n = S.vxs[i] / (double)ni, vyi_n = S.vys[i] / (double)ni;
     const int m = cnt[i];
     R dia = 0, fv = 0;
     for (int k = 0; k < m; ++k) {
@@ -71,13 +75,14 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
             // divergence of the porous-weighted predicted velocity (:241-270)
             R ddx, ddy;
             if (tid_j == BSC_TID_FLUID) {
-                const R nj = (R)S.por[j], rhoj = (R)S.rho[j], qj = (R)q[j];
-                const R rho_ij = (R)2 * rhoj * rhoi / (nj * ni) / (qj + qi);
+                // 2 rho_i rho_j / (n_i n_j (rho_i/n_i + rho_j/n_j)) = 2 q_i q_j / (q_i + q_j)
+                const R qj = (R)q[j];
+                const R rho_ij = (R)2 * qi * qj / (qi + qj);
                 ddx = rho_ij * (R)(usx[j] - usxi);
                 ddy = rho_ij * (R)(usy[j] - usyi);
             } else {
-                ddx = qi * ((R)(S.vxs[j] - S.vxs[i]) / ni);
-                ddy = qi * ((R)(S.vys[j] - S.vys[i]) / ni);
+                ddx = qi * ((R)(S.vxs[j] - S.vxs[i]) * inv_ni);
+                ddy = qi * ((R)(S.vys[j] - S.vys[i]) * inv_ni);
             }
             fv += pvol * (ddx * gx + ddy * gy);
         } else if (tid_i == BSC_TID_GHOST) {
@@ -94,8 +99,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
                 val = -t;
                 dia += t;
                 const R qj = (R)q[j];
-                const R ddx = qj * (R)(usx[j] - S.vxs[i] / (double)ni);
-                const R ddy = qj * (R)(usy[j] - S.vys[i] / (double)ni);
+                const R ddx = qj * (R)(usx[j] - vxi_n);
+                const R ddy = qj * (R)(usy[j] - vyi_n);
                 fv += mi_over_rhoi * (ddx * gx + ddy * gy);
             } else {
                 const R t = (R)2 * pvol * ((R)dx * g.x + (R)dy * g.y) * p_dist;
