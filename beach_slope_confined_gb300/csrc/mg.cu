@@ -37,30 +37,41 @@ constexpr int MG_BLOCK = 256;
 __device__ __forceinline__ int stencil_slot(int dx, int dy) { return (dx + 1) * 3 + (dy + 1); }
 
 // ---- hierarchy ----------------------------------------------------------------
-// level 1 from the fine matrix: thread per cell, its particles in the cell
-// list's (id-sorted) order, each particle's row in neighbour-list order
-__global__ void k_mg_galerkin0(int nx, int ny, const int32_t* __restrict__ cell_start,
+// level 1 from the fine matrix, in two coalesced passes: (1) thread per row,
+// the row's entries summed into the 9 neighbour-cell slots of its own cell
+// (every neighbour lies in the 3x3 cells around it); (2) thread per cell, its
+// rows' slot sums added in the cell list's (id-sorted) order
+__global__ void k_mg_rowslots(int64_t n, int ny, const int32_t* __restrict__ pcell, EllOp<double> A,
+                              double* __restrict__ rs) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int ci = pcell[i], cx = ci / ny, cy = ci % ny;
+    double acc[9] = {0, 0, 0, 0, 1.0, 0, 0, 0, 0};  // the unit diagonal
+    const int m = A.cnt[i];
+    const int64_t e0 = ell(i, 0, A.kmax);
+    for (int k = 0; k < m; ++k) {
+        const int64_t e = e0 + (int64_t)k * 32;
+        const int cj = pcell[A.nbr[e]];
+        const int dx = cj / ny - cx, dy = cj % ny - cy;
+        if (dx < -1 || dx > 1 || dy < -1 || dy > 1) continue;  // cannot happen: lists come from the 3x3 cells
+        acc[stencil_slot(dx, dy)] += A.aval[e];
+    }
+#pragma unroll
+    for (int s = 0; s < 9; ++s) rs[s * n + i] = acc[s];
+}
+
+__global__ void k_mg_galerkin0(int nx, int ny, int64_t n, const int32_t* __restrict__ cell_start,
                                const int32_t* __restrict__ cell_count, const int32_t* __restrict__ sorted,
-                               const int32_t* __restrict__ pcell, EllOp<double> A, double* __restrict__ Ac,
-                               double* __restrict__ dinv) {
+                               const double* __restrict__ rs, double* __restrict__ Ac, double* __restrict__ dinv) {
     const int64_t nc = (int64_t)nx * ny;
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= nc) return;
-    const int cx = (int)(c / ny), cy = (int)(c % ny);
     double acc[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     const int q0 = cell_start[c], qn = cell_count[c];
     for (int q = q0; q < q0 + qn; ++q) {
         const int i = sorted[q];
-        acc[4] += 1.0;  // the unit diagonal
-        const int m = A.cnt[i];
-        const int64_t e0 = ell(i, 0, A.kmax);
-        for (int k = 0; k < m; ++k) {
-            const int64_t e = e0 + (int64_t)k * 32;
-            const int cj = pcell[A.nbr[e]];
-            const int dx = cj / ny - cx, dy = cj % ny - cy;
-            if (dx < -1 || dx > 1 || dy < -1 || dy > 1) continue;  // cannot happen: lists come from the 3x3 cells
-            acc[stencil_slot(dx, dy)] += A.aval[e];
-        }
+#pragma unroll
+        for (int s = 0; s < 9; ++s) acc[s] += rs[s * n + i];
     }
 #pragma unroll
     for (int s = 0; s < 9; ++s) Ac[s * nc + c] = acc[s];
@@ -603,6 +614,7 @@ int mg_alloc(Ctx* c) {
         L.y = vec + 2 * stride;
         L.t = vec + 3 * stride;
     }
+    if ((rc = mg_dalloc(c, &mg.rowslots, 9 * n))) return rc;  // the level-1 Galerkin pass
     const int64_t nco = mg.L[nlev].nc;
     if ((rc = mg_dalloc(c, &mg.cinv, nco * nco))) return rc;
     unsigned char* fine = nullptr;
@@ -644,8 +656,11 @@ int mg_setup(Ctx* c) {
     Mg& mg = c->mg;
     const EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, 0};
     MgLevel& L1 = mg.L[1];
-    k_mg_galerkin0<<<blocks_for(L1.nc, 128), 128, 0, c->stream>>>(L1.nx, L1.ny, c->cell_start, c->cell_count,
-                                                                   c->sorted, c->pcell, A, L1.A, L1.dinv);
+    k_mg_rowslots<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, L1.ny, c->pcell, A, mg.rowslots);
+    BSC_LAUNCH(c);
+    k_mg_galerkin0<<<blocks_for(L1.nc, 128), 128, 0, c->stream>>>(L1.nx, L1.ny, c->n, c->cell_start,
+                                                                   c->cell_count, c->sorted, mg.rowslots, L1.A,
+                                                                   L1.dinv);
     BSC_LAUNCH(c);
     for (int l = 1; l < mg.nlev; ++l) {
         const MgLevel &F = mg.L[l], &C = mg.L[l + 1];
