@@ -149,8 +149,11 @@ class Context:
         ny, nx = g.shape
         self._call("upload_porosity", nx, ny, origin[0], origin[1], step[0], step[1], _dp(g))
 
-    def download_state(self) -> Dict[str, np.ndarray]:
-        out = empty_state(self.n)
+    def download_state(self, out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
+        """The state in id order; into `out` (arrays shaped as empty_state's,
+        e.g. in pinned host memory) when given, else into new arrays."""
+        if out is None:
+            out = empty_state(self.n)
         v = state_view(out)
         self._call("download_state", ctypes.byref(v))
         out["L"] = out["L"].reshape(self.n, 4)

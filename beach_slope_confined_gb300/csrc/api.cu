@@ -510,7 +510,7 @@ int bsc_upload_solids(bsc_ctx* c, int64_t ns, const double* x, const double* y, 
     if (ns == 0) return BSC_OK;
     int rc;
     if ((rc = palloc(c, &c->sx, ns)) || (rc = palloc(c, &c->sy, ns)) || (rc = palloc(c, &c->svol, ns)) ||
-        (rc = palloc(c, &c->spor, ns)) || (rc = palloc(c, &c->sposf, ns)))
+        (rc = palloc(c, &c->spor, ns)) || (rc = palloc(c, &c->sposf, ns)) || (rc = palloc(c, &c->swf, ns)))
         return rc;
     std::vector<double> vol(ns), sp(ns);
     const KParams& K = c->K;

@@ -175,6 +175,7 @@ struct Ctx {
     // pre-test of the pair searches); fluid/wall particles and solids
     float2* posf = nullptr;
     float2* sposf = nullptr;
+    float* swf = nullptr;         // solids' (1 - n_s) V_s in FP32 (the mixed path's porosity sum)
     // solids: their own cell list, static after upload
     double *sx = nullptr, *sy = nullptr, *svol = nullptr, *spor = nullptr;
     int32_t *scell_start = nullptr, *scell_count = nullptr;

@@ -234,12 +234,15 @@ int solids_build(Ctx* c) {
     for (int q = 1; q < c->ncell; ++q) start[q] = start[q - 1] + count[q - 1];
     std::vector<double> sx2(ns), sy2(ns), sv2(ns), sp2(ns);
     std::vector<float2> so(ns);
+    std::vector<float> sw(ns);
     for (int64_t k = 0; k < ns; ++k) {
         sx2[k] = hx[ord[k]]; sy2[k] = hy[ord[k]]; sv2[k] = hv[ord[k]]; sp2[k] = hp[ord[k]];
+        sw[k] = (float)((1.0 - sp2[k]) * sv2[k]);
         const int cxk = key[ord[k]] / K.ny, cyk = key[ord[k]] % K.ny;
         so[k] = make_float2((float)(sx2[k] - (K.gx0 + cxk * K.cs)), (float)(sy2[k] - (K.gy0 + cyk * K.cs)));
     }
     BSC_H2D(c, c->sposf, so.data(), sizeof(float2) * ns);
+    BSC_H2D(c, c->swf, sw.data(), sizeof(float) * ns);
     BSC_H2D(c, c->sx, sx2.data(), sizeof(double) * ns);
     BSC_H2D(c, c->sy, sy2.data(), sizeof(double) * ns);
     BSC_H2D(c, c->svol, sv2.data(), sizeof(double) * ns);

@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
                                                       const int32_t* __restrict__ scs, const int32_t* __restrict__ scc,
                                                       const double* __restrict__ sx, const double* __restrict__ sy,
                                                       const float2* __restrict__ sposf,
+                                                      const float* __restrict__ swf,
                                                       const double* __restrict__ svol,
                                                       const double* __restrict__ spor) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -231,7 +232,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
     if (S.tid[i] != BSC_TID_FLUID) return;
     const double xi = S.x[i], yi = S.y[i];
     const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
-    const float H2f = (float)(K.H2 * (1.0 + PRE_MARGIN));
+    const float H2f = (float)(K.H2 * (1.0 + PRE_MARGIN)), H2f0 = (float)K.H2;
     const float csf = (float)K.cs;
     const float2 pi = make_float2((float)(xi - (K.gx0 + cx * K.cs)), (float)(yi - (K.gy0 + cy * K.cs)));
     const bool pre_i = pre_ok(pi, csf);
@@ -248,7 +249,15 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
                 const float2 ps = sposf[s];
                 if (pre_i && pre_ok(ps, csf)) {
                     const float fdx = pi.x - (ps.x + shx), fdy = pi.y - (ps.y + shy);
-                    if (fdx * fdx + fdy * fdy > H2f) continue;
+                    const float r2f = fdx * fdx + fdy * fdy;
+                    if constexpr (sizeof(R) == 4) {
+                        // FP32 sum: W is continuous and vanishes at r = 2h, so
+                        // the FP32 distance decides nothing that matters and
+                        // the whole pair stays in FP32 (weight (1-n_s) V_s)
+                        if (r2f < H2f0) frac += swf[s] * kern_w<float>(K, sqrtf(r2f));
+                        continue;
+                    }
+                    if (r2f > H2f) continue;
                 }
                 const double dx = xi - sx[s], dy = yi - sy[s];
                 const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
@@ -281,10 +290,10 @@ int op_effpor(Ctx* c) {
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
         k_effpor<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
-                                                       c->sx, c->sy, c->sposf, c->svol, c->spor);
+                                                       c->sx, c->sy, c->sposf, c->swf, c->svol, c->spor);
     else
         k_effpor<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
-                                                        c->sx, c->sy, c->sposf, c->svol, c->spor);
+                                                        c->sx, c->sy, c->sposf, c->swf, c->svol, c->spor);
     BSC_LAUNCH(c);
     return BSC_OK;
 }

@@ -27,8 +27,10 @@ def main(argv=None):
     args = ap.parse_args(argv)
     spec = sc.config_spec(args.config)
     scen = sc.build(spec)
+    # the inner-solve settings of bench.py for each preconditioner
+    mg = args.precond == "mg"
     P = sc.make_params(spec, scen.bounds, precision=args.precision, tol=1e-8, maxit=args.maxit,
-                       inner_tol=0.1, max_outer=4, precond=args.precond, restart=40)
+                       inner_tol=1e-5 if mg else 0.1, max_outer=40 if mg else 4, precond=args.precond, restart=40)
     g = Solver(P)
     setup_tank(g, scen)
     for _ in range(args.steps):

@@ -4,11 +4,13 @@
 
 Workload: the 4.0 m x 0.6 m tank at dx = 1.2 mm (833,250 fluid particles plus
 walls; per-cell porosity 0.4 +/- 0.05 in the slope), Wendland C2 with
-h = 1.3 dx, BiCGSTAB PPE to relative residual 1e-8, fixed dt = 1e-4 s.  A step
-is the whole main.f90:41-65 sequence (two neighbour searches, porosity,
-eddy viscosity, predictor, PPE assembly + solve, projection, shifting).
-The headline `value` is the mixed-precision path (FP32 pair sums and inner
-Krylov sweeps, FP64 refinement); the plain FP64 path is reported beside it.
+h = 1.3 dx, PPE to relative residual 1e-8 (by default FGMRES preconditioned by
+the cell-multigrid V-cycle; `--precond none` runs the reference's
+unpreconditioned BiCGSTAB), fixed dt = 1e-4 s.  A step is the whole
+main.f90:41-65 sequence (two neighbour searches, porosity, eddy viscosity,
+predictor, PPE assembly + solve, projection, shifting).  The headline `value`
+is the mixed-precision path (FP32 pair sums, FP32 inner FGMRES and V-cycle,
+FP64 assembly and refinement); the plain FP64 path is reported beside it.
 
 `--impl reference` times the reference algorithm on the host cores instead:
 the C++ OpenMP restatement of the Fortran routines (the Fortran itself needs
@@ -163,11 +165,44 @@ def spmv_bytes(nnz: int, n: int, fp32: bool) -> int:
     return 12 * nnz + 28 * n
 
 
-def spmv_z_bytes(nnz: int, n: int, z_bytes: int) -> int:
-    """Algorithmic bytes of one k_spmv_z launch (w = A z, the FP64 operator
-    applied to a preconditioned vector of z_bytes per element): per stored
-    entry the FP64 value and the column; per row the count, z_i and w_i."""
-    return 12 * nnz + (4 + z_bytes + 8) * n
+def spmv_mg_bytes(nnz: int, n: int, fp32: bool) -> int:
+    """Algorithmic bytes of the SpMV w = A z of one multigrid-preconditioned
+    FGMRES iteration: k_spmv_f (FP32 operator and vectors, the mixed path's
+    inner solve) or k_spmv_z<double> (FP64).  Per stored entry the value and
+    the column; per row the count, z_i and w_i.  Neighbour values z_j come
+    from cache."""
+    if fp32:
+        return 8 * nnz + 12 * n
+    return 12 * nnz + 20 * n
+
+
+PINNED = False
+
+
+def pinned_like(a: np.ndarray) -> np.ndarray:
+    """A copy of `a` in page-locked host memory (torch's pinned allocator),
+    so host<->device copies run at the interconnect's DMA rate."""
+    global PINNED
+    try:
+        import torch
+
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)), pin_memory=True)
+        out = t.numpy()
+        out[...] = a
+        PINNED = True
+        return out
+    except Exception:  # no CUDA-capable torch: pageable copies
+        return np.array(a, copy=True)
+
+
+def fp64_bound_kernels():
+    """The pair kernels whose time is set by the FP64 pipe (not HBM), from the
+    committed ncu summary: name, FP64-pipe utilisation, DRAM throughput."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "fp64_bound_kernels.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return None
 
 
 def traffic_per_row(kind: str):
@@ -218,10 +253,12 @@ def run_ours(args, dist: Dist):
                              solve_ms=t.ms[T_PPE_SOLVE] / args.steps, launches=int(t.kernel_launches),
                              clocks=clk.summary(), n=scen.n)
         states[prec] = g.download_state()
-        # e2e through the C ABI with host buffers: upload, step, download
+        # e2e through the C ABI with host buffers in pinned memory: every
+        # step uploads the state, steps, and downloads the state
         if prec == "mixed":
             host = g.download_state()
-            up = {k: np.ascontiguousarray(v.reshape(-1)) for k, v in host.items()}
+            up = {k: pinned_like(v.reshape(-1)) for k, v in host.items()}
+            out = {k: pinned_like(v) for k, v in host.items()}
             h2d = sum(a.nbytes for a in up.values())
             g.upload_state(up)
             g.step(1)
@@ -232,12 +269,13 @@ def run_ours(args, dist: Dist):
             for _ in range(ke):
                 g.upload_state(up)
                 g.step(1)
-                out = g.download_state()
+                g.download_state(out)
             e2e_s = time.perf_counter() - t0
             d2h = sum(np.asarray(a).nbytes for a in out.values())
             ev, _ = aggregate(e2e_s, nf * ke, dist)
             results[prec]["e2e"] = dict(value=ev, unit="particle-steps/s", h2d_bytes_per_step=int(h2d),
-                                        d2h_bytes_per_step=int(d2h), steps=ke)
+                                        d2h_bytes_per_step=int(d2h), steps=ke,
+                                        host_memory="pinned" if PINNED else "pageable")
         g.close()
     errs = None
     if "fp64" in states:
@@ -366,9 +404,9 @@ def main():
     hbm, peak_kind = measured_peak_hbm()
     mg = args.precond == "mg"
     if mg:
-        byts = spmv_z_bytes(m["nnz"], m["n"], 4)
-        kname = "k_spmv_z<float> (FP64 ELL SpMV of the FP32 preconditioned vector)"
-        tpr = traffic_per_row("spmv_z_fp32")
+        byts = spmv_mg_bytes(m["nnz"], m["n"], fp32=True)
+        kname = "k_spmv_f (FP32 ELL SpMV of the inner FGMRES)"
+        tpr = traffic_per_row("spmv_f_fp32")
     else:
         byts = spmv_bytes(m["nnz"], m["n"], fp32=True)
         kname = "k_bicg_1<EllOp<float>,float> (FP32 ELL SpMV + dot)"
@@ -383,7 +421,7 @@ def main():
     fp64 = None
     if "fp64" in res:
         f = res["fp64"]
-        b64 = spmv_z_bytes(f["nnz"], f["n"], 8) if mg else spmv_bytes(f["nnz"], f["n"], fp32=False)
+        b64 = spmv_mg_bytes(f["nnz"], f["n"], fp32=False) if mg else spmv_bytes(f["nnz"], f["n"], fp32=False)
         a64 = b64 / (f["spmv_ms"] * 1e-3) / 1e9 if f["spmv_ms"] > 0 else None
         t64 = traffic_per_row("spmv_z_fp64" if mg else "fp64")
         fp64 = {"value": f["value"], "ms_per_step": f["ms_per_step"], "ppe_iterations": [i[0] for i in f["iters"]],
@@ -427,6 +465,7 @@ def main():
         "clocks": m["clocks"],
         "gpu_launches": m["launches"],
         "measured_peaks": {"fp64_gflops": peaks[0], "fp32_gflops": peaks[1], "copy_gbs": peaks[2]} if peaks else None,
+        "fp64_bound_kernels": fp64_bound_kernels(),
         "wcsph_adjoint_forward_ratio": None,
     }
     print(json.dumps(line), flush=True)

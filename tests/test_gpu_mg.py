@@ -84,7 +84,9 @@ def test_mg_deterministic():
 
 def test_mg_reorder_keeps_results():
     """A Morton reorder at every cell shift (which swaps the cell-map buffers
-    under the cached per-iteration graphs) gives the same physics as every 20."""
+    under the cached per-iteration graphs) gives the same physics as every 20:
+    to 1e-8 in FP64; to 1e-6 on the mixed path, whose FP32 pair sums change
+    their order with the particles' (a stale cell map would be far off)."""
     spec = small_spec()
     scen = sc.build(spec)
     for prec in ("fp64", "mixed"):
@@ -97,5 +99,6 @@ def test_mg_reorder_keeps_results():
             g.step(4)
             out.append(g.download_state())
             g.close()
+        tol = 1e-8 if prec == "fp64" else 1e-6
         for f in ("x", "y", "vx", "vy", "p"):
-            assert rel_l2(out[0][f], out[1][f]) < 1e-8, (prec, f)
+            assert rel_l2(out[0][f], out[1][f]) < tol, (prec, f)
