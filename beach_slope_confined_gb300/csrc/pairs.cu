@@ -653,10 +653,11 @@ int op_opt2_shift(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "opt2_shift before neighbour");
     int8_t* mark = (int8_t*)c->pslot;  // scratch: pslot is free between cell builds
     const unsigned g = blocks_for(c->n, NB_BLOCK);
-    if (c->mixed)
-        k_shift<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, mark);
-    else
-        k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, mark);
+    // FP64 on both paths: the shift adds grad(v).delta to the velocity, a
+    // gradient sum that cancels heavily; in FP32 it moved the mixed path's
+    // velocities by ~7e-6 (relative) from the FP64 path's after 8 steps of
+    // the c3 tank, in FP64 by ~1e-6, for 0.3 ms a step
+    k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, mark);
     BSC_LAUNCH(c);
     k_shift_apply<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, mark);
     BSC_LAUNCH(c);

@@ -62,7 +62,7 @@ def test_mg_mixed_against_fp64():
     print("mixed vs fp64 relative L2 (multigrid):", errs)
     assert errs["x"] < 1e-9 and errs["y"] < 1e-9
     assert errs["porosity"] < 1e-6
-    assert errs["p"] < 1e-4 and errs["vx"] < 1e-3 and errs["vy"] < 1e-3
+    assert errs["p"] < 1e-6 and errs["vx"] < 1e-5 and errs["vy"] < 1e-5
 
 
 def test_mg_deterministic():
