@@ -108,45 +108,81 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
     const float2 pi = posf[i];
     const bool pre_i = pre_ok(pi, csf);
     R m0 = 0, m1 = 0, m2 = 0, m3 = 0;
-    int count = 0;
-    for (int ax = cx - 1; ax <= cx + 1; ++ax) {
-        if (ax < 0 || ax >= K.nx) continue;
-        const float shx = (float)(ax - cx) * csf;
-        for (int ay = cy - 1; ay <= cy + 1; ++ay) {
-            if (ay < 0 || ay >= K.ny) continue;
-            const float shy = (float)(ay - cy) * csf;
-            const int cc = ax * K.ny + ay;
-            const int s0 = cstart[cc], s1 = s0 + ccount[cc];
-            for (int s = s0; s < s1; ++s) {
-                const int j = sorted[s];
-                if (j == (int)i) continue;  // (tid,matid) self test, search.f90:53-55
-                const float2 pj = posf[j];
-                if (pre_i && pre_ok(pj, csf)) {
-                    const float fdx = pi.x - (pj.x + shx), fdy = pi.y - (pj.y + shy);
-                    if (fdx * fdx + fdy * fdy > H2f) continue;
+    int count = 0, nc = 0;
+    // the FP64 work of one candidate: the exact test, grad W, the list entry
+    // and the M sum
+    auto pair = [&](int j) {
+        const double dx = xi - S.x[j], dy = yi - S.y[j];
+        const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        if (!(d2 < K.H2x)) return;  // exactly sqrt(d2) < 2h, no FMA contraction
+        const double r = __dsqrt_rn(d2);
+        // grad W per pair in FP64 (stored in FP64, and in FP32 for the FP32
+        // pair sums of the mixed path); the M sum runs in R
+        const double F = grad_factor<double>(K, r);
+        const double gx64 = F * dx, gy64 = F * dy;
+        const R gx = (R)gx64, gy = (R)gy64;
+        if (count < K.kmax) {
+            const int64_t e = ell(i, count, K.kmax);
+            nbr[e] = j;
+            gw[e] = {gx64, gy64};
+            if (gwf) gwf[e] = {(float)gx64, (float)gy64};
+        }
+        ++count;
+        const R vj = (R)S.vol[j];
+        const R rx = -vj * (R)dx, ry = -vj * (R)dy;  // m_j (x_j - x_i) / rho_j
+        m0 += gx * rx;
+        m1 += gy * rx;
+        m2 += gx * ry;
+        m3 += gy * ry;
+    };
+    if (pre_i) {
+        // Two phases, so the FP64 work runs on full warps: (1) the FP32
+        // pre-test compacts the surviving candidates, in cell-list order,
+        // into this row's list slots; (2) the FP64 pair work walks them.  A
+        // warp's lanes would otherwise take their FP64 branches at different
+        // candidates, and the FP64 pipe (2 lanes a clock per SM here) would
+        // run mostly idle lanes.  The pre-test margin lets through only
+        // candidates within 1e-5 of the support, so phase 2 rejects almost
+        // none.  A row whose survivors exceed the list capacity takes the
+        // one-pass loop below, which counts the true neighbours.
+        for (int ax = cx - 1; ax <= cx + 1; ++ax) {
+            if (ax < 0 || ax >= K.nx) continue;
+            const float shx = (float)(ax - cx) * csf;
+            for (int ay = cy - 1; ay <= cy + 1; ++ay) {
+                if (ay < 0 || ay >= K.ny) continue;
+                const float shy = (float)(ay - cy) * csf;
+                const int cc = ax * K.ny + ay;
+                const int s0 = cstart[cc], s1 = s0 + ccount[cc];
+                for (int s = s0; s < s1; ++s) {
+                    const int j = sorted[s];
+                    if (j == (int)i) continue;  // (tid,matid) self test, search.f90:53-55
+                    const float2 pj = posf[j];
+                    if (pre_ok(pj, csf)) {
+                        const float fdx = pi.x - (pj.x + shx), fdy = pi.y - (pj.y + shy);
+                        if (fdx * fdx + fdy * fdy > H2f) continue;
+                    }
+                    if (nc < K.kmax) nbr[ell(i, nc, K.kmax)] = j;
+                    ++nc;
                 }
-                const double dx = xi - S.x[j], dy = yi - S.y[j];
-                const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-                if (!(d2 < K.H2x)) continue;  // exactly sqrt(d2) < 2h, no FMA contraction
-                const double r = __dsqrt_rn(d2);
-                // grad W per pair in FP64 (stored in FP64, and in FP32 for the
-                // FP32 pair sums of the mixed path); the M sum runs in R
-                const double F = grad_factor<double>(K, r);
-                const double gx64 = F * dx, gy64 = F * dy;
-                const R gx = (R)gx64, gy = (R)gy64;
-                if (count < K.kmax) {
-                    const int64_t e = ell(i, count, K.kmax);
-                    nbr[e] = j;
-                    gw[e] = {gx64, gy64};
-                    if (gwf) gwf[e] = {(float)gx64, (float)gy64};
+            }
+        }
+        // slot `count` <= k is written only after slot k is read
+        if (nc <= K.kmax)
+            for (int k = 0; k < nc; ++k) pair(nbr[ell(i, k, K.kmax)]);
+    }
+    if (!pre_i || nc > K.kmax) {
+        // far from its binned cell (no pre-test), or too many survivors: one
+        // pass over the 3x3 cells
+        for (int ax = cx - 1; ax <= cx + 1; ++ax) {
+            if (ax < 0 || ax >= K.nx) continue;
+            for (int ay = cy - 1; ay <= cy + 1; ++ay) {
+                if (ay < 0 || ay >= K.ny) continue;
+                const int cc = ax * K.ny + ay;
+                const int s0 = cstart[cc], s1 = s0 + ccount[cc];
+                for (int s = s0; s < s1; ++s) {
+                    const int j = sorted[s];
+                    if (j != (int)i) pair(j);
                 }
-                ++count;
-                const R vj = (R)S.vol[j];
-                const R rx = -vj * (R)dx, ry = -vj * (R)dy;  // m_j (x_j - x_i) / rho_j
-                m0 += gx * rx;
-                m1 += gy * rx;
-                m2 += gx * ry;
-                m3 += gy * ry;
             }
         }
     }
