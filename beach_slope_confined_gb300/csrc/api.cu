@@ -160,7 +160,7 @@ static int alloc_for(Ctx* c, int64_t n) {
     int rc;
     if ((rc = alloc_state(c, c->S, n)) || (rc = alloc_state(c, c->S2, n))) return rc;
     if ((rc = dalloc(c, &c->pcell, n)) || (rc = dalloc(c, &c->pslot, n)) || (rc = dalloc(c, &c->sorted, n))) return rc;
-    if ((rc = dalloc(c, &c->posf, n))) return rc;
+    if ((rc = dalloc(c, &c->posf, n)) || (rc = dalloc(c, &c->lstage, 4 * n))) return rc;
     const int64_t slots = ((n + 31) / 32) * 32 * (int64_t)c->K.kmax;
     if ((rc = dalloc(c, &c->nbr, slots)) || (rc = dalloc(c, &c->cnt, n))) return rc;
     // FP64 grad W and PPE values in both precisions; the mixed path adds FP32
@@ -239,6 +239,25 @@ __global__ void k_to_id_order(int64_t n, const double* __restrict__ src, double*
                               const int32_t* __restrict__ id) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (k < n) dst[id[k]] = src[k];
+}
+
+// L of the state view is n x 4 interleaved; the device keeps four arrays
+__global__ void k_split_L(int64_t n, const double* __restrict__ L4, State S) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double4 l = reinterpret_cast<const double4*>(L4)[i];
+    S.L0[i] = l.x; S.L1[i] = l.y; S.L2[i] = l.z; S.L3[i] = l.w;
+}
+
+__global__ void k_join_L_to_id_order(int64_t n, State S, double* __restrict__ L4) {
+    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    reinterpret_cast<double4*>(L4)[S.id[k]] = make_double4(S.L0[k], S.L1[k], S.L2[k], S.L3[k]);
+}
+
+__global__ void k_fill(int64_t n, double* __restrict__ d, double v) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i < n) d[i] = v;
 }
 
 __global__ void k_to_id_order_u8(int64_t n, const uint8_t* __restrict__ src, uint8_t* __restrict__ dst,
@@ -452,8 +471,8 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
         } else if (dflt == 0.0) {
             BSC_CUDA(c, cudaMemsetAsync(d, 0, sizeof(double) * n, c->stream));
         } else {
-            std::vector<double> tmp(n, dflt);
-            BSC_H2D(c, d, tmp.data(), sizeof(double) * n);
+            k_fill<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, d, dflt);
+            BSC_LAUNCH(c);
         }
         return BSC_OK;
     };
@@ -466,12 +485,9 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
         (rc = up(S.xrest, s->xrest ? s->xrest : s->x, 0)))
         return rc;
     if (s->L) {
-        std::vector<double> l[4];
-        for (int q = 0; q < 4; ++q) l[q].resize(n);
-        for (int64_t i = 0; i < n; ++i)
-            for (int q = 0; q < 4; ++q) l[q][i] = s->L[4 * i + q];
-        double* d[4] = {S.L0, S.L1, S.L2, S.L3};
-        for (int q = 0; q < 4; ++q) BSC_H2D(c, d[q], l[q].data(), sizeof(double) * n);
+        BSC_CUDA(c, cudaMemcpyAsync(c->lstage, s->L, 4 * sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+        k_split_L<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, c->lstage, S);
+        BSC_LAUNCH(c);
     } else {
         if ((rc = up(S.L0, nullptr, 1.0)) || (rc = up(S.L1, nullptr, 0)) || (rc = up(S.L2, nullptr, 0)) ||
             (rc = up(S.L3, nullptr, 1.0)))
@@ -541,46 +557,42 @@ int bsc_download_state(bsc_ctx* c, bsc_state_view* s) {
     if (!s || s->n != c->n) return set_err(c, BSC_E_INVALID, "download_state: size mismatch");
     StageTimer tm(c, BSC_T_DOWNLOAD);
     const int64_t n = c->n;
-    State& S = c->S;
-    double* stage = c->S2.x;  // S2 is free outside a reorder
+    const State& S = c->S;
+    const State& T = c->S2;  // free outside a reorder: per-field staging in id order
     const unsigned g = blocks_for(n, 256);
-    auto dn = [&](const double* src, double* host) -> int {
+    // every gather and copy is queued on the stream; one wait at the end
+    auto dn = [&](const double* src, double* stage, double* host) -> int {
         if (!host) return BSC_OK;
         k_to_id_order<<<g, 256, 0, c->stream>>>(n, src, stage, S.id);
         BSC_LAUNCH(c);
         BSC_CUDA(c, cudaMemcpyAsync(host, stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
-        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+        return BSC_OK;
+    };
+    auto dn8 = [&](const uint8_t* src, uint8_t* stage, uint8_t* host) -> int {
+        if (!host) return BSC_OK;
+        k_to_id_order_u8<<<g, 256, 0, c->stream>>>(n, src, stage, S.id);
+        BSC_LAUNCH(c);
+        BSC_CUDA(c, cudaMemcpyAsync(host, stage, n, cudaMemcpyDeviceToHost, c->stream));
         return BSC_OK;
     };
     int rc;
-    if ((rc = dn(S.x, s->x)) || (rc = dn(S.y, s->y)) || (rc = dn(S.vx, s->vx)) || (rc = dn(S.vy, s->vy)) ||
-        (rc = dn(S.xs, s->xs)) || (rc = dn(S.ys, s->ys)) || (rc = dn(S.vxs, s->vxs)) || (rc = dn(S.vys, s->vys)) ||
-        (rc = dn(S.p, s->p)) || (rc = dn(S.rho, s->rho)) || (rc = dn(S.oden, s->oden)) ||
-        (rc = dn(S.mass, s->mass)) || (rc = dn(S.por, s->porosity)) || (rc = dn(S.gradvx, s->gradvx)) ||
-        (rc = dn(S.nut, s->nut)) || (rc = dn(S.tke, s->tke)) || (rc = dn(S.resist, s->resist)) ||
-        (rc = dn(S.varts, s->varts)) || (rc = dn(S.vel, s->vel)) || (rc = dn(S.xrest, s->xrest)))
+    if ((rc = dn(S.x, T.x, s->x)) || (rc = dn(S.y, T.y, s->y)) || (rc = dn(S.vx, T.vx, s->vx)) ||
+        (rc = dn(S.vy, T.vy, s->vy)) || (rc = dn(S.xs, T.xs, s->xs)) || (rc = dn(S.ys, T.ys, s->ys)) ||
+        (rc = dn(S.vxs, T.vxs, s->vxs)) || (rc = dn(S.vys, T.vys, s->vys)) || (rc = dn(S.p, T.p, s->p)) ||
+        (rc = dn(S.rho, T.rho, s->rho)) || (rc = dn(S.oden, T.oden, s->oden)) || (rc = dn(S.mass, T.mass, s->mass)) ||
+        (rc = dn(S.por, T.por, s->porosity)) || (rc = dn(S.gradvx, T.gradvx, s->gradvx)) ||
+        (rc = dn(S.nut, T.nut, s->nut)) || (rc = dn(S.tke, T.tke, s->tke)) ||
+        (rc = dn(S.resist, T.resist, s->resist)) || (rc = dn(S.varts, T.varts, s->varts)) ||
+        (rc = dn(S.vel, T.vel, s->vel)) || (rc = dn(S.xrest, T.xrest, s->xrest)))
         return rc;
     if (s->L) {
-        std::vector<double> l(n);
-        double* d[4] = {S.L0, S.L1, S.L2, S.L3};
-        for (int q = 0; q < 4; ++q) {
-            if ((rc = dn(d[q], l.data()))) return rc;
-            for (int64_t i = 0; i < n; ++i) s->L[4 * i + q] = l[i];
-        }
-    }
-    uint8_t* st8 = (uint8_t*)c->S2.y;
-    if (s->tid) {
-        k_to_id_order_u8<<<g, 256, 0, c->stream>>>(n, (const uint8_t*)S.tid, st8, S.id);
+        k_join_L_to_id_order<<<g, 256, 0, c->stream>>>(n, S, c->lstage);
         BSC_LAUNCH(c);
-        BSC_CUDA(c, cudaMemcpyAsync(s->tid, st8, n, cudaMemcpyDeviceToHost, c->stream));
-        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
+        BSC_CUDA(c, cudaMemcpyAsync(s->L, c->lstage, 4 * sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
     }
-    if (s->flags) {
-        k_to_id_order_u8<<<g, 256, 0, c->stream>>>(n, S.flags, st8, S.id);
-        BSC_LAUNCH(c);
-        BSC_CUDA(c, cudaMemcpyAsync(s->flags, st8, n, cudaMemcpyDeviceToHost, c->stream));
-        BSC_CUDA(c, cudaStreamSynchronize(c->stream));
-    }
+    if ((rc = dn8((const uint8_t*)S.tid, (uint8_t*)T.tid, (uint8_t*)s->tid)) || (rc = dn8(S.flags, T.flags, s->flags)))
+        return rc;
+    BSC_CUDA(c, cudaStreamSynchronize(c->stream));
     return BSC_OK;
 }
 

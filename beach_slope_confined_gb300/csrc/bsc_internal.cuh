@@ -174,6 +174,7 @@ struct Ctx {
     // positions as float offsets from the origin of their own cell (the FP32
     // pre-test of the pair searches); fluid/wall particles and solids
     float2* posf = nullptr;
+    double* lstage = nullptr;  // 4n: the interleaved L of the host state view, on the device
     float2* sposf = nullptr;
     float* swf = nullptr;         // solids' (1 - n_s) V_s in FP32 (the mixed path's porosity sum)
     // solids: their own cell list, static after upload
