@@ -111,6 +111,7 @@ static void free_all(Ctx* c) {
     if (c->h_sc) cudaFreeHost(c->h_sc);
     if (c->h_flag) cudaFreeHost(c->h_flag);
     c->h_sc = nullptr;
+    c->h_it = nullptr;
     c->h_flag = nullptr;
     c->cap = 0;
 }
@@ -150,8 +151,9 @@ static int alloc_solver_work(Ctx* c, int64_t n, bool fp64, bool fp32) {
     if ((rc = dalloc(c, &c->sc, 1)) || (rc = dalloc(c, &c->sc2, 1))) return rc;
     if ((rc = dalloc(c, &c->ticket, 1))) return rc;
     BSC_CUDA(c, cudaMemsetAsync(c->ticket, 0, sizeof(unsigned), c->stream));
-    if (!c->h_sc) BSC_CUDA(c, cudaMallocHost((void**)&c->h_sc, 2 * sizeof(Scalars)));
-    std::memset(c->h_sc, 0, 2 * sizeof(Scalars));
+    if (!c->h_sc) BSC_CUDA(c, cudaMallocHost((void**)&c->h_sc, 4 * sizeof(Scalars)));
+    std::memset(c->h_sc, 0, 4 * sizeof(Scalars));
+    c->h_it = c->h_sc + 2;
     return BSC_OK;
 }
 
@@ -406,14 +408,14 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
         return BSC_E_CUDA;
     }
     for (int k = 0; k < 2 * Ctx::EVPOOL; ++k) cudaEventCreate(&c->evs[k]);
-    cudaEventCreate(&c->ev_spmv[0]);
-    cudaEventCreate(&c->ev_spmv[1]);
+    for (int k = 0; k < 6; ++k) cudaEventCreate(&c->ev_spmv[k]);
     if (const char* e = std::getenv("BSC_GRAPHS")) c->use_graphs = e[0] != '0';
     if (const char* e = std::getenv("BSC_DEBUG")) c->debug = e[0] == '1';
     if (const char* e = std::getenv("BSC_SPMV_UNROLL")) c->spmv_unroll = e[0] == '1';
     if (const char* e = std::getenv("BSC_PROFILE_ITER")) c->prof_iter = e[0] == '1';
     if (const char* e = std::getenv("BSC_MG_TAIL")) c->mg_tail_cells = std::atoi(e);
     for (int k = 0; k < 6; ++k) cudaEventCreate(&c->ev_it[k]);
+    for (int k = 0; k < 2; ++k) cudaEventCreateWithFlags(&c->ev_lag[k], cudaEventDisableTiming);
     *out = c;
     return BSC_OK;
 }
@@ -426,8 +428,10 @@ int bsc_destroy(bsc_ctx* c) {
     c->pallocs.clear();
     for (int k = 0; k < 2 * Ctx::EVPOOL; ++k)
         if (c->evs[k]) cudaEventDestroy(c->evs[k]);
-    for (int k = 0; k < 2; ++k)
+    for (int k = 0; k < 6; ++k)
         if (c->ev_spmv[k]) cudaEventDestroy(c->ev_spmv[k]);
+    for (int k = 0; k < 2; ++k)
+        if (c->ev_lag[k]) cudaEventDestroy(c->ev_lag[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return BSC_OK;

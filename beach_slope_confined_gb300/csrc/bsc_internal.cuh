@@ -55,6 +55,11 @@ struct Scalars {
     int32_t done, breakdown, it, k5;  // k5: work of the last kernel of a BiCGSTAB iteration
 };
 
+// an FGMRES cycle has stopped (converged, broken down or at its restart
+// length): the kernels of iterations queued past that point return at once
+__device__ __forceinline__ bool fg_skip(const Scalars* sc) { return sc->done || sc->tmp[2] != 0.0; }
+__device__ __forceinline__ bool mg_skip(const Scalars* sk) { return sk && fg_skip(sk); }
+
 // ---- kernel constants --------------------------------------------------------
 struct KParams {
     int kernel;
@@ -145,6 +150,7 @@ struct Mg {
     double* Z = nullptr;           // preconditioned vectors m x n (FP64 path)
     float *Vf = nullptr, *Zf = nullptr;  // the same in FP32 (mixed path's inner solve)
     float *wf = nullptr, *rf = nullptr;  // FP32 work vectors
+    const Scalars* skip = nullptr;  // the calling FGMRES's scalars: V-cycles queued past its stop return at once
     std::vector<void*> allocs;
 };
 
@@ -230,6 +236,8 @@ struct Ctx {
     double* part = nullptr;       // reduction partials RED_GRID x 64
     Scalars* sc = nullptr;
     Scalars* h_sc = nullptr;      // pinned mirror
+    Scalars* h_it = nullptr;      // pinned: scalars after the last two queued FGMRES iterations, by parity
+    cudaEvent_t ev_lag[2] = {};   // end of the last two queued FGMRES iterations, by parity
     int fg_m = 0;
 
     // timing: stage events recorded on the stream, resolved lazily
@@ -240,7 +248,9 @@ struct Ctx {
     double ms[BSC_TIMING_SLOTS] = {0};
     int64_t calls[BSC_TIMING_SLOTS] = {0};
     bool timing = true;
-    cudaEvent_t ev_spmv[2] = {};  // around one SpMV per Krylov batch
+    // around one SpMV per Krylov batch (pair 0); pairs 1 and 2: the SpMV of
+    // the multigrid FGMRES iterations, by iteration parity
+    cudaEvent_t ev_spmv[6] = {};
     double* stepsc = nullptr;     // device: umax, numax (timestep reductions)
     Mg mg;                        // multigrid preconditioner of the PPE (mg.cu)
 };

@@ -258,24 +258,27 @@ template <typename T, int MODE>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg_smooth(int nx, int ny, const T* __restrict__ A,
                                                          const T* __restrict__ dinv, const T* __restrict__ b,
                                                          const T* __restrict__ xin, const T* __restrict__ xc, int nyc,
-                                                         T scale, T w, T* __restrict__ xout) {
+                                                         T scale, T w, T* __restrict__ xout,
+                                                         const Scalars* __restrict__ sk) {
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (c >= (int64_t)nx * ny) return;
+    if (c >= (int64_t)nx * ny || mg_skip(sk)) return;
     xout[c] = smooth_at<T, MODE>(nx, ny, c, A, dinv, b, xin, xc, nyc, scale, w);
 }
 
 // one sweep from a zero guess: x = w D^-1 b
 template <typename T>
-__global__ void k_mg_jacobi0(int64_t nc, const T* __restrict__ dinv, const T* __restrict__ b, T w, T* __restrict__ x) {
+__global__ void k_mg_jacobi0(int64_t nc, const T* __restrict__ dinv, const T* __restrict__ b, T w, T* __restrict__ x,
+                             const Scalars* __restrict__ sk) {
+    if (mg_skip(sk)) return;
     GRID_LOOP(c, nc) x[c] = w * dinv[c] * b[c];
 }
 
 template <typename T>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const T* __restrict__ A,
                                                            const T* __restrict__ b, const T* __restrict__ x, int nxc,
-                                                           int nyc, T* __restrict__ bc) {
+                                                           int nyc, T* __restrict__ bc, const Scalars* __restrict__ sk) {
     const int64_t C = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (C >= (int64_t)nxc * nyc) return;
+    if (C >= (int64_t)nxc * nyc || mg_skip(sk)) return;
     bc[C] = restrict_at<T>(nx, ny, A, b, x, C, nyc);
 }
 
@@ -301,11 +304,13 @@ struct TailArgs {
     int l0, nlev, nu;
     T w, scale;
     const double* cinv;
+    const Scalars* sk;
     TailLevel<T> L[MG_MAX_LEVELS + 1];
 };
 
 template <typename T>
 __global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
+    if (mg_skip(P.sk)) return;
     const int t = threadIdx.x, NT = blockDim.x;
     const T w = P.w, sc = P.scale;
     const int nu = P.nu;
@@ -364,7 +369,8 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
 // two sweeps from a zero guess: x1 = w v; x2 = x1 + w (v - A x1)
 template <typename T, typename VI>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<T> A, const VI* __restrict__ v, T w,
-                                                        T* __restrict__ x) {
+                                                        T* __restrict__ x, const Scalars* __restrict__ sk) {
+    if (mg_skip(sk)) return;
     GRID_LOOP(i, n) {
         const T Av = A.template row<VI, T>(i, v);
         const T vi = (T)v[i];
@@ -373,28 +379,36 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<T> A, co
 }
 
 template <typename T, typename VI>
-__global__ void k_mg0_scale(int64_t n, const VI* __restrict__ v, T w, T* __restrict__ x) {
+__global__ void k_mg0_scale(int64_t n, const VI* __restrict__ v, T w, T* __restrict__ x,
+                            const Scalars* __restrict__ sk) {
+    if (mg_skip(sk)) return;
     GRID_LOOP(i, n) x[i] = w * (T)v[i];
 }
 
 // x_out = x + w (v - A x)
 template <typename T, typename VI, typename O>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<T> A, const VI* __restrict__ v,
-                                                         const T* __restrict__ x, T w, O* __restrict__ xout) {
+                                                         const T* __restrict__ x, T w, O* __restrict__ xout,
+                                                         const Scalars* __restrict__ sk) {
+    if (mg_skip(sk)) return;
     GRID_LOOP(i, n) xout[i] = (O)(x[i] + w * ((T)v[i] - A.template row<T, T>(i, x)));
 }
 
 // r = v - A x
 template <typename T, typename VI>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg0_resid(int64_t n, EllOp<T> A, const VI* __restrict__ v,
-                                                         const T* __restrict__ x, T* __restrict__ r) {
+                                                         const T* __restrict__ x, T* __restrict__ r,
+                                                         const Scalars* __restrict__ sk) {
+    if (mg_skip(sk)) return;
     GRID_LOOP(i, n) r[i] = (T)v[i] - A.template row<T, T>(i, x);
 }
 
 // level-1 right-hand side: the residual summed over each cell's particles
 template <typename T>
 __global__ void k_mg0_restrict(int64_t nc, const int32_t* __restrict__ cell_start, const int32_t* __restrict__ cell_count,
-                               const int32_t* __restrict__ sorted, const T* __restrict__ r, T* __restrict__ b1) {
+                               const int32_t* __restrict__ sorted, const T* __restrict__ r, T* __restrict__ b1,
+                               const Scalars* __restrict__ sk) {
+    if (mg_skip(sk)) return;
     GRID_LOOP(c, nc) {
         const int q0 = cell_start[c], qn = cell_count[c];
         T s = 0;
@@ -409,7 +423,8 @@ template <typename T, typename VI, typename O>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg0_post(int64_t n, EllOp<T> A, const VI* __restrict__ v,
                                                         const T* __restrict__ x, const T* __restrict__ x1,
                                                         const int32_t* __restrict__ pcell, T scale, T w,
-                                                        O* __restrict__ xout) {
+                                                        O* __restrict__ xout, const Scalars* __restrict__ sk) {
+    if (mg_skip(sk)) return;
     GRID_LOOP(i, n) {
         const T yi = x[i] + scale * x1[pcell[i]];
         T Ay = yi;
@@ -467,6 +482,7 @@ int cycle_level(Ctx* c, int l) {
         P.w = w;
         P.scale = sc;
         P.cinv = mg.cinv;
+        P.sk = mg.skip;
         for (int q = l; q <= mg.nlev; ++q) {
             Lv<T> u = level_view<T>(mg.L[q]);
             P.L[q] = TailLevel<T>{mg.L[q].nx, mg.L[q].ny, u.A, u.dinv, u.b, u.x, u.y, u.t};
@@ -479,19 +495,19 @@ int cycle_level(Ctx* c, int l) {
     // more, the first is folded into the second
     T* cur = v.y;
     if (nu == 1)
-        k_mg_jacobi0<T><<<g, MG_BLOCK, 0, c->stream>>>(L.nc, v.dinv, v.b, w, cur);
+        k_mg_jacobi0<T><<<g, MG_BLOCK, 0, c->stream>>>(L.nc, v.dinv, v.b, w, cur, c->mg.skip);
     else
-        k_mg_smooth<T, 1><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, nullptr, nullptr, 0, sc, w, cur);
+        k_mg_smooth<T, 1><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, nullptr, nullptr, 0, sc, w, cur, c->mg.skip);
     BSC_LAUNCH(c);
     for (int k = 2; k < nu; ++k) {
         T* out = cur == v.y ? v.t : v.y;
-        k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w, out);
+        k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w, out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }
     const MgLevel& Lc = mg.L[l + 1];
     Lv<T> vc = level_view<T>(Lc);
-    k_mg_restrict<T><<<blocks_for(Lc.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.b, cur, Lc.nx, Lc.ny, vc.b);
+    k_mg_restrict<T><<<blocks_for(Lc.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.b, cur, Lc.nx, Lc.ny, vc.b, c->mg.skip);
     BSC_LAUNCH(c);
     if (int rc = cycle_level<T>(c, l + 1)) return rc;
     // post-smoothing: the prolongation folded into the first sweep; the last
@@ -499,9 +515,9 @@ int cycle_level(Ctx* c, int l) {
     for (int k = 0; k < nu; ++k) {
         T* out = (k == nu - 1) ? v.x : (cur == v.y ? v.t : v.y);
         if (k == 0)
-            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w, out);
+            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w, out, c->mg.skip);
         else
-            k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w, out);
+            k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w, out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }
@@ -521,21 +537,21 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
     if (c->prof_iter) record_event(c, c->ev_it[0]);
     T* cur = P0;
     if (nu == 1)
-        k_mg0_scale<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, vin, w, cur);
+        k_mg0_scale<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, vin, w, cur, c->mg.skip);
     else
-        k_mg0_pre2<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, cur);
+        k_mg0_pre2<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, cur, c->mg.skip);
     BSC_LAUNCH(c);
     for (int k = 2; k < nu; ++k) {
         T* out = cur == P0 ? Q0 : P0;
-        k_mg0_sweep<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out);
+        k_mg0_sweep<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }
-    k_mg0_resid<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, R0);
+    k_mg0_resid<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, R0, c->mg.skip);
     BSC_LAUNCH(c);
     const MgLevel& L1 = mg.L[1];
     Lv<T> v1 = level_view<T>(L1);
-    k_mg0_restrict<T><<<blocks_for(L1.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L1.nc, c->cell_start, c->cell_count, c->sorted, R0, v1.b);
+    k_mg0_restrict<T><<<blocks_for(L1.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L1.nc, c->cell_start, c->cell_count, c->sorted, R0, v1.b, c->mg.skip);
     BSC_LAUNCH(c);
     if (c->prof_iter) record_event(c, c->ev_it[1]);
     if (int rc = cycle_level<T>(c, 1)) return rc;
@@ -545,13 +561,13 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
         const bool last = k == nu - 1;
         T* out = cur == P0 ? Q0 : P0;
         if (k == 0 && last)
-            k_mg0_post<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, z);
+            k_mg0_post<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, z, c->mg.skip);
         else if (k == 0)
-            k_mg0_post<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, out);
+            k_mg0_post<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, out, c->mg.skip);
         else if (last)
-            k_mg0_sweep<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, z);
+            k_mg0_sweep<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, z, c->mg.skip);
         else
-            k_mg0_sweep<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out);
+            k_mg0_sweep<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }

@@ -490,8 +490,6 @@ __global__ void k_fg_v0(int64_t n, const T* __restrict__ r, T* __restrict__ V0, 
     GRID_LOOP(i, n) V0[i] = (T)((double)r[i] * inv);
 }
 
-__device__ __forceinline__ bool fg_skip(const Scalars* sc) { return sc->done || sc->tmp[2] != 0.0; }
-
 // w = A v_j
 template <typename Op, typename T>
 __global__ void __launch_bounds__(RED_BLOCK) k_fg_spmv(int64_t n, Op A, const T* __restrict__ V, T* __restrict__ w,
@@ -562,8 +560,7 @@ __global__ void __launch_bounds__(RED_BLOCK) k_fg_maxpy(int64_t n, const T* __re
 }
 
 // h(j+1,j) = ||w||; Givens; residual estimate; cycle/convergence control
-__global__ void k_fg_givens(const double* __restrict__ part, Scalars* sc, double* Hd, FgLayout F, int j) {
-    if (fg_skip(sc)) return;
+__device__ void fg_givens(const double* __restrict__ part, Scalars* sc, double* Hd, FgLayout F, int j) {
     double v[1];
     reduce_partials<1>(part, v);
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -594,6 +591,14 @@ __global__ void k_fg_givens(const double* __restrict__ part, Scalars* sc, double
     Hd[F.g(j)] = cs * gj;
     sc->tmp[3] = hn;  // scale of v_{j+1}
     if (fabs(Hd[F.g(j + 1)]) <= sc->target || hn == 0.0 || j + 1 == F.m) sc->tmp[2] = 1.0;
+}
+
+// `mirror` (pinned host memory, optional) receives the scalars after this
+// iteration, whether it ran or was skipped
+__global__ void k_fg_givens(const double* __restrict__ part, Scalars* sc, double* Hd, FgLayout F, int j,
+                            Scalars* mirror) {
+    if (!fg_skip(sc)) fg_givens(part, sc, Hd, F, j);
+    if (mirror && threadIdx.x == 0) *mirror = *sc;
 }
 
 // v_{j+1} = w / h(j+1,j)
@@ -839,7 +844,7 @@ int run_fgmres(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_r0
                 k_fg_maxpy<T><<<G, B, 0, c->stream>>>(n, w.V, wv, j, c->Hd, F, pass, c->part, c->sc);
                 c->launches += 3;
             }
-            k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, j);
+            k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, j, nullptr);
             k_fg_next<T><<<G, B, 0, c->stream>>>(n, wv, w.V, j, c->sc);
             c->launches += 3;
         }
@@ -974,7 +979,7 @@ int run_fgmres_ir(Ctx* c, int64_t n, bsc_solve_info* si) {
                 k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc2);
                 k_fg_maxpy<double><<<G, B, 0, c->stream>>>(n, c->V, w, j, c->Hd, F, pass, c->part, c->sc2);
             }
-            k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, j);
+            k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, j, nullptr);
             k_fg_next<double><<<G, B, 0, c->stream>>>(n, w, c->V, j, c->sc2);
             c->launches += 11;
             BSC_CUDA(c, cudaGetLastError());
@@ -1022,14 +1027,47 @@ void mg_iter_profile(Ctx* c) {
 }
 
 // the SpMV bracketed by ev_spmv (the stream idle) into the SPMV slot
-void spmv_time(Ctx* c) {
+void spmv_time(Ctx* c, int pair = 0) {
     if (!c->timing) return;
     float ms = 0.f;
-    if (cudaEventElapsedTime(&ms, c->ev_spmv[0], c->ev_spmv[1]) == cudaSuccess) {
+    if (cudaEventElapsedTime(&ms, c->ev_spmv[2 * pair], c->ev_spmv[2 * pair + 1]) == cudaSuccess) {
         c->ms[BSC_T_SPMV] += ms;
         c->calls[BSC_T_SPMV]++;
     }
     (void)cudaGetLastError();
+}
+
+// One FGMRES restart cycle of multigrid-preconditioned iterations.
+// queue(j, mirror) queues iteration j, whose last kernel copies the scalars
+// `dsc` into the pinned `mirror`.  Iteration j+1 is queued before iteration
+// j's scalars are read, so the GPU never waits for the host between
+// iterations; an iteration queued past the cycle's stop returns at every
+// kernel.  With per-iteration profiling on (events shared by all
+// iterations), each iteration is read before the next one is queued.
+// `h` receives the scalars of the last iteration that ran; *iters counts them.
+template <typename Q>
+int fg_cycle(Ctx* c, int m, int budget, Scalars* h, int* iters, Q queue) {
+    if (!c->h_it) return set_err(c, BSC_E_INVALID, "multigrid FGMRES without its pinned scalar mirror");
+    const bool lag = !c->prof_iter;
+    int last = -1;  // queued, not yet read
+    for (int j = 0;; ++j) {
+        const bool more = j < m && *iters + (lag && last >= 0 ? 1 : 0) < budget;
+        if (more) {
+            if (int rc = queue(j, c->h_it + (j & 1))) return rc;
+            BSC_CUDA(c, cudaEventRecord(c->ev_lag[j & 1], c->stream));
+        }
+        const int chk = lag ? last : (more ? j : -1);
+        if (chk >= 0) {
+            BSC_CUDA(c, cudaEventSynchronize(c->ev_lag[chk & 1]));
+            *h = c->h_it[chk & 1];
+            ++*iters;
+            mg_iter_profile(c);
+            spmv_time(c, 1 + (chk & 1));
+            if (h->tmp[2] != 0.0) return BSC_OK;  // iteration j, if queued, skips
+        }
+        if (!more) return BSC_OK;
+        last = j;
+    }
 }
 
 // Flexible GMRES(m) in FP64 on the FP64 operator, right-preconditioned by
@@ -1059,39 +1097,36 @@ int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
         if (c->h_sc[1].done || iters >= P.maxit) break;
         k_fg_v0<double><<<G, B, 0, c->stream>>>(n, c->r, V, c->sc2);
         BSC_LAUNCH(c);
-        for (int j = 0; j < m && iters < P.maxit; ++j) {
+        mg.skip = c->sc2;
+        rc = fg_cycle(c, m, P.maxit, c->h_sc + 1, &iters, [&](int j, Scalars* mirror) -> int {
             double* zj = Z + (int64_t)j * n;
             const double* vj = V + (int64_t)j * n;
             // one iteration (V-cycle, SpMV, CGS2, Givens) as a cached graph per
             // column j, keyed by the cell map too, whose buffer a Morton
             // reorder swaps
-            rc = graph_run(c, c->pcell, vj, zj, n, [&]() -> int {
+            return graph_run(c, c->pcell, vj, zj, n, [&]() -> int {
                 if (int r = mg_vcycle_f64(c, vj, zj)) return r;
                 // the SpMV w = A z_j is bracketed by events: the dominant
                 // HBM-bound kernel, timed in place
-                if (c->timing) record_event(c, c->ev_spmv[0]);
+                if (c->timing) record_event(c, c->ev_spmv[2 + 2 * (j & 1)]);
                 k_spmv_z<double><<<G, B, 0, c->stream>>>(n, A, zj, w, c->sc2);
-                if (c->timing) record_event(c, c->ev_spmv[1]);
+                if (c->timing) record_event(c, c->ev_spmv[3 + 2 * (j & 1)]);
                 if (c->prof_iter) record_event(c, c->ev_it[4]);
                 for (int pass = 0; pass < 2; ++pass) {
                     k_fg_mdot<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc2);
                     k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc2);
                     k_fg_maxpy<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, pass, c->part, c->sc2);
                 }
-                k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, j);
+                k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc2, c->Hd, F, j, mirror);
                 k_fg_next<double><<<G, B, 0, c->stream>>>(n, w, V, j, c->sc2);
                 if (c->prof_iter) record_event(c, c->ev_it[5]);
                 c->launches += 9;
                 BSC_CUDA(c, cudaGetLastError());
                 return BSC_OK;
             });
-            if (rc) return rc;
-            ++iters;
-            if ((rc = fetch_outer(c))) return rc;
-            mg_iter_profile(c);
-            spmv_time(c);
-            if (c->h_sc[1].tmp[2] != 0.0) break;
-        }
+        });
+        mg.skip = nullptr;
+        if (rc) return rc;
         k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc2, c->Hd, F);
         k_fg_update_z<double><<<G, B, 0, c->stream>>>(n, x, Z, c->Hd, F, c->sc2);
         c->launches += 2;
@@ -1237,37 +1272,34 @@ int run_fgmres_ir_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
         k_fg_start<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, 1, inner_tol, 1);
         k_fgf_v0<<<G, B, 0, c->stream>>>(n, rf, V, c->sc);
         c->launches += 4;
-        for (int j = 0; j < m && inner < P.maxit; ++j) {
+        mg.skip = c->sc;
+        rc = fg_cycle(c, m, P.maxit, c->h_sc, &inner, [&](int j, Scalars* mirror) -> int {
             float* zj = Z + (int64_t)j * n;
             const float* vj = V + (int64_t)j * n;
             // one inner iteration as a cached graph per column j (and cell map)
-            rc = graph_run(c, c->pcell, vj, zj, n, [&]() -> int {
+            return graph_run(c, c->pcell, vj, zj, n, [&]() -> int {
                 if (int r = mg_vcycle_f32(c, vj, zj)) return r;
                 // the FP32 SpMV w = A z_j is bracketed by events (the
                 // dominant HBM-bound kernel, timed in place)
-                if (c->timing) record_event(c, c->ev_spmv[0]);
+                if (c->timing) record_event(c, c->ev_spmv[2 + 2 * (j & 1)]);
                 k_spmv_f<<<G, B, 0, c->stream>>>(n, Af, zj, w, c->sc);
-                if (c->timing) record_event(c, c->ev_spmv[1]);
+                if (c->timing) record_event(c, c->ev_spmv[3 + 2 * (j & 1)]);
                 if (c->prof_iter) record_event(c, c->ev_it[4]);
                 for (int pass = 0; pass < 2; ++pass) {
                     k_fgf_mdot<<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc);
                     k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, pass, c->sc);
                     k_fgf_maxpy<<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, pass, c->part, c->sc);
                 }
-                k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, j);
+                k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, j, mirror);
                 k_fgf_next<<<G, B, 0, c->stream>>>(n, w, V, j, c->sc);
                 if (c->prof_iter) record_event(c, c->ev_it[5]);
                 c->launches += 9;
                 BSC_CUDA(c, cudaGetLastError());
                 return BSC_OK;
             });
-            if (rc) return rc;
-            ++inner;
-            if ((rc = fetch_scalars(c))) return rc;
-            mg_iter_profile(c);
-            spmv_time(c);
-            if (c->h_sc[0].tmp[2] != 0.0) break;
-        }
+        });
+        mg.skip = nullptr;
+        if (rc) return rc;
         k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc, c->Hd, F);
         k_ir_addz<<<G, B, 0, c->stream>>>(n, x, Z, c->Hd, F, c->sc);
         c->launches += 2;
