@@ -374,8 +374,8 @@ int bsc_default_params(bsc_params* p, double dl) {
     p->max_neighbors = 64;
     p->reorder_every = 20;
     p->precond = BSC_PRECOND_NONE;
-    p->mg_omega = 0.8;
-    p->mg_scale = 1.5;
+    p->mg_omega = 0.9;
+    p->mg_scale = 1.8;
     p->mg_sweeps = 2;
     p->mg_coarse_max = MG_COARSE_MAX;
     return BSC_OK;
