@@ -140,7 +140,10 @@ struct Mg {
     int tail_l0 = 0;               // levels tail_l0..nlev run in one single-CTA kernel
     MgLevel L[MG_MAX_LEVELS + 1];
     double* cinv = nullptr;        // inverse of the coarsest level, FP64, row-major
+    float* cinvf = nullptr;        // its FP32 copy (mixed path)
+    int tail_smem = 0;             // bytes of shared memory the tail stages its levels in; 0: none
     double* rowslots = nullptr;    // 9 x n: each row's sums over the 3x3 neighbour cells
+    float* rowslotsf = nullptr;    // their FP32 copy (mixed path)
     int64_t n = 0;                 // rows the buffers are sized for
     int gx = 0, gy = 0;            // level-1 grid they are sized for
     int m = 0;                     // FGMRES restart length

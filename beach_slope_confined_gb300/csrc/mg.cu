@@ -42,7 +42,7 @@ __device__ __forceinline__ int stencil_slot(int dx, int dy) { return (dx + 1) * 
 // (every neighbour lies in the 3x3 cells around it); (2) thread per cell, its
 // rows' slot sums added in the cell list's (id-sorted) order
 __global__ void k_mg_rowslots(int64_t n, int ny, const int32_t* __restrict__ pcell, EllOp<double> A,
-                              double* __restrict__ rs) {
+                              double* __restrict__ rs, float* __restrict__ rsf) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int ci = pcell[i], cx = ci / ny, cy = ci % ny;
@@ -58,6 +58,9 @@ __global__ void k_mg_rowslots(int64_t n, int ny, const int32_t* __restrict__ pce
     }
 #pragma unroll
     for (int s = 0; s < 9; ++s) rs[s * n + i] = acc[s];
+    if (rsf)
+#pragma unroll
+        for (int s = 0; s < 9; ++s) rsf[s * n + i] = (float)acc[s];
 }
 
 __global__ void k_mg_galerkin0(int nx, int ny, int64_t n, const int32_t* __restrict__ cell_start,
@@ -289,6 +292,11 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const 
 // to fill the GPU; the thresholds are measured (a single SM is latency-bound
 // above about a thousand FP32 cells, and FP64 runs at a small fraction of
 // the FP32 rate on this GPU).
+// With `smem` set, the kernel first copies every tail level's stencil and
+// diagonal and the coarsest level's inverse into shared memory and keeps the
+// tail's vectors there: the phases then wait on shared-memory latency, not
+// on L2's.  Only the first level's right-hand side comes in from global
+// memory and only its solution goes out (the level above prolongs it).
 constexpr int MG_TAIL_CELLS = 1100;
 constexpr int MG_TAIL_CELLS_F64 = 300;
 constexpr int MG_TAIL_THREADS = 1024;
@@ -301,22 +309,78 @@ struct TailLevel {
 };
 template <typename T>
 struct TailArgs {
-    int l0, nlev, nu;
+    int l0, nlev, nu, smem;
     T w, scale;
-    const double* cinv;
+    const T* cinv;
     const Scalars* sk;
     TailLevel<T> L[MG_MAX_LEVELS + 1];
+    int64_t off[MG_MAX_LEVELS + 2];  // shared-memory words: level q's block; off[nlev+1] the inverse
 };
 
+// shared-memory words (of T) the tail stages for levels l0..nlev: per level
+// the 9-point stencil, the diagonal and four vectors, each segment rounded
+// to 16 bytes; then the coarsest inverse
 template <typename T>
-__global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
-    if (mg_skip(P.sk)) return;
+__host__ __device__ inline int64_t tail_seg(int64_t count) {
+    const int64_t per16 = 16 / sizeof(T);
+    return (count + per16 - 1) / per16 * per16;
+}
+template <typename T>
+inline int64_t tail_words(const int64_t* nc, int l0, int nlev, int64_t* off) {
+    int64_t w = 0;
+    for (int q = l0; q <= nlev; ++q) {
+        if (off) off[q] = w;
+        w += tail_seg<T>(9 * nc[q]) + 5 * tail_seg<T>(nc[q]);
+    }
+    if (off) off[nlev + 1] = w;
+    return w + tail_seg<T>(nc[nlev] * nc[nlev]);
+}
+
+// bytes from global to shared memory (both 16-byte aligned), all threads
+__device__ __forceinline__ void tail_copy(void* dst, const void* src, int64_t bytes) {
+    const int64_t n16 = bytes / 16;
+    for (int64_t k = threadIdx.x; k < n16; k += blockDim.x) ((uint4*)dst)[k] = ((const uint4*)src)[k];
+    for (int64_t k = n16 * 16 + threadIdx.x; k < bytes; k += blockDim.x)
+        ((unsigned char*)dst)[k] = ((const unsigned char*)src)[k];
+}
+
+template <typename T>
+__device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* tail_sm) {
     const int t = threadIdx.x, NT = blockDim.x;
     const T w = P.w, sc = P.scale;
     const int nu = P.nu;
+    // level q as the phases see it: in global memory, or staged
+    auto lv = [&](int q) -> TailLevel<T> {
+        TailLevel<T> L = P.L[q];
+        if (P.smem) {
+            const int64_t nc = (int64_t)L.nx * L.ny, sn = tail_seg<T>(nc);
+            T* s = (T*)tail_sm + P.off[q];
+            L.A = s;
+            L.dinv = s + tail_seg<T>(9 * nc);
+            T* v = s + tail_seg<T>(9 * nc) + sn;
+            L.b = v;
+            L.x = v + sn;
+            L.y = v + 2 * sn;
+            L.t = v + 3 * sn;
+        }
+        return L;
+    };
+    const T* cinv = P.smem ? (const T*)((T*)tail_sm + P.off[P.nlev + 1]) : P.cinv;
+    if (P.smem) {
+        for (int l = P.l0; l <= P.nlev; ++l) {
+            const TailLevel<T> L = lv(l);
+            const int64_t nc = (int64_t)L.nx * L.ny;
+            tail_copy((void*)L.A, P.L[l].A, 9 * nc * sizeof(T));
+            tail_copy((void*)L.dinv, P.L[l].dinv, nc * sizeof(T));
+            if (l == P.l0) tail_copy(L.b, P.L[l].b, nc * sizeof(T));
+        }
+        const int64_t nco = (int64_t)P.L[P.nlev].nx * P.L[P.nlev].ny;
+        tail_copy((void*)cinv, P.cinv, nco * nco * sizeof(T));
+        __syncthreads();
+    }
     T* cur[MG_MAX_LEVELS + 1];
     for (int l = P.l0; l < P.nlev; ++l) {
-        const TailLevel<T>& L = P.L[l];
+        const TailLevel<T> L = lv(l);
         const int64_t nc = (int64_t)L.nx * L.ny;
         T* c0 = L.y;
         for (int64_t c = t; c < nc; c += NT)
@@ -331,26 +395,26 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
             c0 = out;
         }
         cur[l] = c0;
-        const TailLevel<T>& C = P.L[l + 1];
+        const TailLevel<T> C = lv(l + 1);
         const int64_t ncc = (int64_t)C.nx * C.ny;
         for (int64_t q = t; q < ncc; q += NT) C.b[q] = restrict_at<T>(L.nx, L.ny, L.A, L.b, c0, q, C.ny);
         __syncthreads();
     }
     {   // coarsest level: x = C^-1 b, a warp per row, lanes along the row
-        const TailLevel<T>& L = P.L[P.nlev];
+        const TailLevel<T> L = lv(P.nlev);
         const int n = L.nx * L.ny;
         const int lane = t & 31;
         for (int r = t >> 5; r < n; r += NT >> 5) {
-            double s = 0.0;
-            for (int q = lane; q < n; q += 32) s += P.cinv[r * n + q] * (double)L.b[q];
+            T s = 0;
+            for (int q = lane; q < n; q += 32) s += cinv[r * n + q] * L.b[q];
             for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (lane == 0) L.x[r] = (T)s;
+            if (lane == 0) L.x[r] = s;
         }
         __syncthreads();
     }
     for (int l = P.nlev - 1; l >= P.l0; --l) {
-        const TailLevel<T>& L = P.L[l];
-        const TailLevel<T>& C = P.L[l + 1];
+        const TailLevel<T> L = lv(l);
+        const TailLevel<T> C = lv(l + 1);
         const int64_t nc = (int64_t)L.nx * L.ny;
         T* c0 = cur[l];
         for (int k = 0; k < nu; ++k) {
@@ -362,6 +426,18 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
             c0 = out;
         }
     }
+    if (P.smem) {  // the first level's solution, for the level above
+        const TailLevel<T> L = lv(P.l0);
+        const int64_t nc = (int64_t)L.nx * L.ny;
+        for (int64_t c = t; c < nc; c += NT) P.L[P.l0].x[c] = L.x[c];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
+    extern __shared__ __align__(16) unsigned char tail_sm[];
+    if (mg_skip(P.sk)) return;
+    tail_body<T>(P, tail_sm);
 }
 
 // ---- V-cycle, level 0 (the PPE, unit diagonal) ---------------------------------------
@@ -417,25 +493,31 @@ __global__ void k_mg0_restrict(int64_t nc, const int32_t* __restrict__ cell_star
     }
 }
 
-// first post-sweep with the prolonged level-1 correction folded in:
-// y = x + scale * x1[cell]; x_out = y + w (v - A y)
-template <typename T, typename VI, typename O>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_post(int64_t n, EllOp<T> A, const VI* __restrict__ v,
-                                                        const T* __restrict__ x, const T* __restrict__ x1,
-                                                        const int32_t* __restrict__ pcell, T scale, T w,
-                                                        O* __restrict__ xout, const Scalars* __restrict__ sk) {
+// First post-sweep, with the prolonged level-1 correction folded in and no
+// pass over the matrix.  With y = x + s P x1 and r = v - A x (the residual
+// restricted on the way down, still in place):
+//   v - A y = r - s (A P x1),   (A P x1)_i = sum_k rs_k(i) x1[cell k of i's 3x3],
+// rs_k(i) being row i's sums over its 3x3 neighbour cells (with the unit
+// diagonal), the same sums the level-1 Galerkin product is built from.
+// Reads 9 sums and 9 cell values per row instead of the row's entries.
+template <typename T, typename O>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_post(int64_t n, int nx, int ny, const T* __restrict__ x,
+                                                        const T* __restrict__ r, const T* __restrict__ x1,
+                                                        const int32_t* __restrict__ pcell, const T* __restrict__ rs,
+                                                        T scale, T w, O* __restrict__ xout,
+                                                        const Scalars* __restrict__ sk) {
     if (mg_skip(sk)) return;
     GRID_LOOP(i, n) {
-        const T yi = x[i] + scale * x1[pcell[i]];
-        T Ay = yi;
-        const int m = A.cnt[i];
-        const int64_t e0 = ell(i, 0, A.kmax);
-        for (int k = 0; k < m; ++k) {
-            const int64_t e = e0 + (int64_t)k * 32;
-            const int j = A.nbr[e];
-            Ay += A.aval[e] * (x[j] + scale * x1[pcell[j]]);
+        const int c = pcell[i], cx = c / ny, cy = c - cx * ny;
+        T apx = 0;
+#pragma unroll
+        for (int s = 0; s < 9; ++s) {
+            const int gx = cx + s / 3 - 1, gy = cy + s % 3 - 1;
+            if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
+            apx += rs[s * n + i] * x1[(int64_t)gx * ny + gy];
         }
-        xout[i] = (O)(yi + w * ((T)v[i] - Ay));
+        const T yi = x[i] + scale * x1[c];
+        xout[i] = (O)(yi + w * (r[i] - scale * apx));
     }
 }
 
@@ -481,13 +563,22 @@ int cycle_level(Ctx* c, int l) {
         P.nu = nu;
         P.w = w;
         P.scale = sc;
-        P.cinv = mg.cinv;
+        if constexpr (sizeof(T) == 4)
+            P.cinv = mg.cinvf;
+        else
+            P.cinv = mg.cinv;
         P.sk = mg.skip;
+        P.smem = mg.tail_smem > 0;
+        {
+            int64_t nc[MG_MAX_LEVELS + 1] = {};
+            for (int q = l; q <= mg.nlev; ++q) nc[q] = mg.L[q].nc;
+            tail_words<T>(nc, l, mg.nlev, P.off);
+        }
         for (int q = l; q <= mg.nlev; ++q) {
             Lv<T> u = level_view<T>(mg.L[q]);
             P.L[q] = TailLevel<T>{mg.L[q].nx, mg.L[q].ny, u.A, u.dinv, u.b, u.x, u.y, u.t};
         }
-        k_mg_tail<T><<<1, MG_TAIL_THREADS, 0, c->stream>>>(P);
+        k_mg_tail<T><<<1, MG_TAIL_THREADS, mg.tail_smem, c->stream>>>(P);
         BSC_LAUNCH(c);
         return BSC_OK;
     }
@@ -557,13 +648,20 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
     if (int rc = cycle_level<T>(c, 1)) return rc;
     if (c->prof_iter) record_event(c, c->ev_it[2]);
     // post-smoothing; the last sweep writes z
+    const T* rs;
+    if constexpr (sizeof(T) == 4)
+        rs = mg.rowslotsf;
+    else
+        rs = mg.rowslots;
     for (int k = 0; k < nu; ++k) {
         const bool last = k == nu - 1;
         T* out = cur == P0 ? Q0 : P0;
         if (k == 0 && last)
-            k_mg0_post<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, z, c->mg.skip);
+            k_mg0_post<T, O><<<G, MG_BLOCK, 0, c->stream>>>(n, L1.nx, L1.ny, cur, R0, v1.x, c->pcell, rs, sc, w, z,
+                                                            c->mg.skip);
         else if (k == 0)
-            k_mg0_post<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, v1.x, c->pcell, sc, w, out, c->mg.skip);
+            k_mg0_post<T, T><<<G, MG_BLOCK, 0, c->stream>>>(n, L1.nx, L1.ny, cur, R0, v1.x, c->pcell, rs, sc, w,
+                                                            out, c->mg.skip);
         else if (last)
             k_mg0_sweep<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, z, c->mg.skip);
         else
@@ -631,8 +729,28 @@ int mg_alloc(Ctx* c) {
         L.t = vec + 3 * stride;
     }
     if ((rc = mg_dalloc(c, &mg.rowslots, 9 * n))) return rc;  // the level-1 Galerkin pass
+    if (f32 && (rc = mg_dalloc(c, &mg.rowslotsf, 9 * n))) return rc;
     const int64_t nco = mg.L[nlev].nc;
     if ((rc = mg_dalloc(c, &mg.cinv, nco * nco))) return rc;
+    if (f32 && (rc = mg_dalloc(c, &mg.cinvf, nco * nco))) return rc;
+    // stage the tail in shared memory when it fits
+    {
+        int64_t nc[MG_MAX_LEVELS + 1] = {};
+        for (int l = 1; l <= nlev; ++l) nc[l] = mg.L[l].nc;
+        const int64_t bytes = f32 ? tail_words<float>(nc, mg.tail_l0, nlev, nullptr) * (int64_t)sizeof(float)
+                                  : tail_words<double>(nc, mg.tail_l0, nlev, nullptr) * (int64_t)sizeof(double);
+        int optin = 0;
+        BSC_CUDA(c, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+        mg.tail_smem = bytes <= optin ? (int)bytes : 0;
+        // the attribute is per function, process-wide: allow the device's
+        // maximum, whatever this context needs
+        if (mg.tail_smem > 0) {
+            if (f32)
+                BSC_CUDA(c, cudaFuncSetAttribute(k_mg_tail<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+            else
+                BSC_CUDA(c, cudaFuncSetAttribute(k_mg_tail<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+        }
+    }
     unsigned char* fine = nullptr;
     if ((rc = mg_dalloc(c, &fine, 3 * n * (int64_t)vs))) return rc;
     mg.r0 = fine;
@@ -672,7 +790,8 @@ int mg_setup(Ctx* c) {
     Mg& mg = c->mg;
     const EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, 0};
     MgLevel& L1 = mg.L[1];
-    k_mg_rowslots<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, L1.ny, c->pcell, A, mg.rowslots);
+    k_mg_rowslots<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, L1.ny, c->pcell, A, mg.rowslots,
+                                                                mg.f32 ? mg.rowslotsf : nullptr);
     BSC_LAUNCH(c);
     k_mg_galerkin0<<<blocks_for(L1.nc, 128), 128, 0, c->stream>>>(L1.nx, L1.ny, c->n, c->cell_start,
                                                                    c->cell_count, c->sorted, mg.rowslots, L1.A,
@@ -689,13 +808,16 @@ int mg_setup(Ctx* c) {
                                      MG_COARSE_MAX * MG_COARSE_MAX * (int)sizeof(double)));
     k_mg_dense_inverse<<<1, 1024, smem, c->stream>>>(Lc.nx, Lc.ny, Lc.A, mg.cinv);
     BSC_LAUNCH(c);
-    if (mg.f32)
+    if (mg.f32) {
         for (int l = 1; l <= mg.nlev; ++l) {
             const MgLevel& L = mg.L[l];
             k_mg_to_f32<<<blocks_for(9 * L.nc, 256), 256, 0, c->stream>>>(9 * L.nc, L.A, L.Af);
             k_mg_to_f32<<<blocks_for(L.nc, 256), 256, 0, c->stream>>>(L.nc, L.dinv, L.dinvf);
             c->launches += 2;
         }
+        k_mg_to_f32<<<blocks_for(Lc.nc * Lc.nc, 256), 256, 0, c->stream>>>(Lc.nc * Lc.nc, mg.cinv, mg.cinvf);
+        BSC_LAUNCH(c);
+    }
     return BSC_OK;
 }
 
