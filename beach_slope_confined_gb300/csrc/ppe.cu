@@ -1113,7 +1113,7 @@ int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
                 // the SpMV w = A z_j is bracketed by events: the dominant
                 // HBM-bound kernel, timed in place
                 if (c->timing) record_event(c, c->ev_spmv[2 + 2 * (j & 1)]);
-                k_spmv_z<double><<<G, B, 0, c->stream>>>(n, A, zj, w, c->sc2);
+                k_spmv_z<double><<<blocks_for(n, B), B, 0, c->stream>>>(n, A, zj, w, c->sc2);
                 if (c->timing) record_event(c, c->ev_spmv[3 + 2 * (j & 1)]);
                 if (c->prof_iter) record_event(c, c->ev_it[4]);
                 k_fg_mdot<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc2);
@@ -1284,7 +1284,7 @@ int run_fgmres_ir_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
                 // the FP32 SpMV w = A z_j is bracketed by events (the
                 // dominant HBM-bound kernel, timed in place)
                 if (c->timing) record_event(c, c->ev_spmv[2 + 2 * (j & 1)]);
-                k_spmv_f<<<G, B, 0, c->stream>>>(n, Af, zj, w, c->sc);
+                k_spmv_f<<<blocks_for(n, B), B, 0, c->stream>>>(n, Af, zj, w, c->sc);
                 if (c->timing) record_event(c, c->ev_spmv[3 + 2 * (j & 1)]);
                 if (c->prof_iter) record_event(c, c->ev_it[4]);
                 k_fgf_mdot<<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc);
