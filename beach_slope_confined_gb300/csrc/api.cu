@@ -169,7 +169,9 @@ static int alloc_for(Ctx* c, int64_t n) {
     // copies for its FP32 pair sums and inner Krylov sweeps
     if ((rc = dalloc(c, &c->gw, slots)) || (rc = dalloc(c, &c->aval, slots))) return rc;
     if (c->mixed) {
-        if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->avalf, slots))) return rc;
+        if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->avalf, slots)) ||
+            (rc = dalloc(c, &c->avalh, slots)))
+            return rc;
     }
     if ((rc = dalloc(c, &c->b, n))) return rc;
     if ((rc = alloc_solver_work(c, n, !c->mixed, c->mixed))) return rc;

@@ -14,6 +14,7 @@
 //    values share the neighbour-list layout (no extra column indices).
 #pragma once
 
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -205,6 +206,7 @@ struct Ctx {
     // PPE
     double* aval = nullptr;       // FP64 off-diagonals (ELL layout)
     float* avalf = nullptr;       // FP32 off-diagonals (mixed)
+    __half* avalh = nullptr;      // FP16 off-diagonals (mixed): the V-cycle's fine-level sweeps
     double* b = nullptr;
     float* bf = nullptr;
     // Krylov work (FP64) and (FP32)

@@ -443,8 +443,8 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
 // ---- V-cycle, level 0 (the PPE, unit diagonal) ---------------------------------------
 // VI: type of the right-hand side v; O: type of the result z (the last sweep)
 // two sweeps from a zero guess: x1 = w v; x2 = x1 + w (v - A x1)
-template <typename T, typename VI>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<T> A, const VI* __restrict__ v, T w,
+template <typename T, typename VI, typename AV>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<AV> A, const VI* __restrict__ v, T w,
                                                         T* __restrict__ x, const Scalars* __restrict__ sk) {
     if (mg_skip(sk)) return;
     GRID_LOOP(i, n) {
@@ -462,8 +462,8 @@ __global__ void k_mg0_scale(int64_t n, const VI* __restrict__ v, T w, T* __restr
 }
 
 // x_out = x + w (v - A x)
-template <typename T, typename VI, typename O>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<T> A, const VI* __restrict__ v,
+template <typename T, typename VI, typename O, typename AV>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<AV> A, const VI* __restrict__ v,
                                                          const T* __restrict__ x, T w, O* __restrict__ xout,
                                                          const Scalars* __restrict__ sk) {
     if (mg_skip(sk)) return;
@@ -471,8 +471,8 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<T> A, c
 }
 
 // r = v - A x
-template <typename T, typename VI>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_resid(int64_t n, EllOp<T> A, const VI* __restrict__ v,
+template <typename T, typename VI, typename AV>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_resid(int64_t n, EllOp<AV> A, const VI* __restrict__ v,
                                                          const T* __restrict__ x, T* __restrict__ r,
                                                          const Scalars* __restrict__ sk) {
     if (mg_skip(sk)) return;
@@ -536,15 +536,28 @@ Lv<T> level_view(const MgLevel& L) {
         return {L.A, L.dinv, (T*)L.b, (T*)L.x, (T*)L.y, (T*)L.t};
 }
 
+// the fine-level operator of the V-cycle: the FP64 matrix on the FP64 path;
+// on the mixed path an FP16 copy of the Jacobi-scaled off-diagonals (all of
+// magnitude below about one).  The V-cycle is only a preconditioner of a
+// flexible Krylov method whose residuals use the FP32 and FP64 operators, so
+// the FP16 rounding (2^-11 relative) can cost iterations, never accuracy;
+// it cuts the bytes of the three matrix passes per V-cycle by a quarter.
 template <typename T>
-EllOp<T> fine_op(Ctx* c);
+struct FineVal;
+template <>
+struct FineVal<double> { using type = double; };
+template <>
+struct FineVal<float> { using type = __half; };
+
+template <typename T>
+EllOp<typename FineVal<T>::type> fine_op(Ctx* c);
 template <>
 EllOp<double> fine_op<double>(Ctx* c) {
     return EllOp<double>{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
 }
 template <>
-EllOp<float> fine_op<float>(Ctx* c) {
-    return EllOp<float>{c->avalf, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+EllOp<__half> fine_op<float>(Ctx* c) {
+    return EllOp<__half>{c->avalh, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
 }
 
 // approximate solve of level l >= 1 (b_l -> x_l)
@@ -620,7 +633,8 @@ template <typename T, typename VI, typename O>
 int vcycle(Ctx* c, const VI* vin, O* z) {
     Mg& mg = c->mg;
     const int64_t n = c->n;
-    const EllOp<T> A = fine_op<T>(c);
+    using AV = typename FineVal<T>::type;
+    const EllOp<AV> A = fine_op<T>(c);
     const T w = (T)c->P.mg_omega, sc = (T)c->P.mg_scale;
     const int nu = c->P.mg_sweeps;
     T *P0 = (T*)mg.y0, *Q0 = (T*)mg.t0, *R0 = (T*)mg.r0;
@@ -633,15 +647,15 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
     if (nu == 1)
         k_mg0_scale<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, vin, w, cur, c->mg.skip);
     else
-        k_mg0_pre2<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, cur, c->mg.skip);
+        k_mg0_pre2<T, VI, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, cur, c->mg.skip);
     BSC_LAUNCH(c);
     for (int k = 2; k < nu; ++k) {
         T* out = cur == P0 ? Q0 : P0;
-        k_mg0_sweep<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out, c->mg.skip);
+        k_mg0_sweep<T, VI, T, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }
-    k_mg0_resid<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, R0, c->mg.skip);
+    k_mg0_resid<T, VI, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, R0, c->mg.skip);
     BSC_LAUNCH(c);
     const MgLevel& L1 = mg.L[1];
     Lv<T> v1 = level_view<T>(L1);
@@ -666,9 +680,9 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
             k_mg0_post<T, T><<<G, MG_BLOCK, 0, c->stream>>>(n, L1.nx, L1.ny, cur, R0, v1.x, c->pcell, rs, sc, w,
                                                             out, c->mg.skip);
         else if (last)
-            k_mg0_sweep<T, VI, O><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, z, c->mg.skip);
+            k_mg0_sweep<T, VI, O, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, z, c->mg.skip);
         else
-            k_mg0_sweep<T, VI, T><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out, c->mg.skip);
+            k_mg0_sweep<T, VI, T, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }

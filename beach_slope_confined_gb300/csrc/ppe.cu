@@ -37,7 +37,7 @@ template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                         const typename Vec2<R>::type* __restrict__ gw,
                                                         const int32_t* __restrict__ cnt, R* __restrict__ aval,
-                                                        float* __restrict__ avalf,
+                                                        float* __restrict__ avalf, __half* __restrict__ avalh,
                                                         double* __restrict__ b, const double* __restrict__ q,
                                                         const double* __restrict__ usx, const double* __restrict__ usy,
                                                         double dt) {
@@ -116,6 +116,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
         for (int k = 0; k < m; ++k) {
             aval[ell(i, k, K.kmax)] = 0;
             if (avalf) avalf[ell(i, k, K.kmax)] = 0.f;
+            if (avalh) avalh[ell(i, k, K.kmax)] = __float2half_rn(0.f);
         }
         b[i] = 0.0;
         return;
@@ -126,6 +127,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
         const R v = aval[e] * inv;
         aval[e] = v;
         if (avalf) avalf[e] = (float)v;  // the mixed path's inner-sweep copy
+        if (avalh) avalh[e] = __float2half_rn((float)v);  // and its V-cycle copy
     }
     b[i] = ((double)fv / dt) / d;
 }
@@ -150,7 +152,8 @@ int op_ppe_assemble(Ctx* c) {
     // rounding moves the pressure by ~5e-6 (relative) at 1e-8 residual; the
     // mixed path keeps an FP32 copy for its inner sweeps
     k_assemble<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
-                                                      c->mixed ? c->avalf : nullptr, c->b, q, ux, uy, c->dt);
+                                                      c->mixed ? c->avalf : nullptr, c->mixed ? c->avalh : nullptr, c->b, q, ux,
+                                                      uy, c->dt);
     BSC_LAUNCH(c);
     c->have_csr = true;
     return BSC_OK;
