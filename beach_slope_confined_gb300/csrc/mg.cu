@@ -65,7 +65,8 @@ __global__ void k_mg_rowslots(int64_t n, int ny, const int32_t* __restrict__ pce
 
 __global__ void k_mg_galerkin0(int nx, int ny, int64_t n, const int32_t* __restrict__ cell_start,
                                const int32_t* __restrict__ cell_count, const int32_t* __restrict__ sorted,
-                               const double* __restrict__ rs, double* __restrict__ Ac, double* __restrict__ dinv) {
+                               const double* __restrict__ rs, double* __restrict__ Ac, double* __restrict__ dinv,
+                               float* __restrict__ Acf, float* __restrict__ dinvf) {
     const int64_t nc = (int64_t)nx * ny;
     const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (c >= nc) return;
@@ -79,11 +80,17 @@ __global__ void k_mg_galerkin0(int nx, int ny, int64_t n, const int32_t* __restr
 #pragma unroll
     for (int s = 0; s < 9; ++s) Ac[s * nc + c] = acc[s];
     dinv[c] = acc[4] != 0.0 ? 1.0 / acc[4] : 0.0;
+    if (Acf) {  // the mixed path's FP32 copies
+#pragma unroll
+        for (int s = 0; s < 9; ++s) Acf[s * nc + c] = (float)acc[s];
+        dinvf[c] = (float)dinv[c];
+    }
 }
 
 // level l -> l+1 over 2x2 blocks
 __global__ void k_mg_galerkin(int nxf, int nyf, const double* __restrict__ Af, int nxc, int nyc,
-                              double* __restrict__ Ac, double* __restrict__ dinv) {
+                              double* __restrict__ Ac, double* __restrict__ dinv, float* __restrict__ Acf,
+                              float* __restrict__ dinvf) {
     const int64_t ncc = (int64_t)nxc * nyc, ncf = (int64_t)nxf * nyf;
     const int64_t C = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (C >= ncc) return;
@@ -108,22 +115,34 @@ __global__ void k_mg_galerkin(int nxf, int nyf, const double* __restrict__ Af, i
 #pragma unroll
     for (int s = 0; s < 9; ++s) Ac[s * ncc + C] = acc[s];
     dinv[C] = acc[4] != 0.0 ? 1.0 / acc[4] : 0.0;
+    if (Acf) {
+#pragma unroll
+        for (int s = 0; s < 9; ++s) Acf[s * ncc + C] = (float)acc[s];
+        dinvf[C] = (float)dinv[C];
+    }
 }
 
 // Dense inverse of the coarsest level by Gauss-Jordan elimination with
 // partial (row) pivoting, in place in shared memory, one CTA.  Empty cells
 // (all-zero rows) become identity rows.  A zero pivot is replaced by a tiny
 // one: the preconditioner then loses that direction but stays finite.
+// Computed in FP32 (R below) on both paths and written as O: one SM runs
+// it, where FP64 is ~60x slower, and the coarsest solve is part of a
+// preconditioner, whose rounding costs iterations, never accuracy.
+template <typename O>
 __global__ void __launch_bounds__(1024) k_mg_dense_inverse(int nx, int ny, const double* __restrict__ A,
-                                                            double* __restrict__ cinv) {
-    extern __shared__ double M[];  // n x n, row-major
+                                                            O* __restrict__ cinv) {
+    using R = float;
+    extern __shared__ __align__(16) unsigned char dense_sm[];
+    R* M = reinterpret_cast<R*>(dense_sm);  // n x n, row-major
     __shared__ int perm[MG_COARSE_MAX];
-    __shared__ double fcol[MG_COARSE_MAX];
+    __shared__ R fcol[MG_COARSE_MAX];
     __shared__ int piv_row;
-    __shared__ double piv_inv;
+    __shared__ R piv_inv;
     const int n = nx * ny;
     const int t = threadIdx.x, T = blockDim.x;
-    for (int q = t; q < n * n; q += T) M[q] = 0.0;
+    const int lane = t & 31, warp = t >> 5, nwarps = T >> 5;
+    for (int q = t; q < n * n; q += T) M[q] = (R)0;
     __syncthreads();
     for (int c = t; c < n; c += T) {
         const int cx = c / ny, cy = c % ny;
@@ -132,23 +151,23 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inverse(int nx, int ny, const
             const double v = A[(int64_t)s * n + c];
             const int gx = cx + s / 3 - 1, gy = cy + s % 3 - 1;
             if (v == 0.0 || gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
-            M[c * n + gx * ny + gy] += v;
+            M[c * n + gx * ny + gy] += (R)v;
             any = true;
         }
-        if (!any) M[c * n + c] = 1.0;
+        if (!any) M[c * n + c] = (R)1;
     }
     __syncthreads();
     for (int k = 0; k < n; ++k) {
         // pivot: the largest |M[i][k]| over i >= k (warp 0)
         if (t < 32) {
-            double best = -1.0;
+            R best = (R)-1;
             int bi = k;
             for (int i = k + t; i < n; i += 32) {
-                const double a = fabs(M[i * n + k]);
+                const R a = fabs(M[i * n + k]);
                 if (a > best) { best = a; bi = i; }
             }
             for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_down_sync(0xffffffffu, best, o);
+                const R ob = __shfl_down_sync(0xffffffffu, best, o);
                 const int oi = __shfl_down_sync(0xffffffffu, bi, o);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
@@ -158,27 +177,30 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inverse(int nx, int ny, const
         const int p = piv_row;
         if (p != k)
             for (int j = t; j < n; j += T) {
-                const double a = M[k * n + j];
+                const R a = M[k * n + j];
                 M[k * n + j] = M[p * n + j];
                 M[p * n + j] = a;
             }
         __syncthreads();
         if (t == 0) {
-            double pv = M[k * n + k];
-            if (pv == 0.0) pv = 1e-300;
-            piv_inv = 1.0 / pv;
-            M[k * n + k] = 1.0;
+            R pv = M[k * n + k];
+            if (pv == (R)0) pv = (R)1e-30f;
+            piv_inv = (R)1 / pv;
+            M[k * n + k] = (R)1;
         }
         __syncthreads();
         for (int j = t; j < n; j += T) M[k * n + j] *= piv_inv;
-        for (int i = t; i < n; i += T) fcol[i] = (i == k) ? 0.0 : M[i * n + k];
+        for (int i = t; i < n; i += T) fcol[i] = (i == k) ? (R)0 : M[i * n + k];
         __syncthreads();
         for (int i = t; i < n; i += T)
-            if (i != k) M[i * n + k] = 0.0;
+            if (i != k) M[i * n + k] = (R)0;
         __syncthreads();
-        for (int q = t; q < n * n; q += T) {
-            const int i = q / n, j = q % n;
-            if (i != k) M[q] -= fcol[i] * M[k * n + j];
+        // eliminate column k from every other row: a warp per row, lanes
+        // along it
+        for (int i = warp; i < n; i += nwarps) {
+            if (i == k) continue;
+            const R f = fcol[i];
+            for (int j = lane; j < n; j += 32) M[i * n + j] -= f * M[k * n + j];
         }
         __syncthreads();
     }
@@ -187,17 +209,13 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inverse(int nx, int ny, const
         const int p = perm[k];
         if (p != k)
             for (int i = t; i < n; i += T) {
-                const double a = M[i * n + k];
+                const R a = M[i * n + k];
                 M[i * n + k] = M[i * n + p];
                 M[i * n + p] = a;
             }
         __syncthreads();
     }
-    for (int q = t; q < n * n; q += T) cinv[q] = M[q];
-}
-
-__global__ void k_mg_to_f32(int64_t n, const double* __restrict__ a, float* __restrict__ b) {
-    GRID_LOOP(i, n) b[i] = (float)a[i];
+    for (int q = t; q < n * n; q += T) cinv[q] = (O)M[q];
 }
 
 // ---- V-cycle, structured levels (l >= 1) -------------------------------------------
@@ -810,31 +828,29 @@ int mg_setup(Ctx* c) {
     k_mg_rowslots<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, L1.ny, c->pcell, A, mg.rowslots,
                                                                 mg.f32 ? mg.rowslotsf : nullptr);
     BSC_LAUNCH(c);
+    const bool f32 = mg.f32;
     k_mg_galerkin0<<<blocks_for(L1.nc, 128), 128, 0, c->stream>>>(L1.nx, L1.ny, c->n, c->cell_start,
                                                                    c->cell_count, c->sorted, mg.rowslots, L1.A,
-                                                                   L1.dinv);
+                                                                   L1.dinv, f32 ? L1.Af : nullptr,
+                                                                   f32 ? L1.dinvf : nullptr);
     BSC_LAUNCH(c);
     for (int l = 1; l < mg.nlev; ++l) {
         const MgLevel &F = mg.L[l], &C = mg.L[l + 1];
-        k_mg_galerkin<<<blocks_for(C.nc, 128), 128, 0, c->stream>>>(F.nx, F.ny, F.A, C.nx, C.ny, C.A, C.dinv);
+        k_mg_galerkin<<<blocks_for(C.nc, 128), 128, 0, c->stream>>>(F.nx, F.ny, F.A, C.nx, C.ny, C.A, C.dinv,
+                                                                     f32 ? C.Af : nullptr, f32 ? C.dinvf : nullptr);
         BSC_LAUNCH(c);
     }
+    // the coarsest inverse (FP32 Gauss-Jordan), in the V-cycle's precision
     const MgLevel& Lc = mg.L[mg.nlev];
-    const int smem = (int)(Lc.nc * Lc.nc * sizeof(double));
-    BSC_CUDA(c, cudaFuncSetAttribute(k_mg_dense_inverse, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     MG_COARSE_MAX * MG_COARSE_MAX * (int)sizeof(double)));
-    k_mg_dense_inverse<<<1, 1024, smem, c->stream>>>(Lc.nx, Lc.ny, Lc.A, mg.cinv);
+    const int smem = (int)(Lc.nc * Lc.nc * sizeof(float));
+    const int smem_max = MG_COARSE_MAX * MG_COARSE_MAX * (int)sizeof(float);
+    BSC_CUDA(c, cudaFuncSetAttribute(k_mg_dense_inverse<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+    BSC_CUDA(c, cudaFuncSetAttribute(k_mg_dense_inverse<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_max));
+    if (f32)
+        k_mg_dense_inverse<float><<<1, 1024, smem, c->stream>>>(Lc.nx, Lc.ny, Lc.A, mg.cinvf);
+    else
+        k_mg_dense_inverse<double><<<1, 1024, smem, c->stream>>>(Lc.nx, Lc.ny, Lc.A, mg.cinv);
     BSC_LAUNCH(c);
-    if (mg.f32) {
-        for (int l = 1; l <= mg.nlev; ++l) {
-            const MgLevel& L = mg.L[l];
-            k_mg_to_f32<<<blocks_for(9 * L.nc, 256), 256, 0, c->stream>>>(9 * L.nc, L.A, L.Af);
-            k_mg_to_f32<<<blocks_for(L.nc, 256), 256, 0, c->stream>>>(L.nc, L.dinv, L.dinvf);
-            c->launches += 2;
-        }
-        k_mg_to_f32<<<blocks_for(Lc.nc * Lc.nc, 256), 256, 0, c->stream>>>(Lc.nc * Lc.nc, mg.cinv, mg.cinvf);
-        BSC_LAUNCH(c);
-    }
     return BSC_OK;
 }
 
