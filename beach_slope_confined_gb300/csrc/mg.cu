@@ -228,15 +228,17 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inverse(int nx, int ny, const
 //   MODE 0: xin;
 //   MODE 1: w D^-1 b (the first sweep from a zero guess, folded in);
 //   MODE 2: xin + scale * xc[parent] (the prolonged coarse correction, folded in).
+// Cell indices fit 32 bits (grids are capped at 16M cells, stencils at 9 x
+// that); 32-bit index arithmetic keeps these latency-bound chains short.
 template <typename T, int MODE>
-__device__ __forceinline__ T smooth_at(int nx, int ny, int64_t c, const T* A, const T* dinv, const T* b,
+__device__ __forceinline__ T smooth_at(int nx, int ny, int c, const T* A, const T* dinv, const T* b,
                                        const T* xin, const T* xc, int nyc, T scale, T w) {
-    const int64_t nc = (int64_t)nx * ny;
-    const int cx = (int)(c / ny), cy = (int)(c % ny);
+    const int nc = nx * ny;
+    const int cx = c / ny, cy = c - cx * ny;
     auto xv = [&](int gx, int gy) -> T {
-        const int64_t g = (int64_t)gx * ny + gy;
+        const int g = gx * ny + gy;
         if (MODE == 1) return w * dinv[g] * b[g];
-        if (MODE == 2) return xin[g] + scale * xc[(int64_t)(gx >> 1) * nyc + (gy >> 1)];
+        if (MODE == 2) return xin[g] + scale * xc[(gx >> 1) * nyc + (gy >> 1)];
         return xin[g];
     };
     T ax = 0;
@@ -251,23 +253,25 @@ __device__ __forceinline__ T smooth_at(int nx, int ny, int64_t c, const T* A, co
 
 // the residual b - A x summed over the 2x2 children of coarse cell C
 template <typename T>
-__device__ __forceinline__ T restrict_at(int nx, int ny, const T* A, const T* b, const T* x, int64_t C, int nyc) {
-    const int64_t nc = (int64_t)nx * ny;
-    const int CX = (int)(C / nyc), CY = (int)(C % nyc);
+__device__ __forceinline__ T restrict_at(int nx, int ny, const T* A, const T* b, const T* x, int C, int nyc) {
+    const int nc = nx * ny;
+    const int CX = C / nyc, CY = C - CX * nyc;
     T sum = 0;
+#pragma unroll
     for (int a = 0; a < 2; ++a) {
         const int fx = 2 * CX + a;
         if (fx >= nx) continue;
+#pragma unroll
         for (int bb = 0; bb < 2; ++bb) {
             const int fy = 2 * CY + bb;
             if (fy >= ny) continue;
-            const int64_t f = (int64_t)fx * ny + fy;
+            const int f = fx * ny + fy;
             T ax = 0;
 #pragma unroll
             for (int s = 0; s < 9; ++s) {
                 const int gx = fx + s / 3 - 1, gy = fy + s % 3 - 1;
                 if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
-                ax += A[s * nc + f] * x[(int64_t)gx * ny + gy];
+                ax += A[s * nc + f] * x[gx * ny + gy];
             }
             sum += b[f] - ax;
         }
@@ -281,9 +285,12 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg_smooth(int nx, int ny, const T*
                                                          const T* __restrict__ xin, const T* __restrict__ xc, int nyc,
                                                          T scale, T w, T* __restrict__ xout,
                                                          const Scalars* __restrict__ sk) {
-    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (c >= (int64_t)nx * ny || mg_skip(sk)) return;
-    xout[c] = smooth_at<T, MODE>(nx, ny, c, A, dinv, b, xin, xc, nyc, scale, w);
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= nx * ny) return;
+    // the loads are in bounds whatever the solver state: they go out before
+    // the skip test's own load returns
+    const T v = smooth_at<T, MODE>(nx, ny, c, A, dinv, b, xin, xc, nyc, scale, w);
+    if (!mg_skip(sk)) xout[c] = v;
 }
 
 // one sweep from a zero guess: x = w D^-1 b
@@ -298,9 +305,10 @@ template <typename T>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const T* __restrict__ A,
                                                            const T* __restrict__ b, const T* __restrict__ x, int nxc,
                                                            int nyc, T* __restrict__ bc, const Scalars* __restrict__ sk) {
-    const int64_t C = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (C >= (int64_t)nxc * nyc || mg_skip(sk)) return;
-    bc[C] = restrict_at<T>(nx, ny, A, b, x, C, nyc);
+    const int C = blockIdx.x * blockDim.x + threadIdx.x;
+    if (C >= nxc * nyc) return;
+    const T v = restrict_at<T>(nx, ny, A, b, x, C, nyc);
+    if (!mg_skip(sk)) bc[C] = v;
 }
 
 // The small levels l0..nlev in one CTA: the same sweeps, restrictions, dense
@@ -363,7 +371,7 @@ __device__ __forceinline__ void tail_copy(void* dst, const void* src, int64_t by
 }
 
 template <typename T>
-__device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* tail_sm) {
+__device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* tail_sm, const Scalars* sk) {
     const int t = threadIdx.x, NT = blockDim.x;
     const T w = P.w, sc = P.scale;
     const int nu = P.nu;
@@ -396,18 +404,19 @@ __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* t
         tail_copy((void*)cinv, P.cinv, nco * nco * sizeof(T));
         __syncthreads();
     }
+    if (mg_skip(sk)) return;  // after the staging loads went out; the same for every thread
     T* cur[MG_MAX_LEVELS + 1];
     for (int l = P.l0; l < P.nlev; ++l) {
         const TailLevel<T> L = lv(l);
         const int64_t nc = (int64_t)L.nx * L.ny;
         T* c0 = L.y;
-        for (int64_t c = t; c < nc; c += NT)
+        for (int c = t; c < nc; c += NT)
             c0[c] = nu == 1 ? w * L.dinv[c] * L.b[c]
                             : smooth_at<T, 1>(L.nx, L.ny, c, L.A, L.dinv, L.b, nullptr, nullptr, 0, sc, w);
         __syncthreads();
         for (int k = 2; k < nu; ++k) {
             T* out = c0 == L.y ? L.t : L.y;
-            for (int64_t c = t; c < nc; c += NT)
+            for (int c = t; c < nc; c += NT)
                 out[c] = smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w);
             __syncthreads();
             c0 = out;
@@ -415,7 +424,7 @@ __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* t
         cur[l] = c0;
         const TailLevel<T> C = lv(l + 1);
         const int64_t ncc = (int64_t)C.nx * C.ny;
-        for (int64_t q = t; q < ncc; q += NT) C.b[q] = restrict_at<T>(L.nx, L.ny, L.A, L.b, c0, q, C.ny);
+        for (int q = t; q < ncc; q += NT) C.b[q] = restrict_at<T>(L.nx, L.ny, L.A, L.b, c0, q, C.ny);
         __syncthreads();
     }
     {   // coarsest level: x = C^-1 b, a warp per row, lanes along the row
@@ -437,7 +446,7 @@ __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* t
         T* c0 = cur[l];
         for (int k = 0; k < nu; ++k) {
             T* out = (k == nu - 1) ? L.x : (c0 == L.y ? L.t : L.y);
-            for (int64_t c = t; c < nc; c += NT)
+            for (int c = t; c < nc; c += NT)
                 out[c] = k == 0 ? smooth_at<T, 2>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, C.x, C.ny, sc, w)
                                 : smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w);
             __syncthreads();
@@ -454,8 +463,7 @@ __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* t
 template <typename T>
 __global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
     extern __shared__ __align__(16) unsigned char tail_sm[];
-    if (mg_skip(P.sk)) return;
-    tail_body<T>(P, tail_sm);
+    tail_body<T>(P, tail_sm, P.sk);
 }
 
 // ---- V-cycle, level 0 (the PPE, unit diagonal) ---------------------------------------
