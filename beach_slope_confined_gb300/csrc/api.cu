@@ -83,6 +83,7 @@ static void derive_kparams(Ctx* c) {
     K.wend_F = 35.0 / (4.0 * 3.140 * ((h * h) * (h * h)));
     K.wend_W = 7.0 / (4 * 3.140 * (h * h));
     K.w0 = (P.kernel == BSC_KERNEL_WENDLAND_C2) ? K.wend_W : 4.0 * K.hyb_A + 6.0 * K.hyb_B;
+    K.inv_w0 = 1.0 / K.w0;
     K.inv_h = 1.0 / h;
     K.hyb_n1 = (9.0 * K.hyb_A + 3.0 * K.hyb_B) / (h * h * h);  // r < h: n1 r - n0 - n2/(r h)
     K.hyb_n0 = 12.0 * K.hyb_A / (h * h);
@@ -169,6 +170,10 @@ static int alloc_for(Ctx* c, int64_t n) {
     // copies for its FP32 pair sums and inner Krylov sweeps
     if ((rc = dalloc(c, &c->gw, slots)) || (rc = dalloc(c, &c->aval, slots))) return rc;
     if (c->mixed) {
+        float* tw = nullptr;
+        if ((rc = dalloc(c, &tw, 6 * n))) return rc;
+        c->f_vol = tw; c->f_nu = tw + n; c->f_nut = tw + 2 * n; c->f_tke = tw + 3 * n; c->f_varts = tw + 4 * n;
+        c->f_q = tw + 5 * n;
         if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->avalf, slots)) ||
             (rc = dalloc(c, &c->avalh, slots)))
             return rc;

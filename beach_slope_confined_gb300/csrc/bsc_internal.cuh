@@ -70,7 +70,7 @@ struct KParams {
     double eddy_cs, eddy_cv, eddy_ce, varts_ps;
     double bxmin, bxmax;
     // kernel coefficients: grad_i W = F(r) (x_i - x_j)
-    double hyb_A, hyb_B, wend_F, wend_W, w0;
+    double hyb_A, hyb_B, wend_F, wend_W, w0, inv_w0;
     double inv_h, hyb_n0, hyb_n1, hyb_n2, hyb_f;  // folded hybrid-gradient constants
     // cell grid
     double gx0, gy0, cs;
@@ -187,6 +187,12 @@ struct Ctx {
     double* lstage = nullptr;  // 4n: the interleaved L of the host state view, on the device
     float2* sposf = nullptr;
     float* swf = nullptr;         // solids' (1 - n_s) V_s in FP32 (the mixed path's porosity sum)
+    // mixed path: FP32 twins of per-particle fields read per pair by the FP32
+    // pair sums, written once per particle by each stage's prologue kernel
+    // (an FP64 -> FP32 conversion runs on GB300's FP64 pipe: per pair it costs
+    // as much as an FP64 add)
+    float *f_vol = nullptr, *f_nu = nullptr, *f_nut = nullptr, *f_tke = nullptr, *f_varts = nullptr,
+          *f_q = nullptr;
     // solids: their own cell list, static after upload
     double *sx = nullptr, *sy = nullptr, *svol = nullptr, *spor = nullptr;
     int32_t *scell_start = nullptr, *scell_count = nullptr;

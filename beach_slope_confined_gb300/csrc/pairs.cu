@@ -315,11 +315,24 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
     S.vol[i] = S.mass[i] / rho;
     // Ergun/Darcy-Forchheimer coefficient (porous.f90:192,204-212),
     // Fch*sqrt(lamk) written as beta/sqrt(n^3)
-    const double n3 = nn * nn * nn, d = K.d50;
-    const double vx = S.vx[i], vy = S.vy[i];
-    const double vmag = sqrt(vx * vx + vy * vy);
-    S.resist[i] = -((vis_of(oden) / oden) * K.alpha * ((1.0 - nn) * (1.0 - nn)) / (n3 * (d * d))) -
-                  ((K.beta / sqrt(n3)) * vmag * (1.0 - nn)) / (sqrt(n3) * d);
+    if constexpr (sizeof(R) == 4) {
+        // FP32 on the mixed path (its divisions and roots would dominate this
+        // kernel on the FP64 pipe); the coefficient only enters the implicit
+        // drag factor 1/(1 - dt R n)
+        const float nf = (float)nn, n3 = nf * nf * nf, d = (float)K.d50, od = (float)oden;
+        const float vx = (float)S.vx[i], vy = (float)S.vy[i];
+        const float vmag = sqrtf(vx * vx + vy * vy), sp = od - 1000.f;
+        const float mu = (1.002f + 0.001652f * sp + 0.0000083f * (sp * sp)) * 0.001f;
+        const float rn3 = sqrtf(n3);
+        S.resist[i] = (double)(-((mu / od) * (float)K.alpha * ((1.f - nf) * (1.f - nf)) / (n3 * (d * d))) -
+                               ((float)K.beta / rn3) * vmag * (1.f - nf) / (rn3 * d));
+    } else {
+        const double n3 = nn * nn * nn, d = K.d50;
+        const double vx = S.vx[i], vy = S.vy[i];
+        const double vmag = sqrt(vx * vx + vy * vy);
+        S.resist[i] = -((vis_of(oden) / oden) * K.alpha * ((1.0 - nn) * (1.0 - nn)) / (n3 * (d * d))) -
+                      ((K.beta / sqrt(n3)) * vmag * (1.0 - nn)) / (sqrt(n3) * d);
+    }
 }
 
 int op_effpor(Ctx* c) {
@@ -335,12 +348,15 @@ int op_effpor(Ctx* c) {
 }
 
 // per-particle quotients shared by the pair loops: u = v/n (eddyvis, int_vel)
-__global__ void k_vel_over_por(int64_t n, State S, double* __restrict__ ux, double* __restrict__ uy) {
+// (mixed path: also the FP32 twin of V)
+__global__ void k_vel_over_por(int64_t n, State S, double* __restrict__ ux, double* __restrict__ uy,
+                               float* __restrict__ f_vol) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double nn = S.por[i];
     ux[i] = S.vx[i] / nn;
     uy[i] = S.vy[i] / nn;
+    if (f_vol) f_vol[i] = (float)S.vol[i];
 }
 
 // ---- turbulence.f90:12-110 eddyvis -----------------------------------------------
@@ -348,7 +364,7 @@ template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                        const typename Vec2<R>::type* __restrict__ gw,
                                                        const int32_t* __restrict__ cnt, const double* __restrict__ ux,
-                                                       const double* __restrict__ uy) {
+                                                       const double* __restrict__ uy, const float* __restrict__ f_vol) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || S.tid[i] != BSC_TID_FLUID) return;
     const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
@@ -359,8 +375,12 @@ __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParam
         const int64_t e = ell(i, k, K.kmax);
         const int j = nbr[e];
         const auto g = gw[e];
-        const R vj = (R)S.vol[j];
-        const R du = (R)(ux[j] - uxi), dv = (R)(uy[j] - uyi);
+        R vj;
+        if constexpr (sizeof(R) == 4)
+            vj = f_vol[j];
+        else
+            vj = S.vol[j];
+        const R du = (R)(ux[j] - uxi), dv = (R)(uy[j] - uyi);  // differences in FP64: they cancel
         const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
         t1 += vj * du * gx;
         t2 += vj * dv * gy;
@@ -376,13 +396,13 @@ __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParam
 int op_eddyvis(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "eddyvis before neighbour");
     double *ux = c->r, *uy = c->rh;  // Krylov work vectors double as scratch outside the solve
-    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy);
+    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy, c->mixed ? c->f_vol : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
-        k_eddyvis<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy);
+        k_eddyvis<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy, c->f_vol);
     else
-        k_eddyvis<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy);
+        k_eddyvis<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy, nullptr);
     BSC_LAUNCH(c);
     return BSC_OK;
 }
@@ -393,7 +413,8 @@ template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_varts(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                      const typename Vec2<R>::type* __restrict__ gw,
                                                      const int32_t* __restrict__ cnt, const double* __restrict__ ux,
-                                                     const double* __restrict__ uy, const double* __restrict__ umax) {
+                                                     const double* __restrict__ uy, const double* __restrict__ umax,
+                                                     const float* __restrict__ f_vol, float* __restrict__ f_varts) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || !(S.flags[i] & BSC_FLAG_FREE)) return;
     const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
@@ -404,13 +425,19 @@ __global__ void __launch_bounds__(NB_BLOCK) k_varts(int64_t n, State S, KParams 
         const int64_t e = ell(i, k, K.kmax);
         const int j = nbr[e];
         const auto g = gw[e];
-        const R vj = (R)S.vol[j];
+        R vj;
+        if constexpr (sizeof(R) == 4)
+            vj = f_vol[j];
+        else
+            vj = S.vol[j];
         t1 += (R)(ux[j] - uxi) * (L0 * g.x + L1 * g.y) * vj;
         t2 += (R)(uy[j] - uyi) * (L2 * g.x + L3 * g.y) * vj;
     }
     const double T1 = t1, T2 = t2, vx = S.vx[i], vy = S.vy[i];
-    S.varts[i] = K.varts_ps * (K.dl * K.dl) * sqrt(T1 * T1 + T2 * T2) * sqrt(vx * vx + vy * vy) /
-                 ((*umax + (double)1e-6f) * S.por[i]);
+    const double va = K.varts_ps * (K.dl * K.dl) * sqrt(T1 * T1 + T2 * T2) * sqrt(vx * vx + vy * vy) /
+                      ((*umax + (double)1e-6f) * S.por[i]);
+    S.varts[i] = va;
+    if (f_varts) f_varts[i] = (float)va;
 }
 
 // pass 2: viscous (Morris, harmonic mu/oden), eddy viscosity, SPS k gradient,
@@ -419,9 +446,12 @@ template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                        const typename Vec2<R>::type* __restrict__ gw,
                                                        const int32_t* __restrict__ cnt,
-                                                       const double* __restrict__ nu, double dt) {
+                                                       const double* __restrict__ nu, double dt, const float* __restrict__ f_vol,
+                                                       const float* __restrict__ f_nu, const float* __restrict__ f_nut,
+                                                       const float* __restrict__ f_tke, const float* __restrict__ f_varts) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
+    constexpr bool F32 = sizeof(R) == 4;  // FP32 sums: the per-particle fields come from their FP32 twins
     const uint8_t fi = S.flags[i];
     if (S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD))) {
         const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
@@ -429,7 +459,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
         const R nui = (R)nu[i], nuti = (R)S.nut[i], tkei = (R)S.tke[i], ni = (R)S.por[i];
         const bool free_i = fi & BSC_FLAG_FREE;
         const R varts_i = (R)S.varts[i];
-        const R inv_w0 = (R)(1.0 / K.w0);
+        const R inv_w0 = (R)K.inv_w0;
         const R eps6 = (R)(double)1e-6f;
         R ax = 0, ay = 0;
         const int m = cnt[i];
@@ -440,40 +470,60 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
             const bool fluid_j = S.tid[j] == BSC_TID_FLUID;
             R cmu;
             if (fluid_j) {
-                const R nuj = (R)nu[j];
+                const R nuj = F32 ? (R)f_nu[j] : (R)nu[j];
                 cmu = (R)2 * nui * nuj / (nui + nuj);
             } else {
                 cmu = nui;
             }
             const double dx = xi - S.x[j], dy = yi - S.y[j];
+            // r^2 in R: from the rounded offsets on the FP32 path (the same
+            // accuracy as rounding the FP64 r^2, without the FP64 products)
+            R r2;
+            if constexpr (F32) {
+                const R fx = (R)dx, fy = (R)dy;
+                r2 = fx * fx + fy * fy;
+            } else {
+                r2 = dx * dx + dy * dy;
+            }
             R vart = 0;
             if (free_i) {
                 vart = varts_i;
             } else if ((S.flags[j] & BSC_FLAG_FREE) && !(fi & BSC_FLAG_BUFFER)) {
-                const R r = (R)sqrt(dx * dx + dy * dy);
-                vart = kern_w<R>(K, r) * (R)S.varts[j] * inv_w0;
+                R r;
+                if constexpr (F32)
+                    r = sqrtf(r2);
+                else
+                    r = sqrt(dx * dx + dy * dy);
+                vart = kern_w<R>(K, r) * (F32 ? (R)f_varts[j] : (R)S.varts[j]) * inv_w0;
             }
-            const R pvol = (R)S.vol[j];
-            const R p_dist = (R)1 / ((R)(dx * dx + dy * dy) + (R)K.lam);
+            const R pvol = F32 ? (R)f_vol[j] : (R)S.vol[j];
+            const R p_dist = (R)1 / (r2 + (R)K.lam);
             const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
             const R geo = (R)2 * pvol * ((R)dx * gx + (R)dy * gy) * p_dist;
-            const R dvx = (R)(vxi - S.vx[j]), dvy = (R)(vyi - S.vy[j]);
+            const R dvx = (R)(vxi - S.vx[j]), dvy = (R)(vyi - S.vy[j]);  // FP64 differences: they cancel
             R visc = cmu + vart;
             if (fluid_j) {
-                const R nutj = (R)S.nut[j];
+                const R nutj = F32 ? (R)f_nut[j] : (R)S.nut[j];
                 if (nuti < eps6 && nutj < eps6) visc += (nuti + nutj) * (R)0.5;
                 else visc += ((R)2 * nuti * nutj) / (nuti + nutj);
             }
             ax += geo * dvx * visc;
             ay += geo * dvy * visc;
             // SPS turbulence (:645-666)
-            const R dk = pvol * ((R)S.tke[j] - tkei);
+            const R dk = pvol * ((F32 ? (R)f_tke[j] : (R)S.tke[j]) - tkei);
             ax -= dk * gx * ni * (R)2 / (R)3;
             ay -= dk * gy * ni * (R)2 / (R)3;
         }
         const double nn = S.por[i], R_ = S.resist[i];
-        double vxs = (vxi + dt * (double)ax) / (1.0 - dt * R_ * nn);
-        double vys = (vyi + dt * (double)ay) / (1.0 - dt * R_ * nn);
+        double vxs, vys;
+        if constexpr (F32) {
+            const double inv = 1.0 / (1.0 - dt * R_ * nn);  // one FP64 division for both components
+            vxs = (vxi + dt * (double)ax) * inv;
+            vys = (vyi + dt * (double)ay) * inv;
+        } else {
+            vxs = (vxi + dt * (double)ax) / (1.0 - dt * R_ * nn);
+            vys = (vyi + dt * (double)ay) / (1.0 - dt * R_ * nn);
+        }
         vys = vys + K.g * nn * dt;
         S.vxs[i] = vxs;
         S.vys[i] = vys;
@@ -484,38 +534,60 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
     }
 }
 
-__global__ void k_kin_visc(int64_t n, State S, double* __restrict__ nu) {
+// nu = mu(oden)/oden; on the mixed path also the FP32 twins the pair sum reads
+__global__ void k_kin_visc(int64_t n, State S, double* __restrict__ nu, float* __restrict__ f_nu,
+                           float* __restrict__ f_nut, float* __restrict__ f_tke) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double o = S.oden[i];
-    nu[i] = vis_of(o) / o;
+    const double v = vis_of(o) / o;
+    nu[i] = v;
+    if (f_nu) {
+        f_nu[i] = (float)v;
+        f_nut[i] = (float)S.nut[i];
+        f_tke[i] = (float)S.tke[i];
+    }
 }
 
 int op_int_vel(Ctx* c, const double* d_umax) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "int_vel before neighbour");
     double *ux = c->r, *uy = c->rh, *nu = c->pd;
     const unsigned g = blocks_for(c->n, NB_BLOCK);
-    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy);
+    const bool mx = c->mixed;
+    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy, mx ? c->f_vol : nullptr);
     BSC_LAUNCH(c);
-    if (c->mixed)
-        k_varts<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy, d_umax);
+    if (mx)
+        k_varts<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy, d_umax,
+                                                      c->f_vol, c->f_varts);
     else
-        k_varts<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy, d_umax);
+        k_varts<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy, d_umax,
+                                                       nullptr, nullptr);
     BSC_LAUNCH(c);
-    k_kin_visc<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, nu);
+    k_kin_visc<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, nu, mx ? c->f_nu : nullptr,
+                                                             mx ? c->f_nut : nullptr, mx ? c->f_tke : nullptr);
     BSC_LAUNCH(c);
-    if (c->mixed)
-        k_int_vel<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, nu, c->dt);
+    if (mx)
+        k_int_vel<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, nu, c->dt,
+                                                        c->f_vol, c->f_nu, c->f_nut, c->f_tke, c->f_varts);
     else
-        k_int_vel<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, nu, c->dt);
+        k_int_vel<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, nu, c->dt,
+                                                         nullptr, nullptr, nullptr, nullptr, nullptr);
     BSC_LAUNCH(c);
     return BSC_OK;
 }
 
 // ---- integrator.f90:715-865 comp_vel (comp_pos is separate, cells.cu) ---------------
-__global__ void k_rho_over_por(int64_t n, State S, double* __restrict__ q) {
+// (mixed path: also the FP32 twins of q and V)
+__global__ void k_rho_over_por(int64_t n, State S, double* __restrict__ q, float* __restrict__ f_q,
+                               float* __restrict__ f_vol) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i < n) q[i] = S.rho[i] / S.por[i];
+    if (i >= n) return;
+    const double v = S.rho[i] / S.por[i];
+    q[i] = v;
+    if (f_q) {
+        f_q[i] = (float)v;
+        f_vol[i] = (float)S.vol[i];
+    }
 }
 
 template <typename R>
@@ -575,7 +647,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S,
                                                               const double2* __restrict__ gw,
                                                               const float2* __restrict__ gwf,
                                                               const int32_t* __restrict__ cnt,
-                                                              const double* __restrict__ q, double dt) {
+                                                              const float* __restrict__ f_q,
+                                                              const float* __restrict__ f_vol, double dt) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint8_t fi = S.flags[i];
@@ -583,7 +656,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S,
         const double L0 = S.L0[i], L1 = S.L1[i], L2 = S.L2[i], L3 = S.L3[i];
         const float L0f = (float)L0, L1f = (float)L1, L2f = (float)L2, L3f = (float)L3;
         const double pi = S.p[i];
-        const float qi = (float)q[i];
+        const float qi = f_q[i];
         double sx = 0.0, sy = 0.0;
         float ax = 0.f, ay = 0.f;
         const int m = cnt[i];
@@ -595,8 +668,9 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S,
             const double vj = S.vol[j];
             sx += vj * (L0 * g.x + L1 * g.y);
             sy += vj * (L2 * g.x + L3 * g.y);
-            const float w = (S.tid[j] == BSC_TID_FLUID) ? 2.f * (float)vj * qi / (qi + (float)q[j]) : (float)vj;
-            const float dp = (float)(S.p[j] - pi);
+            const float vjf = f_vol[j];
+            const float w = (S.tid[j] == BSC_TID_FLUID) ? 2.f * vjf * qi / (qi + f_q[j]) : vjf;
+            const float dp = (float)(S.p[j] - pi);  // FP64 difference: pressures cancel
             ax += w * dp * (L0f * gf.x + L1f * gf.y);
             ay += w * dp * (L2f * gf.x + L3f * gf.y);
         }
@@ -619,11 +693,13 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S,
 int op_comp_vel(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "comp_vel before neighbour");
     double* q = c->r;
-    k_rho_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, q);
+    k_rho_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, q, c->mixed ? c->f_q : nullptr,
+                                                                 c->mixed ? c->f_vol : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
-        k_comp_vel_mixed<<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->gwf, c->cnt, q, c->dt);
+        k_comp_vel_mixed<<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->gwf, c->cnt, c->f_q,
+                                                        c->f_vol, c->dt);
     else
         k_comp_vel<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, q, c->dt);
     BSC_LAUNCH(c);
