@@ -421,6 +421,7 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
     if (const char* e = std::getenv("BSC_SPMV_UNROLL")) c->spmv_unroll = e[0] == '1';
     if (const char* e = std::getenv("BSC_PROFILE_ITER")) c->prof_iter = e[0] == '1';
     if (const char* e = std::getenv("BSC_MG_TAIL")) c->mg_tail_cells = std::atoi(e);
+    if (const char* e = std::getenv("BSC_EXACT_DIV")) c->exact_div = e[0] == '1';
     for (int k = 0; k < 6; ++k) cudaEventCreate(&c->ev_it[k]);
     for (int k = 0; k < 2; ++k) cudaEventCreateWithFlags(&c->ev_lag[k], cudaEventDisableTiming);
     *out = c;
@@ -782,13 +783,9 @@ int bsc_export_csr(bsc_ctx* c, int64_t* rowptr, int32_t* col, double* val, doubl
     std::vector<int32_t> nb(slots);
     std::vector<double> v(slots);
     BSC_D2H(c, nb.data(), c->nbr, sizeof(int32_t) * slots);
-    if (c->mixed) {
-        std::vector<float> vf(slots);
-        BSC_D2H(c, vf.data(), c->avalf, sizeof(float) * slots);
-        for (int64_t e = 0; e < slots; ++e) v[e] = vf[e];
-    } else {
-        BSC_D2H(c, v.data(), c->aval, sizeof(double) * slots);
-    }
+    // the FP64 system on both paths (the mixed path's outer refinement
+    // solves it; its FP32 and FP16 copies only serve the inner sweeps)
+    BSC_D2H(c, v.data(), c->aval, sizeof(double) * slots);
     std::vector<std::pair<int32_t, double>> row;
     for (int64_t q = 0; q < n; ++q) {
         const int64_t k = slot_of[q];

@@ -56,6 +56,19 @@ struct Scalars {
     int32_t done, breakdown, it, k5;  // k5: work of the last kernel of a BiCGSTAB iteration
 };
 
+// 1/x by one Newton-Raphson step for the reciprocal, y1 = y0 (2 - x y0), from
+// y0 = the FP32 reciprocal of x rounded to FP32.  y0 is within 2^-23 of 1/x
+// (two FP32 roundings), so y1 is within about 2^-46 (the step squares the
+// relative error) plus FP64 rounding.  Costs two conversions and two FMAs on
+// the FP64 pipe instead of a full FP64 division.  Outside the normal FP32
+// range (and for NaN) it returns the FP64 quotient.
+__device__ __forceinline__ double rcp_nr(double x) {
+    const float xf = (float)x;
+    if (!(fabsf(xf) >= 1.2e-38f && fabsf(xf) <= 1.7e38f)) return 1.0 / x;
+    const double y0 = (double)__frcp_rn(xf);
+    return fma(y0, fma(-x, y0, 1.0), y0);
+}
+
 // an FGMRES cycle has stopped (converged, broken down or at its restart
 // length): the kernels of iterations queued past that point return at once
 __device__ __forceinline__ bool fg_skip(const Scalars* sc) { return sc->done || sc->tmp[2] != 0.0; }
@@ -240,6 +253,7 @@ struct Ctx {
     int spmv_unroll = 1;          // four ELL entries per round (BSC_SPMV_UNROLL=0: one)
     bool prof_iter = false;       // BSC_PROFILE_ITER=1: events around each Krylov kernel
     int mg_tail_cells = -1;       // BSC_MG_TAIL=<cells>: largest level in the single-CTA tail
+    bool exact_div = false;       // BSC_EXACT_DIV=1: IEEE divisions in the mixed path's FP64 assembly
     cudaEvent_t ev_it[6] = {};
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64
     float* Vf = nullptr;          // FGMRES basis FP32 (mixed)

@@ -33,7 +33,10 @@ namespace bsc {
 // ============================================================================
 // assembly
 // ============================================================================
-template <typename R>
+// FAST (the mixed path): the per-pair and per-row quotients by rcp_nr, a
+// Newton-Raphson reciprocal within ~2^-46 of the FP64 quotient.  The FP64
+// path divides (correctly rounded, as the reference).
+template <typename R, bool FAST>
 __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                         const typename Vec2<R>::type* __restrict__ gw,
                                                         const int32_t* __restrict__ cnt, R* __restrict__ aval,
@@ -49,12 +52,13 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
     const R ni = (R)S.por[i], qi = (R)q[i];
     const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
     const double usxi = usx[i], usyi = usy[i];
-    const R mi_over_rhoi = (R)(S.mass[i] / S.rho[i]);
+    auto quot = [](double a, double d) -> double { return FAST ? a * rcp_nr(d) : a / d; };
+    const R mi_over_rhoi = (R)quot(S.mass[i], S.rho[i]);
     const R lamp_f = (R)(1.0 / (K.rho0 * K.rel_den));
     // per-row quotients hoisted out of the pair loop (FP64 divisions are
     // expensive on this GPU): 1/n_i, and v*_i/n_i for the fixed-wall rows
-    const R inv_ni = (R)1 / ni;
-    const double vxi_n = S.vxs[i] / (double)ni, vyi_n = S.vys[i] / (double)ni;
+    const R inv_ni = (R)quot(1.0, ni);
+    const double vxi_n = quot(S.vxs[i], (double)ni), vyi_n = quot(S.vys[i], (double)ni);
     const int m = cnt[i];
     R dia = 0, fv = 0;
     for (int k = 0; k < m; ++k) {
@@ -63,7 +67,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
         const auto g = gw[e];
         const int tid_j = S.tid[j];
         const double dx = xi - S.x[j], dy = yi - S.y[j];
-        const R p_dist = (R)1 / ((R)(dx * dx + dy * dy) + (R)K.lam);
+        const R p_dist = (R)quot(1.0, (R)(dx * dx + dy * dy) + (R)K.lam);
         const R pvol = (R)S.vol[j];
         R val = 0;
         if (tid_i == BSC_TID_FLUID) {
@@ -77,7 +81,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
             if (tid_j == BSC_TID_FLUID) {
                 // 2 rho_i rho_j / (n_i n_j (rho_i/n_i + rho_j/n_j)) = 2 q_i q_j / (q_i + q_j)
                 const R qj = (R)q[j];
-                const R rho_ij = (R)2 * qi * qj / (qi + qj);
+                const R rho_ij = (R)quot((R)2 * qi * qj, qi + qj);
                 ddx = rho_ij * (R)(usx[j] - usxi);
                 ddy = rho_ij * (R)(usy[j] - usyi);
             } else {
@@ -151,9 +155,13 @@ int op_ppe_assemble(Ctx* c) {
     // FP64 assembly in both paths: the PPE coefficients are sums whose FP32
     // rounding moves the pressure by ~5e-6 (relative) at 1e-8 residual; the
     // mixed path keeps an FP32 copy for its inner sweeps
-    k_assemble<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
-                                                      c->mixed ? c->avalf : nullptr, c->mixed ? c->avalh : nullptr, c->b, q, ux,
-                                                      uy, c->dt);
+    if (c->mixed && !c->exact_div)
+        k_assemble<double, true><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
+                                                                c->avalf, c->avalh, c->b, q, ux, uy, c->dt);
+    else
+        k_assemble<double, false><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
+                                                                 c->mixed ? c->avalf : nullptr,
+                                                                 c->mixed ? c->avalh : nullptr, c->b, q, ux, uy, c->dt);
     BSC_LAUNCH(c);
     c->have_csr = true;
     return BSC_OK;
