@@ -572,36 +572,51 @@ __global__ void __launch_bounds__(RED_BLOCK) k_fg_maxpy(int64_t n, const T* __re
 
 // h(j+1,j) = ||w||; Givens; residual estimate; cycle/convergence control
 __device__ void fg_givens(const double* __restrict__ part, Scalars* sc, double* Hd, FgLayout F, int j) {
+    // the column and the earlier rotations are staged in shared memory by
+    // all threads; one thread then applies the rotations (a serial chain
+    // that would otherwise wait on global memory at every step)
+    __shared__ double hcol[FG_MAXM + 1], csv[FG_MAXM], snv[FG_MAXM];
     double v[1];
     reduce_partials<1>(part, v);
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    const double hn = sqrt(v[0]);
-    Hd[F.H(j + 1, j)] = hn;
-    for (int i = 0; i < j; ++i) {
-        const double a = Hd[F.H(i, j)], c = Hd[F.H(i + 1, j)];
-        Hd[F.H(i, j)] = Hd[F.cs(i)] * a + Hd[F.sn(i)] * c;
-        Hd[F.H(i + 1, j)] = -Hd[F.sn(i)] * a + Hd[F.cs(i)] * c;
+    const int t = threadIdx.x;
+    for (int i = t; i <= j; i += blockDim.x) hcol[i] = Hd[F.H(i, j)];
+    for (int i = t; i < j; i += blockDim.x) {
+        csv[i] = Hd[F.cs(i)];
+        snv[i] = Hd[F.sn(i)];
     }
-    const double a = Hd[F.H(j, j)], c = Hd[F.H(j + 1, j)];
-    const double den = sqrt(a * a + c * c);
-    sc->it += 1;
-    sc->tmp[1] = (double)(j + 1);
-    if (den == 0.0) {
-        sc->breakdown = 1;
-        sc->tmp[1] = (double)j;
-        sc->tmp[2] = 1.0;
-        return;
+    __syncthreads();
+    if (t == 0) {
+        const double hn = sqrt(v[0]);
+        hcol[j + 1] = hn;
+        for (int i = 0; i < j; ++i) {
+            const double a = hcol[i], c = hcol[i + 1];
+            hcol[i] = csv[i] * a + snv[i] * c;
+            hcol[i + 1] = -snv[i] * a + csv[i] * c;
+        }
+        const double a = hcol[j], c = hcol[j + 1];
+        const double den = sqrt(a * a + c * c);
+        sc->it += 1;
+        sc->tmp[1] = (double)(j + 1);
+        if (den == 0.0) {
+            sc->breakdown = 1;
+            sc->tmp[1] = (double)j;
+            sc->tmp[2] = 1.0;
+        } else {
+            const double cs = a / den, sn = c / den;
+            Hd[F.cs(j)] = cs;
+            Hd[F.sn(j)] = sn;
+            hcol[j] = den;
+            hcol[j + 1] = 0.0;
+            const double gj = Hd[F.g(j)];
+            const double gn = -sn * gj;
+            Hd[F.g(j + 1)] = gn;
+            Hd[F.g(j)] = cs * gj;
+            sc->tmp[3] = hn;  // scale of v_{j+1}
+            if (fabs(gn) <= sc->target || hn == 0.0 || j + 1 == F.m) sc->tmp[2] = 1.0;
+        }
     }
-    const double cs = a / den, sn = c / den;
-    Hd[F.cs(j)] = cs;
-    Hd[F.sn(j)] = sn;
-    Hd[F.H(j, j)] = den;
-    Hd[F.H(j + 1, j)] = 0.0;
-    const double gj = Hd[F.g(j)];
-    Hd[F.g(j + 1)] = -sn * gj;
-    Hd[F.g(j)] = cs * gj;
-    sc->tmp[3] = hn;  // scale of v_{j+1}
-    if (fabs(Hd[F.g(j + 1)]) <= sc->target || hn == 0.0 || j + 1 == F.m) sc->tmp[2] = 1.0;
+    __syncthreads();
+    for (int i = t; i <= j + 1; i += blockDim.x) Hd[F.H(i, j)] = hcol[i];
 }
 
 // `mirror` (pinned host memory, optional) receives the scalars after this
