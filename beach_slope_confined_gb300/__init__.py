@@ -71,6 +71,20 @@ def default_params(dl: float) -> Params:
     return p
 
 
+def selftest(n: int = 1 << 22):
+    """bsc_selftest: (FP32 rounding mismatches, largest FP32 ulp difference,
+    largest relative error of the Newton-Raphson reciprocal) over n inputs."""
+    f = lib().bsc_selftest
+    f.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                  ctypes.POINTER(ctypes.c_double)]
+    f.restype = ctypes.c_int
+    a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+    rc = f(int(n), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    if rc:
+        raise BscError(rc, "selftest", "")
+    return a.value, b.value, c.value
+
+
 def measure_peaks():
     """(FP64 GFLOP/s, FP32 GFLOP/s, copy GB/s) measured on the current GPU."""
     a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

@@ -69,6 +69,20 @@ __device__ __forceinline__ double rcp_nr(double x) {
     return fma(y0, fma(-x, y0, 1.0), y0);
 }
 
+// FP64 -> FP32 on the integer pipe: round to nearest (ties away from zero)
+// by adding half an FP32 ulp to the bit pattern, then repacking exponent and
+// mantissa.  For finite |v| below 2^127; magnitudes below FP32's normal
+// range become signed zeros.  The hardware conversion issues on the FP64
+// pipe, this GPU's scarce resource; this is a dozen integer operations.
+__device__ __forceinline__ float f32_of(double v) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v) + (1ull << 28);
+    const unsigned hi = (unsigned)(b >> 32), lo = (unsigned)b;
+    const int e = (int)((hi >> 20) & 0x7ffu) - 896;  // FP64 bias 1023 -> FP32 bias 127
+    const unsigned sign = hi & 0x80000000u;
+    const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
+    return __uint_as_float(e > 0 ? (sign | ((unsigned)e << 23) | m) : sign);
+}
+
 // an FGMRES cycle has stopped (converged, broken down or at its restart
 // length): the kernels of iterations queued past that point return at once
 __device__ __forceinline__ bool fg_skip(const Scalars* sc) { return sc->done || sc->tmp[2] != 0.0; }

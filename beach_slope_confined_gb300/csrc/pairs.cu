@@ -80,12 +80,15 @@ __device__ __forceinline__ bool pre_ok(float2 p, float csf) {
     return fabsf(p.x) < PRE_GUARD * csf && fabsf(p.y) < PRE_GUARD * csf;
 }
 
+// (mixed path: also the FP32 twin of V for the neighbour search's M sum)
 __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
-                       const int32_t* __restrict__ pcell, KParams K, float2* __restrict__ posf) {
+                       const int32_t* __restrict__ pcell, KParams K, float2* __restrict__ posf,
+                       const double* __restrict__ vol, float* __restrict__ f_vol) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
     posf[i] = make_float2((float)(x[i] - (K.gx0 + cx * K.cs)), (float)(y[i] - (K.gy0 + cy * K.cs)));
+    if (f_vol) f_vol[i] = (float)vol[i];
 }
 
 // ---- search.f90:13-399 neighbour / nsearch2 ----------------------------------------
@@ -97,7 +100,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                                                          const int32_t* __restrict__ pcell,
                                                          const float2* __restrict__ posf,
                                                          int32_t* __restrict__ nbr, double2* __restrict__ gw,
-                                                         float2* __restrict__ gwf,
+                                                         float2* __restrict__ gwf, const float* __restrict__ f_vol,
                                                          int32_t* __restrict__ cnt, int32_t* __restrict__ flag) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -120,16 +123,20 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
         // pair sums of the mixed path); the M sum runs in R
         const double F = grad_factor<double>(K, r);
         const double gx64 = F * dx, gy64 = F * dy;
-        const R gx = (R)gx64, gy = (R)gy64;
+        // the FP32 path's values come from the integer-pipe rounding (f32_of)
+        // and the FP32 twin of V: no per-pair conversion on the FP64 pipe
+        constexpr bool F32 = sizeof(R) == 4;
+        const R gx = F32 ? (R)f32_of(gx64) : (R)gx64, gy = F32 ? (R)f32_of(gy64) : (R)gy64;
         if (count < K.kmax) {
             const int64_t e = ell(i, count, K.kmax);
             nbr[e] = j;
             gw[e] = {gx64, gy64};
-            if (gwf) gwf[e] = {(float)gx64, (float)gy64};
+            if (gwf) gwf[e] = {(float)gx, (float)gy};
         }
         ++count;
-        const R vj = (R)S.vol[j];
-        const R rx = -vj * (R)dx, ry = -vj * (R)dy;  // m_j (x_j - x_i) / rho_j
+        const R vj = F32 ? (R)f_vol[j] : (R)S.vol[j];
+        const R fdx = F32 ? (R)f32_of(dx) : (R)dx, fdy = F32 ? (R)f32_of(dy) : (R)dy;
+        const R rx = -vj * fdx, ry = -vj * fdy;  // m_j (x_j - x_i) / rho_j
         m0 += gx * rx;
         m1 += gy * rx;
         m2 += gx * ry;
@@ -214,17 +221,18 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
 }
 
 int op_neighbour(Ctx* c) {
-    k_posf<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S.x, c->S.y, c->pcell, c->K, c->posf);
+    k_posf<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S.x, c->S.y, c->pcell, c->K, c->posf, c->S.vol,
+                                                         c->mixed ? c->f_vol : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
         k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
-                                                          c->pcell, c->posf, c->nbr, c->gw, c->gwf, c->cnt,
+                                                          c->pcell, c->posf, c->nbr, c->gw, c->gwf, c->f_vol, c->cnt,
                                                           c->d_flag);
     else
         k_neighbour<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count,
                                                            c->sorted, c->pcell, c->posf, c->nbr, c->gw, nullptr,
-                                                           c->cnt, c->d_flag);
+                                                           nullptr, c->cnt, c->d_flag);
     BSC_LAUNCH(c);
     c->have_lists = true;
     return BSC_OK;
@@ -380,7 +388,9 @@ __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParam
             vj = f_vol[j];
         else
             vj = S.vol[j];
-        const R du = (R)(ux[j] - uxi), dv = (R)(uy[j] - uyi);  // differences in FP64: they cancel
+        // differences in FP64 (they cancel), rounded on the integer pipe for R = float
+        const R du = sizeof(R) == 4 ? (R)f32_of(ux[j] - uxi) : (R)(ux[j] - uxi);
+        const R dv = sizeof(R) == 4 ? (R)f32_of(uy[j] - uyi) : (R)(uy[j] - uyi);
         const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
         t1 += vj * du * gx;
         t2 += vj * dv * gy;
@@ -430,8 +440,10 @@ __global__ void __launch_bounds__(NB_BLOCK) k_varts(int64_t n, State S, KParams 
             vj = f_vol[j];
         else
             vj = S.vol[j];
-        t1 += (R)(ux[j] - uxi) * (L0 * g.x + L1 * g.y) * vj;
-        t2 += (R)(uy[j] - uyi) * (L2 * g.x + L3 * g.y) * vj;
+        const R du = sizeof(R) == 4 ? (R)f32_of(ux[j] - uxi) : (R)(ux[j] - uxi);
+        const R dv = sizeof(R) == 4 ? (R)f32_of(uy[j] - uyi) : (R)(uy[j] - uyi);
+        t1 += du * (L0 * g.x + L1 * g.y) * vj;
+        t2 += dv * (L2 * g.x + L3 * g.y) * vj;
     }
     const double T1 = t1, T2 = t2, vx = S.vx[i], vy = S.vy[i];
     const double va = K.varts_ps * (K.dl * K.dl) * sqrt(T1 * T1 + T2 * T2) * sqrt(vx * vx + vy * vy) /
@@ -476,15 +488,15 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
                 cmu = nui;
             }
             const double dx = xi - S.x[j], dy = yi - S.y[j];
-            // r^2 in R: from the rounded offsets on the FP32 path (the same
-            // accuracy as rounding the FP64 r^2, without the FP64 products)
+            // on the FP32 path: offsets rounded on the integer pipe (f32_of),
+            // r^2 from them (the accuracy of rounding the FP64 r^2, without
+            // the FP64 products)
+            const R fx = F32 ? (R)f32_of(dx) : (R)dx, fy = F32 ? (R)f32_of(dy) : (R)dy;
             R r2;
-            if constexpr (F32) {
-                const R fx = (R)dx, fy = (R)dy;
+            if constexpr (F32)
                 r2 = fx * fx + fy * fy;
-            } else {
+            else
                 r2 = dx * dx + dy * dy;
-            }
             R vart = 0;
             if (free_i) {
                 vart = varts_i;
@@ -499,8 +511,10 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
             const R pvol = F32 ? (R)f_vol[j] : (R)S.vol[j];
             const R p_dist = (R)1 / (r2 + (R)K.lam);
             const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
-            const R geo = (R)2 * pvol * ((R)dx * gx + (R)dy * gy) * p_dist;
-            const R dvx = (R)(vxi - S.vx[j]), dvy = (R)(vyi - S.vy[j]);  // FP64 differences: they cancel
+            const R geo = (R)2 * pvol * (fx * gx + fy * gy) * p_dist;
+            // FP64 differences (they cancel), then rounded
+            const R dvx = F32 ? (R)f32_of(vxi - S.vx[j]) : (R)(vxi - S.vx[j]);
+            const R dvy = F32 ? (R)f32_of(vyi - S.vy[j]) : (R)(vyi - S.vy[j]);
             R visc = cmu + vart;
             if (fluid_j) {
                 const R nutj = F32 ? (R)f_nut[j] : (R)S.nut[j];
@@ -670,7 +684,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S,
             sy += vj * g.y;
             const float vjf = f_vol[j];
             const float w = (S.tid[j] == BSC_TID_FLUID) ? 2.f * vjf * qi / (qi + f_q[j]) : vjf;
-            const float dp = (float)(S.p[j] - pi);  // FP64 difference: pressures cancel
+            const float dp = f32_of(S.p[j] - pi);  // FP64 difference (pressures cancel), rounded on the integer pipe
             ax += w * dp * (L0f * gf.x + L1f * gf.y);
             ay += w * dp * (L2f * gf.x + L3f * gf.y);
         }

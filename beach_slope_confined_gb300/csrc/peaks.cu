@@ -7,8 +7,9 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 
-#include "../../include/bsc.h"
+#include "bsc_internal.cuh"
 
 namespace {
 
@@ -103,4 +104,59 @@ extern "C" int bsc_measure_peaks(double* fp64_gflops, double* fp32_gflops, doubl
     if (fp32_gflops) *fp32_gflops = fma_gflops<float>(sms);
     if (copy_bw) *copy_bw = copy_gbs(sms);
     return cudaGetLastError() == cudaSuccess ? BSC_OK : BSC_E_CUDA;
+}
+
+// ---- self-test of the device arithmetic helpers -----------------------------------
+namespace {
+
+// deterministic inputs: sign, mantissa in [1, 2) and exponent in [-100, 100]
+// from a hash of the index
+__device__ double selftest_value(unsigned long long k) {
+    unsigned long long h = k * 0x9E3779B97F4A7C15ull;
+    h ^= h >> 31;
+    h *= 0xBF58476D1CE4E5B9ull;
+    h ^= h >> 29;
+    const double m = 1.0 + (double)(h >> 11) * (1.0 / 9007199254740992.0);
+    const int e = (int)((h >> 3) % 201) - 100;
+    return ((h & 1) ? -m : m) * exp2((double)e);
+}
+
+__global__ void k_selftest(long long n, unsigned long long* res) {
+    unsigned long long mism = 0, ulp = 0, rel = 0;
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
+         k += (long long)gridDim.x * blockDim.x) {
+        const double x = selftest_value((unsigned long long)k);
+        const float a = bsc::f32_of(x), b = __double2float_rn(x);
+        const int d = abs((int)(__float_as_uint(a) & 0x7fffffffu) - (int)(__float_as_uint(b) & 0x7fffffffu));
+        if (__float_as_uint(a) != __float_as_uint(b)) ++mism;
+        ulp = max(ulp, (unsigned long long)d);
+        const double r = fabs(fma(bsc::rcp_nr(x), x, -1.0));  // relative error of 1/x
+        rel = max(rel, (unsigned long long)__double_as_longlong(r));
+    }
+    atomicAdd(&res[0], mism);
+    atomicMax(&res[1], ulp);
+    atomicMax(&res[2], rel);
+}
+
+}  // namespace
+
+extern "C" int bsc_selftest(int64_t n, int64_t* f32_mismatches, int64_t* f32_max_ulp, double* rcp_max_rel) {
+    if (n <= 0 || !f32_mismatches || !f32_max_ulp || !rcp_max_rel) return BSC_E_INVALID;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return BSC_E_NOT_BUILT;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    unsigned long long* res = nullptr;
+    if (cudaMalloc(&res, 3 * sizeof(unsigned long long)) != cudaSuccess) return BSC_E_NOMEM;
+    unsigned long long h[3] = {0, 0, 0};
+    cudaMemcpy(res, h, sizeof h, cudaMemcpyHostToDevice);
+    k_selftest<<<sms * 8, 256>>>((long long)n, res);
+    cudaMemcpy(h, res, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(res);
+    if (cudaGetLastError() != cudaSuccess) return BSC_E_CUDA;
+    *f32_mismatches = (int64_t)h[0];
+    *f32_max_ulp = (int64_t)h[1];
+    double r;
+    std::memcpy(&r, &h[2], sizeof r);
+    *rcp_max_rel = r;
+    return BSC_OK;
 }

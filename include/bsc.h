@@ -276,6 +276,12 @@ int bsc_csr_solve_noalloc(const bsc_params* p, int32_t n, const int32_t* rowptr,
 /* Measured FP64 and FP32 FMA throughput (GFLOP/s, 2 flops per FMA) and a
  * device-to-device copy bandwidth (GB/s, read+write) on the current device. */
 int bsc_measure_peaks(double* fp64_gflops, double* fp32_gflops, double* copy_gbs);
+/* Self-test of the device arithmetic the mixed path uses in place of FP64
+ * instructions, over n hashed inputs (|x| in 2^[-100,101]): the integer-pipe
+ * FP64->FP32 rounding against the hardware conversion (inputs that differ,
+ * largest difference in FP32 ulps) and the Newton-Raphson reciprocal (largest
+ * |x r(x) - 1|). */
+int bsc_selftest(int64_t n, int64_t* f32_mismatches, int64_t* f32_max_ulp, double* rcp_max_rel);
 
 #ifdef __cplusplus
 }

@@ -50,3 +50,17 @@ def test_newton_reciprocal_assembly_matches_division():
     assert np.linalg.norm(rhs_a - rhs_b) <= 1e-11 * np.linalg.norm(rhs_b)
     # the switch selects a different code path: some entries differ in the last bits
     assert not np.array_equal(val_a, val_b)
+
+
+def test_device_arithmetic_selftest():
+    """f32_of (FP64 -> FP32 rounding on the integer pipe) against the
+    hardware conversion: at most one FP32 ulp apart, and apart only on exact
+    ties (rounded away from zero, not to even); rcp_nr within 2^-44."""
+    from beach_slope_confined_gb300 import selftest
+
+    n = 1 << 22
+    mism, max_ulp, rcp_rel = selftest(n)
+    print("f32_of mismatches", mism, "max ulp", max_ulp, "rcp_nr max rel", rcp_rel)
+    assert max_ulp <= 1
+    assert mism <= n * 1e-4
+    assert rcp_rel < 2.0 ** -44
