@@ -56,19 +56,6 @@ struct Scalars {
     int32_t done, breakdown, it, k5;  // k5: work of the last kernel of a BiCGSTAB iteration
 };
 
-// 1/x by one Newton-Raphson step for the reciprocal, y1 = y0 (2 - x y0), from
-// y0 = the FP32 reciprocal of x rounded to FP32.  y0 is within 2^-23 of 1/x
-// (two FP32 roundings), so y1 is within about 2^-46 (the step squares the
-// relative error) plus FP64 rounding.  Costs two conversions and two FMAs on
-// the FP64 pipe instead of a full FP64 division.  Outside the normal FP32
-// range (and for NaN) it returns the FP64 quotient.
-__device__ __forceinline__ double rcp_nr(double x) {
-    const float xf = (float)x;
-    if (!(fabsf(xf) >= 1.2e-38f && fabsf(xf) <= 1.7e38f)) return 1.0 / x;
-    const double y0 = (double)__frcp_rn(xf);
-    return fma(y0, fma(-x, y0, 1.0), y0);
-}
-
 // FP64 -> FP32 on the integer pipe: round to nearest (ties away from zero)
 // by adding half an FP32 ulp to the bit pattern, then repacking exponent and
 // mantissa.  For finite |v| below 2^127; magnitudes below FP32's normal
@@ -81,6 +68,37 @@ __device__ __forceinline__ float f32_of(double v) {
     const unsigned sign = hi & 0x80000000u;
     const unsigned m = ((hi & 0xfffffu) << 3) | (lo >> 29);
     return __uint_as_float(e > 0 ? (sign | ((unsigned)e << 23) | m) : sign);
+}
+
+// FP32 -> FP64 on the integer pipe (exact), for normal FP32 values
+__device__ __forceinline__ double f64_of(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned hi = (u & 0x80000000u) | ((((u >> 23) & 0xffu) + 896u) << 20) | ((u & 0x7fffffu) >> 3);
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// an FP64 value in the pair arithmetic's type R: the integer-pipe rounding
+// for R = float, unchanged for R = double
+template <typename R>
+__device__ __forceinline__ R to_r(double v) {
+    if constexpr (sizeof(R) == 4)
+        return f32_of(v);
+    else
+        return v;
+}
+
+// 1/x by one Newton-Raphson step for the reciprocal, y1 = y0 (2 - x y0), from
+// y0 = the FP32 reciprocal of x rounded to FP32.  y0 is within 2^-23 of 1/x
+// (two FP32 roundings), so y1 is within about 2^-46 (the step squares the
+// relative error) plus FP64 rounding.  The conversions run on the integer
+// pipe (f32_of, f64_of): two FMAs on the FP64 pipe instead of a full FP64
+// division.  For |x| outside [2^-125, 2^126) (and NaN, infinities) it
+// returns the FP64 quotient.
+__device__ __forceinline__ double rcp_nr(double x) {
+    const int ex = (int)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ff;
+    if (ex < 1023 - 125 || ex > 1023 + 125) return 1.0 / x;
+    const double y0 = f64_of(__frcp_rn(f32_of(x)));
+    return fma(y0, fma(-x, y0, 1.0), y0);
 }
 
 // an FGMRES cycle has stopped (converged, broken down or at its restart

@@ -375,7 +375,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParam
                                                        const double* __restrict__ uy, const float* __restrict__ f_vol) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || S.tid[i] != BSC_TID_FLUID) return;
-    const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+    const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
     const double uxi = ux[i], uyi = uy[i];
     R t1 = 0, t2 = 0, t3 = 0;
     const int m = cnt[i];
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_varts(int64_t n, State S, KParams 
                                                      const float* __restrict__ f_vol, float* __restrict__ f_varts) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || !(S.flags[i] & BSC_FLAG_FREE)) return;
-    const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+    const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
     const double uxi = ux[i], uyi = uy[i];
     R t1 = 0, t2 = 0;
     const int m = cnt[i];
@@ -466,11 +466,11 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
     constexpr bool F32 = sizeof(R) == 4;  // FP32 sums: the per-particle fields come from their FP32 twins
     const uint8_t fi = S.flags[i];
     if (S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD))) {
-        const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+        const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
         const double xi = S.x[i], yi = S.y[i], vxi = S.vx[i], vyi = S.vy[i];
-        const R nui = (R)nu[i], nuti = (R)S.nut[i], tkei = (R)S.tke[i], ni = (R)S.por[i];
+        const R nui = to_r<R>(nu[i]), nuti = to_r<R>(S.nut[i]), tkei = to_r<R>(S.tke[i]), ni = to_r<R>(S.por[i]);
         const bool free_i = fi & BSC_FLAG_FREE;
-        const R varts_i = (R)S.varts[i];
+        const R varts_i = to_r<R>(S.varts[i]);
         const R inv_w0 = (R)K.inv_w0;
         const R eps6 = (R)(double)1e-6f;
         R ax = 0, ay = 0;
@@ -613,7 +613,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel(int64_t n, State S, KPara
     if (i >= n) return;
     const uint8_t fi = S.flags[i];
     if (S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD))) {
-        const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+        const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
         const R ni = (R)S.por[i], rhoi = (R)S.rho[i], pi = (R)S.p[i], qi = (R)q[i];
         const R c0 = ni * ni / rhoi;
         R wgx = 0, wgy = 0;  // sums of w grad W; the row's L is applied after them
@@ -668,7 +668,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S,
     const uint8_t fi = S.flags[i];
     if (S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD))) {
         const double L0 = S.L0[i], L1 = S.L1[i], L2 = S.L2[i], L3 = S.L3[i];
-        const float L0f = (float)L0, L1f = (float)L1, L2f = (float)L2, L3f = (float)L3;
+        const float L0f = f32_of(L0), L1f = f32_of(L1), L2f = f32_of(L2), L3f = f32_of(L3);
         const double pi = S.p[i];
         const float qi = f_q[i];
         double sx = 0.0, sy = 0.0;
@@ -737,7 +737,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_shift(int64_t n, State S, KParams 
     if (!(S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD)))) return;
     const int m = cnt[i];
     if (m == 0) return;
-    const R L0 = (R)S.L0[i], L1 = (R)S.L1[i], L2 = (R)S.L2[i], L3 = (R)S.L3[i];
+    const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
     const double vxi = S.vx[i], vyi = S.vy[i];
     // the corrected gradient L grad W enters linearly and L is the row's own,
     // so L is applied once to the four sums of grad W (dv V) rather than per

@@ -130,8 +130,11 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
         const int64_t e = ell(i, k, K.kmax);
         const R v = aval[e] * inv;
         aval[e] = v;
-        if (avalf) avalf[e] = (float)v;  // the mixed path's inner-sweep copy
-        if (avalh) avalh[e] = __float2half_rn((float)v);  // and its V-cycle copy
+        if (avalf) {  // the mixed path's inner-sweep copy (rounded on the integer pipe) and V-cycle copy
+            const float vf = f32_of(v);
+            avalf[e] = vf;
+            avalh[e] = __float2half_rn(vf);
+        }
     }
     b[i] = ((double)fv / dt) / d;
 }
