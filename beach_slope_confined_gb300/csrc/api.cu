@@ -381,7 +381,7 @@ int bsc_default_params(bsc_params* p, double dl) {
     p->max_neighbors = 64;
     p->reorder_every = 20;
     p->precond = BSC_PRECOND_NONE;
-    p->mg_omega = 0.9;
+    p->mg_omega = 0.82;
     p->mg_scale = 1.8;
     p->mg_sweeps = 2;
     p->mg_coarse_max = MG_COARSE_MAX;
@@ -421,6 +421,13 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
     if (const char* e = std::getenv("BSC_SPMV_UNROLL")) c->spmv_unroll = e[0] == '1';
     if (const char* e = std::getenv("BSC_PROFILE_ITER")) c->prof_iter = e[0] == '1';
     if (const char* e = std::getenv("BSC_MG_TAIL")) c->mg_tail_cells = std::atoi(e);
+    // two sweeps: the weights are the reciprocal degree-2 Chebyshev nodes of
+    // an interval [a, 3a] (measured best on the c3 tank: [0.45, 1.35]), i.e.
+    // mg_omega and (2 + 1/sqrt2)/(2 - 1/sqrt2) times it; otherwise plain
+    // damped Jacobi with mg_omega
+    c->mg_w[0] = c->P.mg_omega;
+    c->mg_w[1] = c->P.mg_sweeps == 2 ? c->P.mg_omega * ((2.0 + M_SQRT1_2) / (2.0 - M_SQRT1_2)) : c->P.mg_omega;
+    if (const char* e = std::getenv("BSC_MG_W")) std::sscanf(e, "%lf,%lf", &c->mg_w[0], &c->mg_w[1]);
     if (const char* e = std::getenv("BSC_EXACT_DIV")) c->exact_div = e[0] == '1';
     for (int k = 0; k < 6; ++k) cudaEventCreate(&c->ev_it[k]);
     for (int k = 0; k < 2; ++k) cudaEventCreateWithFlags(&c->ev_lag[k], cudaEventDisableTiming);

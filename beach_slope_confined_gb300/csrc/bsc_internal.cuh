@@ -285,6 +285,7 @@ struct Ctx {
     int spmv_unroll = 1;          // four ELL entries per round (BSC_SPMV_UNROLL=0: one)
     bool prof_iter = false;       // BSC_PROFILE_ITER=1: events around each Krylov kernel
     int mg_tail_cells = -1;       // BSC_MG_TAIL=<cells>: largest level in the single-CTA tail
+    double mg_w[2] = {0.82, 0.82};  // smoother weights: the first sweep of a pre/post pair, the later ones
     bool exact_div = false;       // BSC_EXACT_DIV=1: IEEE divisions in the mixed path's FP64 assembly
     cudaEvent_t ev_it[6] = {};
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64

@@ -232,12 +232,12 @@ __global__ void __launch_bounds__(1024) k_mg_dense_inverse(int nx, int ny, const
 // that); 32-bit index arithmetic keeps these latency-bound chains short.
 template <typename T, int MODE>
 __device__ __forceinline__ T smooth_at(int nx, int ny, int c, const T* A, const T* dinv, const T* b,
-                                       const T* xin, const T* xc, int nyc, T scale, T w) {
+                                       const T* xin, const T* xc, int nyc, T scale, T w, T w0 = 0) {
     const int nc = nx * ny;
     const int cx = c / ny, cy = c - cx * ny;
     auto xv = [&](int gx, int gy) -> T {
         const int g = gx * ny + gy;
-        if (MODE == 1) return w * dinv[g] * b[g];
+        if (MODE == 1) return w0 * dinv[g] * b[g];
         if (MODE == 2) return xin[g] + scale * xc[(gx >> 1) * nyc + (gy >> 1)];
         return xin[g];
     };
@@ -283,13 +283,13 @@ template <typename T, int MODE>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg_smooth(int nx, int ny, const T* __restrict__ A,
                                                          const T* __restrict__ dinv, const T* __restrict__ b,
                                                          const T* __restrict__ xin, const T* __restrict__ xc, int nyc,
-                                                         T scale, T w, T* __restrict__ xout,
+                                                         T scale, T w, T w0, T* __restrict__ xout,
                                                          const Scalars* __restrict__ sk) {
     const int c = blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= nx * ny) return;
     // the loads are in bounds whatever the solver state: they go out before
     // the skip test's own load returns
-    const T v = smooth_at<T, MODE>(nx, ny, c, A, dinv, b, xin, xc, nyc, scale, w);
+    const T v = smooth_at<T, MODE>(nx, ny, c, A, dinv, b, xin, xc, nyc, scale, w, w0);
     if (!mg_skip(sk)) xout[c] = v;
 }
 
@@ -336,7 +336,7 @@ struct TailLevel {
 template <typename T>
 struct TailArgs {
     int l0, nlev, nu, smem;
-    T w, scale;
+    T w, w1, scale;  // weights of the first and of the later sweeps
     const T* cinv;
     const Scalars* sk;
     TailLevel<T> L[MG_MAX_LEVELS + 1];
@@ -373,7 +373,7 @@ __device__ __forceinline__ void tail_copy(void* dst, const void* src, int64_t by
 template <typename T>
 __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* tail_sm, const Scalars* sk) {
     const int t = threadIdx.x, NT = blockDim.x;
-    const T w = P.w, sc = P.scale;
+    const T w = P.w, w1 = P.w1, sc = P.scale;
     const int nu = P.nu;
     // level q as the phases see it: in global memory, or staged
     auto lv = [&](int q) -> TailLevel<T> {
@@ -412,12 +412,12 @@ __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* t
         T* c0 = L.y;
         for (int c = t; c < nc; c += NT)
             c0[c] = nu == 1 ? w * L.dinv[c] * L.b[c]
-                            : smooth_at<T, 1>(L.nx, L.ny, c, L.A, L.dinv, L.b, nullptr, nullptr, 0, sc, w);
+                            : smooth_at<T, 1>(L.nx, L.ny, c, L.A, L.dinv, L.b, nullptr, nullptr, 0, sc, w1, w);
         __syncthreads();
         for (int k = 2; k < nu; ++k) {
             T* out = c0 == L.y ? L.t : L.y;
             for (int c = t; c < nc; c += NT)
-                out[c] = smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w);
+                out[c] = smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w1);
             __syncthreads();
             c0 = out;
         }
@@ -448,7 +448,7 @@ __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* t
             T* out = (k == nu - 1) ? L.x : (c0 == L.y ? L.t : L.y);
             for (int c = t; c < nc; c += NT)
                 out[c] = k == 0 ? smooth_at<T, 2>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, C.x, C.ny, sc, w)
-                                : smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w);
+                                : smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w1);
             __syncthreads();
             c0 = out;
         }
@@ -471,12 +471,12 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
 // two sweeps from a zero guess: x1 = w v; x2 = x1 + w (v - A x1)
 template <typename T, typename VI, typename AV>
 __global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<AV> A, const VI* __restrict__ v, T w,
-                                                        T* __restrict__ x, const Scalars* __restrict__ sk) {
+                                                        T w1, T* __restrict__ x, const Scalars* __restrict__ sk) {
     if (mg_skip(sk)) return;
     GRID_LOOP(i, n) {
         const T Av = A.template row<VI, T>(i, v);
         const T vi = (T)v[i];
-        x[i] = w * vi + w * (vi - w * Av);
+        x[i] = w * vi + w1 * (vi - w * Av);  // x1 = w v; x2 = x1 + w1 (v - A x1)
     }
 }
 
@@ -593,7 +593,7 @@ int cycle_level(Ctx* c, int l) {
     const MgLevel& L = mg.L[l];
     Lv<T> v = level_view<T>(L);
     const unsigned g = blocks_for(L.nc, MG_BLOCK);
-    const T w = (T)c->P.mg_omega, sc = (T)c->P.mg_scale;
+    const T w = (T)c->mg_w[0], w1 = (T)c->mg_w[1], sc = (T)c->P.mg_scale;
     const int nu = c->P.mg_sweeps;
     if (l >= mg.tail_l0) {  // this level and all coarser ones in one CTA
         TailArgs<T> P{};
@@ -601,6 +601,7 @@ int cycle_level(Ctx* c, int l) {
         P.nlev = mg.nlev;
         P.nu = nu;
         P.w = w;
+        P.w1 = w1;
         P.scale = sc;
         if constexpr (sizeof(T) == 4)
             P.cinv = mg.cinvf;
@@ -627,11 +628,13 @@ int cycle_level(Ctx* c, int l) {
     if (nu == 1)
         k_mg_jacobi0<T><<<g, MG_BLOCK, 0, c->stream>>>(L.nc, v.dinv, v.b, w, cur, c->mg.skip);
     else
-        k_mg_smooth<T, 1><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, nullptr, nullptr, 0, sc, w, cur, c->mg.skip);
+        k_mg_smooth<T, 1><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, nullptr, nullptr, 0, sc, w1, w,
+                                                          cur, c->mg.skip);
     BSC_LAUNCH(c);
     for (int k = 2; k < nu; ++k) {
         T* out = cur == v.y ? v.t : v.y;
-        k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w, out, c->mg.skip);
+        k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w1, w1,
+                                                          out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }
@@ -645,9 +648,11 @@ int cycle_level(Ctx* c, int l) {
     for (int k = 0; k < nu; ++k) {
         T* out = (k == nu - 1) ? v.x : (cur == v.y ? v.t : v.y);
         if (k == 0)
-            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w, out, c->mg.skip);
+            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w, w,
+                                                              out, c->mg.skip);
         else
-            k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w, out, c->mg.skip);
+            k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w1, w1,
+                                                              out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }
@@ -661,7 +666,7 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
     const int64_t n = c->n;
     using AV = typename FineVal<T>::type;
     const EllOp<AV> A = fine_op<T>(c);
-    const T w = (T)c->P.mg_omega, sc = (T)c->P.mg_scale;
+    const T w = (T)c->mg_w[0], w1 = (T)c->mg_w[1], sc = (T)c->P.mg_scale;
     const int nu = c->P.mg_sweeps;
     T *P0 = (T*)mg.y0, *Q0 = (T*)mg.t0, *R0 = (T*)mg.r0;
     // one row per thread: the fine-level passes have no reduction, and a full
@@ -673,11 +678,11 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
     if (nu == 1)
         k_mg0_scale<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, vin, w, cur, c->mg.skip);
     else
-        k_mg0_pre2<T, VI, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, cur, c->mg.skip);
+        k_mg0_pre2<T, VI, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, w1, cur, c->mg.skip);
     BSC_LAUNCH(c);
     for (int k = 2; k < nu; ++k) {
         T* out = cur == P0 ? Q0 : P0;
-        k_mg0_sweep<T, VI, T, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out, c->mg.skip);
+        k_mg0_sweep<T, VI, T, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w1, out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }
@@ -706,9 +711,9 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
             k_mg0_post<T, T><<<G, MG_BLOCK, 0, c->stream>>>(n, L1.nx, L1.ny, cur, R0, v1.x, c->pcell, rs, sc, w,
                                                             out, c->mg.skip);
         else if (last)
-            k_mg0_sweep<T, VI, O, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, z, c->mg.skip);
+            k_mg0_sweep<T, VI, O, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w1, z, c->mg.skip);
         else
-            k_mg0_sweep<T, VI, T, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w, out, c->mg.skip);
+            k_mg0_sweep<T, VI, T, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w1, out, c->mg.skip);
         BSC_LAUNCH(c);
         cur = out;
     }

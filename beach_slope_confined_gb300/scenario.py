@@ -371,7 +371,7 @@ PRECISIONS = {"fp64": 0, "mixed": 1}
 def make_params(spec: TankSpec, bounds=None, *, precision="fp64", solver="bicgstab",
                 tol=1e-8, maxit=2000, restart=30, max_neighbors=48,
                 reorder_every=20, tol_mode=0, dt_mode=0, inner_tol=1e-4,
-                max_outer=20, precond="none", mg_omega=0.9, mg_scale=1.8, mg_sweeps=2,
+                max_outer=20, precond="none", mg_omega=0.82, mg_scale=1.8, mg_sweeps=2,
                 mg_coarse_max=128) -> Params:
     """bsc_params for a tank case (constants of initialize.f90:19-56 where the
     benchmark does not override them)."""

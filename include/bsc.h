@@ -120,7 +120,8 @@ typedef struct bsc_params {
     double  piston_ramp;         /* stroke scaled by (1-cos(pi t/ramp))/2 for t<ramp */
     double  xmin, xmax, ymin, ymax; /* cell-grid bounds; all 0 = derive at upload */
     /* cell-aggregation multigrid (BSC_PRECOND_MG) */
-    double  mg_omega;            /* damped-Jacobi weight of the smoother           */
+    double  mg_omega;            /* smoother weight; with 2 sweeps the 2nd uses    *
+                                  * 2.094x it (Chebyshev nodes of [a, 3a])         */
     double  mg_scale;            /* scaling of the coarse-grid correction          */
     int32_t mg_sweeps;           /* pre- and post-smoothing sweeps per level       */
     int32_t mg_coarse_max;       /* cells of the coarsest level (dense solve)      */
