@@ -820,14 +820,30 @@ __global__ void k_maxred(int64_t n, const double* __restrict__ a, const double* 
     }
 }
 
-__global__ void k_maxfin(int nb, const double* __restrict__ part, double* __restrict__ out) {
+// one block: strided maxima of the block partials, then a tree (a single
+// thread walking them serially waited on each load)
+__global__ void __launch_bounds__(RED_BLOCK) k_maxfin(int nb, const double* __restrict__ part,
+                                                      double* __restrict__ out) {
+    __shared__ double sa[RED_BLOCK], sb[RED_BLOCK];
     double ma = 0.0, mb = 0.0;
-    for (int k = 0; k < nb; ++k) {
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
         ma = fmax(ma, part[2 * k]);
         mb = fmax(mb, part[2 * k + 1]);
     }
-    out[0] = ma;
-    out[1] = mb;
+    sa[threadIdx.x] = ma;
+    sb[threadIdx.x] = mb;
+    __syncthreads();
+    for (int s = RED_BLOCK / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) {
+            sa[threadIdx.x] = fmax(sa[threadIdx.x], sa[threadIdx.x + s]);
+            sb[threadIdx.x] = fmax(sb[threadIdx.x], sb[threadIdx.x + s]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = sa[0];
+        out[1] = sb[0];
+    }
 }
 
 // ---- free-surface elevation probes (greenfield) ------------------------------------
@@ -883,7 +899,7 @@ namespace bsc {
 int op_timestep_reduce(Ctx* c) {
     k_maxred<<<RED_GRID, RED_BLOCK, 0, c->stream>>>(c->n, c->S.vel, c->S.nut, c->part);
     BSC_LAUNCH(c);
-    k_maxfin<<<1, 1, 0, c->stream>>>(RED_GRID, c->part, c->stepsc);
+    k_maxfin<<<1, RED_BLOCK, 0, c->stream>>>(RED_GRID, c->part, c->stepsc);
     BSC_LAUNCH(c);
     return BSC_OK;
 }

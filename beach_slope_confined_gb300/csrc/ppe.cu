@@ -640,15 +640,26 @@ __global__ void k_fg_next(int64_t n, const T* __restrict__ w, T* __restrict__ V,
 }
 
 // y = H^-1 g over the completed columns
+// the triangle and g staged in shared memory by the block; one thread then
+// substitutes (a serial chain that would otherwise wait on global memory)
 __global__ void k_fg_backsolve(Scalars* sc, double* Hd, FgLayout F) {
+    __shared__ double Hs[FG_MAXM][FG_MAXM + 1], gs[FG_MAXM], ys[FG_MAXM];
     if (sc->done) return;
     const int k = (int)sc->tmp[1];
-    for (int i = k - 1; i >= 0; --i) {
-        double s = Hd[F.g(i)];
-        for (int q = i + 1; q < k; ++q) s -= Hd[F.H(i, q)] * Hd[F.y(q)];
-        Hd[F.y(i)] = s / Hd[F.H(i, i)];
+    for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+        const int i = e / k, q = e - i * k;
+        if (q >= i) Hs[i][q] = Hd[F.H(i, q)];
     }
-    for (int i = k; i < F.m; ++i) Hd[F.y(i)] = 0.0;
+    for (int i = threadIdx.x; i < k; i += blockDim.x) gs[i] = Hd[F.g(i)];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int i = k - 1; i >= 0; --i) {
+            double s = gs[i];
+            for (int q = i + 1; q < k; ++q) s -= Hs[i][q] * ys[q];
+            ys[i] = s / Hs[i][i];
+        }
+    __syncthreads();
+    for (int i = threadIdx.x; i < F.m; i += blockDim.x) Hd[F.y(i)] = i < k ? ys[i] : 0.0;
 }
 
 // x += sum_i y_i V_i
@@ -878,7 +889,7 @@ int run_fgmres(Ctx* c, int64_t n, const Op& A, Work<T> w, double tol, int rel_r0
             c->launches += 3;
         }
         BSC_LAUNCH(c);
-        k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc, c->Hd, F);
+        k_fg_backsolve<<<1, 256, 0, c->stream>>>(c->sc, c->Hd, F);
         k_fg_update<T><<<G, B, 0, c->stream>>>(n, w.x, w.V, c->Hd, F, c->sc);
         c->launches += 2;
         BSC_LAUNCH(c);
@@ -1015,7 +1026,7 @@ int run_fgmres_ir(Ctx* c, int64_t n, bsc_solve_info* si) {
             if ((rc = fetch_outer(c))) return rc;
             if (c->h_sc[1].tmp[2] != 0.0) break;
         }
-        k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc2, c->Hd, F);
+        k_fg_backsolve<<<1, 256, 0, c->stream>>>(c->sc2, c->Hd, F);
         k_fg_update_z<<<G, B, 0, c->stream>>>(n, x, c->Zf, c->Hd, F, c->sc2);
         c->launches += 2;
         BSC_CUDA(c, cudaGetLastError());
@@ -1158,7 +1169,7 @@ int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
         });
         mg.skip = nullptr;
         if (rc) return rc;
-        k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc2, c->Hd, F);
+        k_fg_backsolve<<<1, 256, 0, c->stream>>>(c->sc2, c->Hd, F);
         k_fg_update_z<double><<<G, B, 0, c->stream>>>(n, x, Z, c->Hd, F, c->sc2);
         c->launches += 2;
         BSC_CUDA(c, cudaGetLastError());
@@ -1329,7 +1340,7 @@ int run_fgmres_ir_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
         });
         mg.skip = nullptr;
         if (rc) return rc;
-        k_fg_backsolve<<<1, 1, 0, c->stream>>>(c->sc, c->Hd, F);
+        k_fg_backsolve<<<1, 256, 0, c->stream>>>(c->sc, c->Hd, F);
         k_ir_addz<<<G, B, 0, c->stream>>>(n, x, Z, c->Hd, F, c->sc);
         c->launches += 2;
         BSC_CUDA(c, cudaGetLastError());
