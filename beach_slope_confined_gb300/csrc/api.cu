@@ -431,6 +431,8 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
     if (const char* e = std::getenv("BSC_EXACT_DIV")) c->exact_div = e[0] == '1';
     for (int k = 0; k < 6; ++k) cudaEventCreate(&c->ev_it[k]);
     for (int k = 0; k < 2; ++k) cudaEventCreateWithFlags(&c->ev_lag[k], cudaEventDisableTiming);
+    for (int k = 0; k < Ctx::NCOPY; ++k) cudaStreamCreateWithFlags(&c->copy_stream[k], cudaStreamNonBlocking);
+    for (int k = 0; k <= Ctx::NCOPY; ++k) cudaEventCreateWithFlags(&c->copy_ev[k], cudaEventDisableTiming);
     *out = c;
     return BSC_OK;
 }
@@ -447,6 +449,10 @@ int bsc_destroy(bsc_ctx* c) {
         if (c->ev_spmv[k]) cudaEventDestroy(c->ev_spmv[k]);
     for (int k = 0; k < 2; ++k)
         if (c->ev_lag[k]) cudaEventDestroy(c->ev_lag[k]);
+    for (int k = 0; k < Ctx::NCOPY; ++k)
+        if (c->copy_stream[k]) cudaStreamDestroy(c->copy_stream[k]);
+    for (int k = 0; k <= Ctx::NCOPY; ++k)
+        if (c->copy_ev[k]) cudaEventDestroy(c->copy_ev[k]);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return BSC_OK;
@@ -469,6 +475,21 @@ int bsc_get_time(const bsc_ctx* c, double* t, double* dt) {
     return BSC_OK;
 }
 
+// the copy streams wait for everything queued on c->stream so far
+static int copy_fork(Ctx* c) {
+    BSC_CUDA(c, cudaEventRecord(c->copy_ev[Ctx::NCOPY], c->stream));
+    for (int k = 0; k < Ctx::NCOPY; ++k) BSC_CUDA(c, cudaStreamWaitEvent(c->copy_stream[k], c->copy_ev[Ctx::NCOPY], 0));
+    return BSC_OK;
+}
+// c->stream waits for every copy stream
+static int copy_join(Ctx* c) {
+    for (int k = 0; k < Ctx::NCOPY; ++k) {
+        BSC_CUDA(c, cudaEventRecord(c->copy_ev[k], c->copy_stream[k]));
+        BSC_CUDA(c, cudaStreamWaitEvent(c->stream, c->copy_ev[k], 0));
+    }
+    return BSC_OK;
+}
+
 int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
     CTX_GUARD(c);
     if (!s || s->n <= 0 || s->n > (1ll << 30) || !s->x || !s->y || !s->vx || !s->vy || !s->p || !s->rho ||
@@ -484,9 +505,12 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
     c->n = n;
     if ((rc = setup_grid(c, s->x, s->y, n))) return rc;
     State& S = c->S;
+    if ((rc = copy_fork(c))) return rc;
+    int nq = 0;  // copies round-robin over the copy streams
     auto up = [&](double* d, const double* h, double dflt) -> int {
         if (h) {
-            BSC_CUDA(c, cudaMemcpyAsync(d, h, sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+            BSC_CUDA(c, cudaMemcpyAsync(d, h, sizeof(double) * n, cudaMemcpyHostToDevice,
+                                        c->copy_stream[nq++ % Ctx::NCOPY]));
         } else if (dflt == 0.0) {
             BSC_CUDA(c, cudaMemsetAsync(d, 0, sizeof(double) * n, c->stream));
         } else {
@@ -504,16 +528,18 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
         (rc = up(S.xrest, s->xrest ? s->xrest : s->x, 0)))
         return rc;
     if (s->L) {
-        BSC_CUDA(c, cudaMemcpyAsync(c->lstage, s->L, 4 * sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
-        k_split_L<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, c->lstage, S);
+        cudaStream_t cs = c->copy_stream[nq++ % Ctx::NCOPY];
+        BSC_CUDA(c, cudaMemcpyAsync(c->lstage, s->L, 4 * sizeof(double) * n, cudaMemcpyHostToDevice, cs));
+        k_split_L<<<blocks_for(n, 256), 256, 0, cs>>>(n, c->lstage, S);
         BSC_LAUNCH(c);
     } else {
         if ((rc = up(S.L0, nullptr, 1.0)) || (rc = up(S.L1, nullptr, 0)) || (rc = up(S.L2, nullptr, 0)) ||
             (rc = up(S.L3, nullptr, 1.0)))
             return rc;
     }
-    BSC_CUDA(c, cudaMemcpyAsync(S.tid, s->tid, n, cudaMemcpyHostToDevice, c->stream));
-    BSC_CUDA(c, cudaMemcpyAsync(S.flags, s->flags, n, cudaMemcpyHostToDevice, c->stream));
+    BSC_CUDA(c, cudaMemcpyAsync(S.tid, s->tid, n, cudaMemcpyHostToDevice, c->copy_stream[nq++ % Ctx::NCOPY]));
+    BSC_CUDA(c, cudaMemcpyAsync(S.flags, s->flags, n, cudaMemcpyHostToDevice, c->copy_stream[nq++ % Ctx::NCOPY]));
+    if ((rc = copy_join(c))) return rc;
     k_derive_after_upload<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, S);
     BSC_LAUNCH(c);
     c->have_state = true;
@@ -579,22 +605,27 @@ int bsc_download_state(bsc_ctx* c, bsc_state_view* s) {
     const State& S = c->S;
     const State& T = c->S2;  // free outside a reorder: per-field staging in id order
     const unsigned g = blocks_for(n, 256);
-    // every gather and copy is queued on the stream; one wait at the end
+    // every gather and copy is queued on the copy streams (each field's
+    // gather, then its copy); one wait at the end
+    int rc;
+    if ((rc = copy_fork(c))) return rc;
+    int nq = 0;
     auto dn = [&](const double* src, double* stage, double* host) -> int {
         if (!host) return BSC_OK;
-        k_to_id_order<<<g, 256, 0, c->stream>>>(n, src, stage, S.id);
+        cudaStream_t cs = c->copy_stream[nq++ % Ctx::NCOPY];
+        k_to_id_order<<<g, 256, 0, cs>>>(n, src, stage, S.id);
         BSC_LAUNCH(c);
-        BSC_CUDA(c, cudaMemcpyAsync(host, stage, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        BSC_CUDA(c, cudaMemcpyAsync(host, stage, sizeof(double) * n, cudaMemcpyDeviceToHost, cs));
         return BSC_OK;
     };
     auto dn8 = [&](const uint8_t* src, uint8_t* stage, uint8_t* host) -> int {
         if (!host) return BSC_OK;
-        k_to_id_order_u8<<<g, 256, 0, c->stream>>>(n, src, stage, S.id);
+        cudaStream_t cs = c->copy_stream[nq++ % Ctx::NCOPY];
+        k_to_id_order_u8<<<g, 256, 0, cs>>>(n, src, stage, S.id);
         BSC_LAUNCH(c);
-        BSC_CUDA(c, cudaMemcpyAsync(host, stage, n, cudaMemcpyDeviceToHost, c->stream));
+        BSC_CUDA(c, cudaMemcpyAsync(host, stage, n, cudaMemcpyDeviceToHost, cs));
         return BSC_OK;
     };
-    int rc;
     if ((rc = dn(S.x, T.x, s->x)) || (rc = dn(S.y, T.y, s->y)) || (rc = dn(S.vx, T.vx, s->vx)) ||
         (rc = dn(S.vy, T.vy, s->vy)) || (rc = dn(S.xs, T.xs, s->xs)) || (rc = dn(S.ys, T.ys, s->ys)) ||
         (rc = dn(S.vxs, T.vxs, s->vxs)) || (rc = dn(S.vys, T.vys, s->vys)) || (rc = dn(S.p, T.p, s->p)) ||
@@ -605,12 +636,14 @@ int bsc_download_state(bsc_ctx* c, bsc_state_view* s) {
         (rc = dn(S.vel, T.vel, s->vel)) || (rc = dn(S.xrest, T.xrest, s->xrest)))
         return rc;
     if (s->L) {
-        k_join_L_to_id_order<<<g, 256, 0, c->stream>>>(n, S, c->lstage);
+        cudaStream_t cs = c->copy_stream[nq++ % Ctx::NCOPY];
+        k_join_L_to_id_order<<<g, 256, 0, cs>>>(n, S, c->lstage);
         BSC_LAUNCH(c);
-        BSC_CUDA(c, cudaMemcpyAsync(s->L, c->lstage, 4 * sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+        BSC_CUDA(c, cudaMemcpyAsync(s->L, c->lstage, 4 * sizeof(double) * n, cudaMemcpyDeviceToHost, cs));
     }
     if ((rc = dn8((const uint8_t*)S.tid, (uint8_t*)T.tid, (uint8_t*)s->tid)) || (rc = dn8(S.flags, T.flags, s->flags)))
         return rc;
+    if ((rc = copy_join(c))) return rc;
     BSC_CUDA(c, cudaStreamSynchronize(c->stream));
     return BSC_OK;
 }

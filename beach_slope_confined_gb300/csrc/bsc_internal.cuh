@@ -296,6 +296,11 @@ struct Ctx {
     Scalars* h_sc = nullptr;      // pinned mirror
     Scalars* h_it = nullptr;      // pinned: scalars after the last two queued FGMRES iterations, by parity
     cudaEvent_t ev_lag[2] = {};   // end of the last two queued FGMRES iterations, by parity
+    // host<->device state copies spread over several streams (several copy
+    // engines at once), forked from and joined back into `stream`
+    static constexpr int NCOPY = 4;
+    cudaStream_t copy_stream[NCOPY] = {};
+    cudaEvent_t copy_ev[NCOPY + 1] = {};
     int fg_m = 0;
 
     // timing: stage events recorded on the stream, resolved lazily
