@@ -180,6 +180,10 @@ struct MgLevel {
     float* Af = nullptr;           // FP32 copies (mixed path)
     float* dinvf = nullptr;
     void *b = nullptr, *x = nullptr, *y = nullptr, *t = nullptr;  // V-cycle vectors (FP64 or FP32)
+    // the restriction of the pre-smoothed residual as an operator on b: per
+    // cell of level l+1, 36 weights over the 6x6 patch of this level's cells
+    // around its 2x2 children (36 x nc of level l+1, in the V-cycle's type)
+    void* R = nullptr;
 };
 struct Mg {
     int nlev = 0;                  // levels 1..nlev are structured; nlev is solved densely

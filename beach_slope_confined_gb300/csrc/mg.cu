@@ -311,6 +311,87 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg_restrict(int nx, int ny, const 
     if (!mg_skip(sk)) bc[C] = v;
 }
 
+// ---- restriction of the pre-smoothed residual as an operator -------------------------
+// With two pre-sweeps from zero (weights w0, then w1) the residual is
+//   r = (I - w1 B)(I - w0 B) b,  B = A D^-1,
+// so the coarse right-hand side P^T r is a fixed 36-point stencil on b (the
+// 6x6 patch of fine cells within two of the coarse cell's 2x2 children).
+// Built once per hierarchy; the V-cycle then computes it from b alone, in the
+// same launch as the pre-smoothing (the two only read b).
+constexpr int MG_RPATCH = 6;
+constexpr int MG_RW = MG_RPATCH * MG_RPATCH;
+
+template <typename T>
+__global__ void k_mg_build_R(int nx, int ny, const T* __restrict__ A, const T* __restrict__ dinv, int nxc, int nyc,
+                             T w0, T w1, T* __restrict__ R) {
+    const int C = blockIdx.x * blockDim.x + threadIdx.x;
+    if (C >= nxc * nyc) return;
+    const int CX = C / nyc, CY = C - CX * nyc, nc = nx * ny, ncc = nxc * nyc;
+    const int x0 = 2 * CX - 2, y0 = 2 * CY - 2;  // patch origin
+    T acc[MG_RW];
+#pragma unroll
+    for (int k = 0; k < MG_RW; ++k) acc[k] = 0;
+    const T wsum = w0 + w1, wprod = w0 * w1;
+    // fully unrolled: every accumulator index is a compile-time constant, so
+    // acc stays in registers
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const int fx = 2 * CX + a, fy = 2 * CY + q;
+            if (fx >= nx || fy >= ny) continue;
+            const int f = fx * ny + fy;
+            acc[(a + 2) * MG_RPATCH + (q + 2)] += (T)1;
+#pragma unroll
+            for (int s = 0; s < 9; ++s) {
+                const int hx = fx + s / 3 - 1, hy = fy + s % 3 - 1;
+                if (hx < 0 || hx >= nx || hy < 0 || hy >= ny) continue;
+                const int h = hx * ny + hy;
+                const T bfh = A[s * nc + f] * dinv[h];
+                acc[(a + 1 + s / 3) * MG_RPATCH + (q + 1 + s % 3)] -= wsum * bfh;
+#pragma unroll
+                for (int s2 = 0; s2 < 9; ++s2) {
+                    const int gx = hx + s2 / 3 - 1, gy = hy + s2 % 3 - 1;
+                    if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
+                    acc[(a + s / 3 + s2 / 3) * MG_RPATCH + (q + s % 3 + s2 % 3)] +=
+                        wprod * bfh * A[s2 * nc + h] * dinv[gx * ny + gy];
+                }
+            }
+        }
+#pragma unroll
+    for (int k = 0; k < MG_RW; ++k) R[k * ncc + C] = acc[k];
+}
+
+// pre-smoothing of level l (blocks [0, nbs): two sweeps from zero, as
+// k_mg_smooth<1>) and the restriction to level l+1 through R (the other
+// blocks), in one launch
+template <typename T>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg_pre_restrict(int nx, int ny, const T* __restrict__ A,
+                                                               const T* __restrict__ dinv, const T* __restrict__ b,
+                                                               T scale, T w, T w0, T* __restrict__ xout, int nbs,
+                                                               int nxc, int nyc, const T* __restrict__ R,
+                                                               T* __restrict__ bc, const Scalars* __restrict__ sk) {
+    if ((int)blockIdx.x < nbs) {
+        const int c = blockIdx.x * blockDim.x + threadIdx.x;
+        if (c >= nx * ny) return;
+        const T v = smooth_at<T, 1>(nx, ny, c, A, dinv, b, nullptr, nullptr, 0, scale, w, w0);
+        if (!mg_skip(sk)) xout[c] = v;
+        return;
+    }
+    const int C = (blockIdx.x - nbs) * blockDim.x + threadIdx.x, ncc = nxc * nyc;
+    if (C >= ncc) return;
+    const int CX = C / nyc, CY = C - CX * nyc, x0 = 2 * CX - 2, y0 = 2 * CY - 2;
+    // the weights of patch cells outside the grid are exactly zero: clamped,
+    // unconditional loads keep all 72 in flight
+    T sum = 0;
+#pragma unroll
+    for (int k = 0; k < MG_RW; ++k) {
+        const int gx = min(max(x0 + k / MG_RPATCH, 0), nx - 1), gy = min(max(y0 + k % MG_RPATCH, 0), ny - 1);
+        sum += R[k * ncc + C] * b[gx * ny + gy];
+    }
+    if (!mg_skip(sk)) bc[C] = sum;
+}
+
 // The small levels l0..nlev in one CTA: the same sweeps, restrictions, dense
 // solve and prolongations as the per-level kernels, phase by phase with a
 // block barrier between phases (each phase reads what the previous one
@@ -625,6 +706,14 @@ int cycle_level(Ctx* c, int l) {
     // pre-smoothing from a zero guess: one sweep is x = w D^-1 b; with two or
     // more, the first is folded into the second
     T* cur = v.y;
+    const MgLevel& Lc = mg.L[l + 1];
+    Lv<T> vc = level_view<T>(Lc);
+    if (nu == 2 && L.R) {
+        // both sweeps and the restriction in one launch
+        k_mg_pre_restrict<T><<<g + blocks_for(Lc.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(
+            L.nx, L.ny, v.A, v.dinv, v.b, sc, w1, w, cur, (int)g, Lc.nx, Lc.ny, (const T*)L.R, vc.b, c->mg.skip);
+        BSC_LAUNCH(c);
+    } else {
     if (nu == 1)
         k_mg_jacobi0<T><<<g, MG_BLOCK, 0, c->stream>>>(L.nc, v.dinv, v.b, w, cur, c->mg.skip);
     else
@@ -638,10 +727,9 @@ int cycle_level(Ctx* c, int l) {
         BSC_LAUNCH(c);
         cur = out;
     }
-    const MgLevel& Lc = mg.L[l + 1];
-    Lv<T> vc = level_view<T>(Lc);
     k_mg_restrict<T><<<blocks_for(Lc.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.b, cur, Lc.nx, Lc.ny, vc.b, c->mg.skip);
     BSC_LAUNCH(c);
+    }
     if (int rc = cycle_level<T>(c, l + 1)) return rc;
     // post-smoothing: the prolongation folded into the first sweep; the last
     // sweep writes x_l
@@ -776,6 +864,8 @@ int mg_alloc(Ctx* c) {
         L.y = vec + 2 * stride;
         L.t = vec + 3 * stride;
     }
+    for (int l = 1; l < mg.tail_l0; ++l)  // the restriction operators of the per-level kernels
+        if ((rc = mg_dalloc(c, (unsigned char**)&mg.L[l].R, (int64_t)MG_RW * mg.L[l + 1].nc * (int64_t)vs))) return rc;
     if ((rc = mg_dalloc(c, &mg.rowslots, 9 * n))) return rc;  // the level-1 Galerkin pass
     if (f32 && (rc = mg_dalloc(c, &mg.rowslotsf, 9 * n))) return rc;
     const int64_t nco = mg.L[nlev].nc;
@@ -864,6 +954,19 @@ int mg_setup(Ctx* c) {
     else
         k_mg_dense_inverse<double><<<1, 1024, smem, c->stream>>>(Lc.nx, Lc.ny, Lc.A, mg.cinv);
     BSC_LAUNCH(c);
+    // the restriction operators of the levels swept by per-level kernels
+    if (c->P.mg_sweeps == 2)
+        for (int l = 1; l < mg.tail_l0; ++l) {
+            const MgLevel &F = mg.L[l], &C = mg.L[l + 1];
+            const unsigned gb = blocks_for(C.nc, 128);
+            if (f32)
+                k_mg_build_R<float><<<gb, 128, 0, c->stream>>>(F.nx, F.ny, F.Af, F.dinvf, C.nx, C.ny,
+                                                               (float)c->mg_w[0], (float)c->mg_w[1], (float*)F.R);
+            else
+                k_mg_build_R<double><<<gb, 128, 0, c->stream>>>(F.nx, F.ny, F.A, F.dinv, C.nx, C.ny, c->mg_w[0],
+                                                                c->mg_w[1], (double*)F.R);
+            BSC_LAUNCH(c);
+        }
     return BSC_OK;
 }
 
