@@ -18,7 +18,7 @@ from typing import Dict, Optional, Tuple
 
 import numpy as np
 
-from .scenario import Params, SolveInfo, StateView, Timing, empty_state, state_view
+from .scenario import Params, SolveInfo, StateView, Timing, WcsphParams, empty_state, state_view
 
 STATUS = {0: "BSC_OK", -1: "BSC_E_INVALID", -2: "BSC_E_CUDA", -3: "BSC_E_NOMEM",
           -4: "BSC_E_CAPACITY", -5: "BSC_E_NOT_CONVERGED", -6: "BSC_E_BREAKDOWN",
@@ -64,6 +64,10 @@ OPTIONAL_SIGNATURES = {
     "get_timings": [_VP, ctypes.POINTER(Timing)],
     "reset_timings": [_VP],
     "synchronize": [_VP],
+    "wcsph_setup": [_VP, ctypes.POINTER(WcsphParams)],
+    "wcsph_set_params": [_VP, ctypes.c_double, ctypes.c_double, _PD],
+    "wcsph_forward": [_VP, ctypes.c_int32, ctypes.c_int32, _PD],
+    "wcsph_adjoint": [_VP, _PD, _PD],
 }
 
 
@@ -235,6 +239,30 @@ class Context:
     def synchronize(self):
         if "synchronize" in self._fn:
             self._call("synchronize")
+
+    # -- the differentiable WCSPH step (bsc_wcsph_*) ----------------------------
+    def wcsph_setup(self, wp: WcsphParams):
+        """Take the current state as the initial state of every WCSPH run."""
+        self._call("wcsph_setup", ctypes.byref(wp))
+        self._wc_np = int(wp.nprobe)
+        self._wc_nx, self._wc_ny = int(wp.grid_nx), int(wp.grid_ny)
+
+    def wcsph_set_params(self, alpha: float, beta: float, grid: np.ndarray):
+        g = np.ascontiguousarray(grid, dtype=np.float64).reshape(-1)
+        self._call("wcsph_set_params", float(alpha), float(beta), _dp(g))
+
+    def wcsph_forward(self, nsteps: int, every: int) -> np.ndarray:
+        """Probe elevations after each step, shape (nsteps, nprobe)."""
+        eta = np.zeros((nsteps, self._wc_np))
+        self._call("wcsph_forward", int(nsteps), int(every), _dp(eta))
+        return eta
+
+    def wcsph_adjoint(self, dJ_deta: np.ndarray) -> np.ndarray:
+        """Gradient [dJ/dalpha, dJ/dbeta, dJ/dpor (grid, flattened)]."""
+        d = np.ascontiguousarray(dJ_deta, dtype=np.float64)
+        g = np.zeros(2 + self._wc_nx * self._wc_ny)
+        self._call("wcsph_adjoint", _dp(d), _dp(g))
+        return g
 
 
 def csr_solve(lib: ctypes.CDLL, prefix: str, params: Params, rowptr, col, val, b, x0):

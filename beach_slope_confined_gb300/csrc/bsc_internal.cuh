@@ -207,6 +207,8 @@ struct Mg {
     std::vector<void*> allocs;
 };
 
+struct WcState;  // the differentiable WCSPH step (wcsph.cu)
+
 struct Ctx {
     bsc_params P{};
     KParams K{};
@@ -302,6 +304,7 @@ struct Ctx {
     cudaEvent_t ev_lag[2] = {};   // end of the last two queued FGMRES iterations, by parity
     // host<->device state copies spread over several streams (several copy
     // engines at once), forked from and joined back into `stream`
+    WcState* wc = nullptr;        // WCSPH forward/adjoint state, after bsc_wcsph_setup
     static constexpr int NCOPY = 4;
     cudaStream_t copy_stream[NCOPY] = {};
     cudaEvent_t copy_ev[NCOPY + 1] = {};
@@ -376,6 +379,7 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info);
 // multigrid: build the hierarchy for the assembled PPE; apply one V-cycle
 // z = M v to an FP64 vector (FP64 or FP32 arithmetic); release the buffers
 int mg_setup(Ctx* c);
+void wc_free(Ctx* c);
 int mg_vcycle_f64(Ctx* c, const double* v, double* z);
 int mg_vcycle_f32(Ctx* c, const float* v, float* z);
 void mg_free(Ctx* c);

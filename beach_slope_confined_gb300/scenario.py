@@ -359,6 +359,42 @@ class Timing(ctypes.Structure):
                 ("kernel_launches", ctypes.c_int64)]
 
 
+class WcsphParams(ctypes.Structure):
+    """bsc_wcsph_params of include/bsc.h."""
+    _fields_ = [("c0", _D), ("gamma", _D), ("delta", _D), ("surface_y", _D), ("nu", _D), ("alpha", _D),
+                ("beta", _D), ("grid_x0", _D), ("grid_y0", _D), ("grid_dx", _D), ("grid_dy", _D),
+                ("grid_nx", _I), ("grid_ny", _I), ("grid_por", _PD), ("nprobe", _I), ("probe_x", _D * 16),
+                ("probe_depth", _D)]
+
+
+def wcsph_params(spec: "TankSpec", scen: "Scenario", alpha: float = None, beta: float = None,
+                 grid=None) -> "tuple":
+    """The WCSPH model of the calibration case on a tank scenario: Tait EOS
+    with c0 = 10 sqrt(g depth) and gamma = 7, delta-SPH coefficient 0.1, the
+    still-water level as the hydrostatic reference, water's kinematic
+    viscosity, the scenario's porosity grid and probes.  Returns (params,
+    grid array) -- the array must stay alive while the params are used."""
+    g = np.ascontiguousarray(scen.por_grid if grid is None else grid, dtype=np.float64)
+    ny, nx = g.shape
+    w = WcsphParams()
+    w.c0 = 10.0 * np.sqrt(abs(spec.g) * spec.depth)
+    w.gamma = 7.0
+    w.delta = 0.1
+    w.surface_y = spec.depth
+    w.nu = 1.0e-6
+    w.alpha = spec.darcy_alpha if alpha is None else alpha
+    w.beta = spec.forch_beta if beta is None else beta
+    w.grid_x0, w.grid_y0 = scen.por_origin
+    w.grid_dx, w.grid_dy = scen.por_step
+    w.grid_nx, w.grid_ny = nx, ny
+    w.grid_por = g.ctypes.data_as(_PD)
+    w.nprobe = len(spec.probes)
+    for k, xp in enumerate(spec.probes):
+        w.probe_x[k] = xp
+    w.probe_depth = spec.depth
+    return w, g
+
+
 STATE_FIELDS = ("x", "y", "vx", "vy", "xs", "ys", "vxs", "vys", "p", "rho", "oden",
                 "mass", "porosity", "gradvx", "nut", "tke", "resist", "varts", "vel",
                 "xrest")

@@ -273,6 +273,46 @@ int bsc_csr_solve_noalloc(const bsc_params* p, int32_t n, const int32_t* rowptr,
                           const int32_t* col, const double* val, const double* b,
                           double* x, void* stream, bsc_solve_info* info);
 
+/* ---- differentiable WCSPH step and its adjoint ------------------------------ */
+/* A weakly compressible step on the uploaded state (fluid, walls, piston and
+ * porous solids of the ISPH context; FP64 context, Wendland C2 kernel):
+ * Tait EOS clamped at zero pressure, continuity with delta-SPH diffusion and
+ * the hydrostatic correction (wcsph.f90:13-129), symmetric pressure gradient,
+ * Morris viscosity, gravity, implicit Darcy-Forchheimer drag and the
+ * position update.  The calibrated parameters are the drag coefficients and
+ * the porosity of a grid of cells over the slope (each solid takes the
+ * porosity of the cell it lies in; solids outside the grid keep por).  The
+ * adjoint returns the gradient of any loss of the probe elevations, with the
+ * neighbour lists of every step frozen, recomputing each segment of
+ * ckpt_every steps from a checkpoint. */
+#define BSC_WCSPH_MAX_GRID 256
+#define BSC_WCSPH_MAX_PROBES 16
+typedef struct bsc_wcsph_params {
+    double  c0;                  /* sound speed of the Tait EOS                    */
+    double  gamma;               /* Tait exponent                                  */
+    double  delta;               /* delta-SPH density-diffusion coefficient        */
+    double  surface_y;           /* still-water level (hydrostatic density)        */
+    double  nu;                  /* kinematic viscosity                            */
+    double  alpha, beta;         /* Darcy and Forchheimer drag coefficients        */
+    double  grid_x0, grid_y0, grid_dx, grid_dy;  /* porosity grid                  */
+    int32_t grid_nx, grid_ny;    /* grid_nx * grid_ny <= BSC_WCSPH_MAX_GRID        */
+    const double* grid_por;      /* porosities, index iy * grid_nx + ix            */
+    int32_t nprobe;              /* <= BSC_WCSPH_MAX_PROBES                        */
+    double  probe_x[BSC_WCSPH_MAX_PROBES];
+    double  probe_depth;         /* eta = sum_i V_i w1(x_i - x_p) - probe_depth    */
+} bsc_wcsph_params;
+/* Takes the current state as the initial state of every later forward run
+ * (densities set hydrostatic from surface_y) and sets the parameters. */
+int bsc_wcsph_setup(bsc_ctx* ctx, const bsc_wcsph_params* w);
+/* New values of the calibrated parameters (grid_por: grid_nx*grid_ny). */
+int bsc_wcsph_set_params(bsc_ctx* ctx, double alpha, double beta, const double* grid_por);
+/* nsteps steps from the initial state, a checkpoint every ckpt_every steps;
+ * eta[nsteps * nprobe] receives the probe elevations after each step. */
+int bsc_wcsph_forward(bsc_ctx* ctx, int32_t nsteps, int32_t ckpt_every, double* eta);
+/* Reverse pass through the last forward run: given dJ/deta[nsteps * nprobe],
+ * grad[0] = dJ/dalpha, grad[1] = dJ/dbeta, grad[2 + k] = dJ/dpor_k. */
+int bsc_wcsph_adjoint(bsc_ctx* ctx, const double* dJ_deta, double* grad);
+
 /* ---- hardware probes ---------------------------------------------------- */
 /* Measured FP64 and FP32 FMA throughput (GFLOP/s, 2 flops per FMA) and a
  * device-to-device copy bandwidth (GB/s, read+write) on the current device. */
