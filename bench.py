@@ -345,6 +345,73 @@ def cpu_sample(scen, spec, threads: int, gpu_iters: float, solver: str):
     return scen.n_fluid / t_step, desc, t_step
 
 
+def run_wcsph(reps: int = 2):
+    """The differentiable WCSPH workload (c4): a 500-step FP64 forward run with
+    checkpoints every 50 steps, then the adjoint of the squared probe misfit
+    against a target run (alpha=260, beta=0.9, porosity 0.45). Times both
+    through the C ABI, with host timers around the synchronous calls. Checks
+    the alpha and beta gradients against central differences of the same
+    forward run."""
+    from beach_slope_confined_gb300 import Solver, scenario as sc, setup_tank
+
+    spec = sc.config_spec("c4")
+    scen = sc.build(spec)
+    nsteps, every = 500, 50
+    g = Solver(sc.make_params(spec, scen.bounds, precision="fp64"))
+    setup_tank(g, scen)
+    wp, grid0 = sc.wcsph_params(spec, scen)
+    g.wcsph_setup(wp)
+    g.wcsph_set_params(260.0, 0.9, np.full_like(grid0, 0.45))
+    eta_hat = g.wcsph_forward(nsteps, every)
+    a0, b0 = spec.darcy_alpha, spec.forch_beta
+
+    def misfit(a, b):
+        g.wcsph_set_params(a, b, grid0)
+        eta = g.wcsph_forward(nsteps, every)
+        return float(np.sum((eta - eta_hat) ** 2)), eta
+
+    J0, eta = misfit(a0, b0)
+    dJ = 2.0 * (eta - eta_hat)
+    grad = g.wcsph_adjoint(dJ)
+    tf, ta = [], []
+    for _ in range(max(1, reps)):
+        t0 = time.perf_counter()
+        g.wcsph_forward(nsteps, every)
+        t1 = time.perf_counter()
+        g.wcsph_adjoint(dJ)
+        t2 = time.perf_counter()
+        tf.append(t1 - t0)
+        ta.append(t2 - t1)
+    fwd, adj = min(tf), min(ta)
+    # Central differences: the fourth-order stencil at a relative step of 3e-2,
+    # and the two-point one at 1e-6. Roundoff, amplified over 500 steps,
+    # limits the misfit's differences to about 1e-4 relative at steps of
+    # 3e-3 and dominates them at 1e-6.
+    fd = {}
+    for rs, pts in ((3e-2, 4), (1e-6, 2)):
+        out = {}
+        for k, (name, base) in enumerate((("alpha", a0), ("beta", b0))):
+            h = rs * base
+            J = {}
+            for m in ((-2, -1, 1, 2) if pts == 4 else (-1, 1)):
+                J[m] = misfit(a0 + m * h, b0)[0] if k == 0 else misfit(a0, b0 + m * h)[0]
+            if pts == 4:
+                d = (8.0 * (J[1] - J[-1]) - (J[2] - J[-2])) / (12.0 * h)
+            else:
+                d = (J[1] - J[-1]) / (2.0 * h)
+            out[name] = {"fd": d, "adjoint": float(grad[k]),
+                         "rel_diff": abs(float(grad[k]) - d) / abs(d) if d != 0 else None}
+        fd[f"{pts}-point, relative step {rs:g}"] = out
+    g.close()
+    return {"ratio": adj / fwd, "forward_ms": 1e3 * fwd, "adjoint_ms": 1e3 * adj,
+            "workload": f"c4 tank, dx={spec.dx} m, {scen.n_fluid} fluid + {scen.n - scen.n_fluid} wall particles, "
+                        f"{nsteps} FP64 WCSPH steps of dt={spec.dt} s, checkpoints every {every}",
+            "forward_particle_steps_per_s": scen.n_fluid * nsteps / fwd,
+            "misfit": J0, "gradient_alpha_beta": [float(grad[0]), float(grad[1])],
+            "gradient_porosity_grid_norm": float(np.linalg.norm(grad[2:])),
+            "finite_differences": fd}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -361,6 +428,7 @@ def main():
     ap.add_argument("--restart", type=int, default=40)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-wcsph", action="store_true", help="skip the WCSPH forward/adjoint workload (c4)")
     ap.add_argument("--cpu-iters", type=float, default=1350.0,
                     help="PPE iterations per step the reference arm's sample is scaled to")
     args = ap.parse_args()
@@ -431,6 +499,7 @@ def main():
                              "achieved": a64,
                              "peak": hbm, "unit": "GB/s", "frac": (a64 / hbm) if a64 else None,
                              "traffic": (t64 * f["n"]) if t64 else None}}
+    wc = None if args.no_wcsph else run_wcsph()
     cpu = None
     if not args.no_cpu:
         if ref_iters:
@@ -466,7 +535,8 @@ def main():
         "gpu_launches": m["launches"],
         "measured_peaks": {"fp64_gflops": peaks[0], "fp32_gflops": peaks[1], "copy_gbs": peaks[2]} if peaks else None,
         "fp64_bound_kernels": fp64_bound_kernels(),
-        "wcsph_adjoint_forward_ratio": None,
+        "wcsph_adjoint_forward_ratio": wc["ratio"] if wc else None,
+        "wcsph": wc,
     }
     print(json.dumps(line), flush=True)
     dist.close()

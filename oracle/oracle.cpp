@@ -57,6 +57,21 @@ const double C28_314 = (double)(28.0f * 3.14f);  // kernel.f90:52: 28.0*3.14
 const double C3_314 = (double)(3.0f * 3.14f);    // kernel.f90:53: 3.0*3.14
 const double ALP = 0.1;                          // kernel.f90:14
 
+// state of the WCSPH calibration workload (orc_wcsph_*)
+struct WcOrc {
+    bool on = false;
+    double rho0 = 0, B = 0, gam = 0, grav_c = 0, ys = 0, c2 = 0, nu = 0, alpha = 0, beta = 0;
+    double gx0 = 0, gy0 = 0, gdx = 1, gdy = 1, R1 = 0, depth = 0, t0 = 0;
+    int gnx = 0, gny = 0, np = 0;
+    double xp[BSC_WCSPH_MAX_PROBES] = {};
+    std::vector<double> theta, sw, mass, init;  // grid porosities, (1-phi) V_s, masses, x y vx vy rho
+    std::vector<int> sg;                        // solid -> grid cell or -1
+    // forward record: every state, list, porosity and pressure sum
+    int nsteps = 0;
+    std::vector<std::vector<double>> st, nn, PP;
+    std::vector<std::vector<int64_t>> off, ids;
+};
+
 struct Orc {
     bsc_params P{};
     double t = 0.0, dt = 0.0, umax = 0.0, numax = 0.0, dtsol = 0.0;
@@ -93,6 +108,7 @@ struct Orc {
     std::vector<int64_t> col;
     std::vector<double> val, rhs, sol;
     bool have_csr = false;
+    WcOrc wc;
     std::string err;
 };
 
@@ -1255,3 +1271,410 @@ int orc_eval_kernel(const bsc_params* p, double r, double* w, double* f, double*
     return BSC_OK;
 }
 }
+
+// ---------------------------------------------------------------------------
+// WCSPH calibration workload: forward map and its adjoint, restated on the
+// CPU.  The forward step follows the formulae of wcsph.f90 (Tait EOS with the
+// negative-pressure reset of dentopress :36-62, continuity with the delta term
+// and hydrostatic correction of calmasscons :66-129), a pressure gradient and
+// laminar viscosity in the symmetric SPH forms, the Ergun drag of porous.f90:
+// 192-212, and the implicit-drag velocity update with x' = x + dt v'/n.  It
+// runs on the model's own masses m = rho_init dl^2.  The adjoint is written in
+// scatter form: each pair term of particle i's sums sends its derivatives to
+// both i and j.  It is not organised like the gather-form CUDA adjoint, which
+// makes it an independent check of that bookkeeping.  No checkpointing: every
+// state of the run is kept.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct WcPre {
+    std::vector<double> rt, pp, rh, drh;
+};
+
+double wc_wendF(const Orc* o) { const double h = o->P.h; return 35.0 / (4.0 * 3.140 * ((h * h) * (h * h))); }
+double wc_wendW(const Orc* o) { const double h = o->P.h; return 7.0 / (4.0 * 3.140 * (h * h)); }
+// Wendland C2: W(r), F(r) with grad_i W = F (x_i - x_j), dF/dr
+double wc_W(const Orc* o, double r) {
+    const double q = r / o->P.h, a = 1.0 - 0.5 * q;
+    return wc_wendW(o) * (1.0 + 2.0 * q) * a * a * a * a;
+}
+double wc_F(const Orc* o, double r) { const double a = 1.0 - 0.5 * r / o->P.h; return -wc_wendF(o) * a * a * a; }
+double wc_dF(const Orc* o, double r) {
+    const double a = 1.0 - 0.5 * r / o->P.h;
+    return 1.5 * wc_wendF(o) * a * a / o->P.h;
+}
+// the probes' 1-D Wendland C2 kernel of radius R1 and its q-derivative
+double wc_w1(double q, double R1) { const double a = 1.0 - q; return (1.25 / R1) * a * a * a * (1.0 + 3.0 * q); }
+double wc_w1q(double q, double R1) { const double a = 1.0 - q; return -(15.0 / R1) * q * a * a; }
+
+bool fluid(const Orc* o, int64_t i) { return o->tid[i] == BSC_TID_FLUID; }
+
+void wc_pre(const Orc* o, const double* y, const double* rho, WcPre& q) {
+    const WcOrc& w = o->wc;
+    const int64_t n = o->n;
+    q.rt.resize(n); q.pp.resize(n); q.rh.resize(n); q.drh.resize(n);
+    for (int64_t i = 0; i < n; ++i) {
+        const double r = fluid(o, i) ? std::max(rho[i], w.rho0) : rho[i];
+        double p = w.B * (std::pow(r / w.rho0, w.gam) - 1.0);
+        if (p < 0.0) p = 0.0;  // wcsph.f90:49-52
+        q.rt[i] = r;
+        q.pp[i] = p;
+        const double s = 1.0 + w.grav_c * (w.ys - y[i]);
+        q.rh[i] = w.rho0 * std::pow(s, 1.0 / w.gam);       // wcsph.f90:82-86
+        q.drh[i] = -w.rho0 * w.grav_c / w.gam * std::pow(s, 1.0 / w.gam) / s;
+    }
+}
+
+void wc_solids(Orc* o) {
+    WcOrc& w = o->wc;
+    w.sw.resize(o->ns);
+    w.sg.resize(o->ns);
+    for (int64_t s = 0; s < o->ns; ++s) {
+        const double fx = std::floor((o->sx[s] - w.gx0) / w.gdx), fy = std::floor((o->sy[s] - w.gy0) / w.gdy);
+        int g = -1;
+        if (fx >= 0 && fx < w.gnx && fy >= 0 && fy < w.gny) g = (int)fy * w.gnx + (int)fx;
+        const double phi = g >= 0 ? w.theta[g] : o->P.por;
+        w.sw[s] = (1.0 - phi) * (o->sm[s] / o->srho[s]);
+        w.sg[s] = g;
+    }
+}
+
+double wc_porosity(const Orc* o, int64_t i) {
+    const double H2 = 4.0 * o->P.h * o->P.h;
+    double f = 0.0;
+    for (int64_t s = 0; s < o->ns; ++s) {
+        const double dx = o->x[i] - o->sx[s], dy = o->y[i] - o->sy[s], d2 = dx * dx + dy * dy;
+        if (d2 < H2) f += o->wc.sw[s] * wc_W(o, std::sqrt(d2));
+    }
+    return 1.0 - f;
+}
+
+void wc_eta(const Orc* o, const double* x, const double* rho, double* eta) {
+    const WcOrc& w = o->wc;
+    for (int p = 0; p < w.np; ++p) {
+        double s = 0.0;
+        for (int64_t i = 0; i < o->n; ++i) {
+            if (!fluid(o, i)) continue;
+            const double q = std::fabs(x[i] - w.xp[p]) / w.R1;
+            if (q < 1.0) s += (w.mass[i] / rho[i]) * wc_w1(q, w.R1);
+        }
+        eta[p] = s - w.depth;
+    }
+}
+
+// one forward step of the state in o->x, y, vx, vy, rho
+void wc_step(Orc* o, std::vector<double>& nbuf, std::vector<double>& Pbuf) {
+    WcOrc& w = o->wc;
+    const int64_t n = o->n;
+    const double dt = o->dt, lam = o->P.lam, g = o->P.g, d = o->P.d50;
+    o->t += dt;
+    orc_piston(static_cast<orc_ctx*>(o));
+    bin_particles(o);
+    orc_neighbour(static_cast<orc_ctx*>(o));
+    WcPre q;
+    wc_pre(o, o->y.data(), o->rho.data(), q);
+    nbuf.assign(n, 1.0);
+    Pbuf.assign(2 * n, 0.0);
+    std::vector<double> nx(n), ny(n), nvx(n), nvy(n), nr(n);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        nx[i] = o->x[i]; ny[i] = o->y[i]; nvx[i] = o->vx[i]; nvy[i] = o->vy[i]; nr[i] = o->rho[i];
+        if (!fluid(o, i)) continue;
+        const double ni = wc_porosity(o, i);
+        nbuf[i] = ni;
+        const double rti = q.rt[i], pri = q.pp[i] / (rti * rti);
+        double Dr = 0, Px = 0, Py = 0, Vx = 0, Vy = 0;
+        for (int64_t e = o->nb_off[i]; e < o->nb_off[i + 1]; ++e) {
+            const int64_t j = o->nb_id[e];
+            const double dx = o->x[i] - o->x[j], dy = o->y[i] - o->y[j];
+            const double r2 = dx * dx + dy * dy, r = std::sqrt(r2);
+            const double F = wc_F(o, r), G = F * r2 / (r2 + lam);
+            const double mj = w.mass[j], Vj = mj / q.rt[j];
+            const double dvx = o->vx[i] - o->vx[j], dvy = o->vy[i] - o->vy[j];
+            Dr += mj * (rti / q.rt[j]) * F * (dvx * dx + dvy * dy);
+            Dr += w.c2 * (q.rt[j] - rti - q.rh[j] + q.rh[i]) * (-G) * Vj;
+            const double pc = mj * (pri + q.pp[j] / (q.rt[j] * q.rt[j])) * F;
+            Px += pc * dx;
+            Py += pc * dy;
+            Vx += 2.0 * w.nu * Vj * G * dvx;
+            Vy += 2.0 * w.nu * Vj * G * dvy;
+        }
+        const double ax = -ni * Px + Vx, ay = -ni * Py + Vy + ni * g;
+        const double vxi = o->vx[i], vyi = o->vy[i];
+        const double vm = std::sqrt(vxi * vxi + vyi * vyi), on = 1.0 - ni, n3 = ni * ni * ni;
+        const double R = -w.nu * w.alpha * on * on / (n3 * d * d) - w.beta * vm * on / (n3 * d);
+        const double D = 1.0 - dt * R * ni;
+        nvx[i] = (vxi + dt * ax) / D;
+        nvy[i] = (vyi + dt * ay) / D;
+        nx[i] = o->x[i] + dt * nvx[i] / ni;
+        ny[i] = o->y[i] + dt * nvy[i] / ni;
+        nr[i] = rti + dt * Dr;
+        Pbuf[i] = Px;
+        Pbuf[n + i] = Py;
+    }
+    o->x.swap(nx); o->y.swap(ny); o->vx.swap(nvx); o->vy.swap(nvy); o->rho.swap(nr);
+}
+
+void wc_store(const Orc* o, std::vector<double>& dst) {
+    const int64_t n = o->n;
+    dst.resize(5 * n);
+    std::copy(o->x.begin(), o->x.end(), dst.begin());
+    std::copy(o->y.begin(), o->y.end(), dst.begin() + n);
+    std::copy(o->vx.begin(), o->vx.end(), dst.begin() + 2 * n);
+    std::copy(o->vy.begin(), o->vy.end(), dst.begin() + 3 * n);
+    std::copy(o->rho.begin(), o->rho.end(), dst.begin() + 4 * n);
+}
+
+void wc_restore(Orc* o, const std::vector<double>& src) {
+    const int64_t n = o->n;
+    std::copy(src.begin(), src.begin() + n, o->x.begin());
+    std::copy(src.begin() + n, src.begin() + 2 * n, o->y.begin());
+    std::copy(src.begin() + 2 * n, src.begin() + 3 * n, o->vx.begin());
+    std::copy(src.begin() + 3 * n, src.begin() + 4 * n, o->vy.begin());
+    std::copy(src.begin() + 4 * n, src.begin() + 5 * n, o->rho.begin());
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_wcsph_setup(orc_ctx* o, const bsc_wcsph_params* p) {
+    if (!o || !p) return BSC_E_INVALID;
+    const int G = p->grid_nx * p->grid_ny;
+    if (p->grid_nx < 1 || p->grid_ny < 1 || G > BSC_WCSPH_MAX_GRID || !p->grid_por || !(p->grid_dx > 0) ||
+        !(p->grid_dy > 0) || p->nprobe < 1 || p->nprobe > BSC_WCSPH_MAX_PROBES || !(p->c0 > 0) || !(p->gamma > 0))
+        return fail(o, BSC_E_INVALID, "wcsph_setup: bad parameters");
+    WcOrc& w = o->wc;
+    w = WcOrc();
+    w.on = true;
+    w.rho0 = o->P.rho0;
+    w.gam = p->gamma;
+    w.B = o->P.rho0 * p->c0 * p->c0 / p->gamma;
+    w.grav_c = std::fabs(o->P.g) * p->gamma / (p->c0 * p->c0);
+    w.ys = p->surface_y;
+    w.c2 = p->delta * 2.0 * o->P.h * p->c0;
+    w.nu = p->nu;
+    w.alpha = p->alpha;
+    w.beta = p->beta;
+    w.gx0 = p->grid_x0; w.gy0 = p->grid_y0; w.gdx = p->grid_dx; w.gdy = p->grid_dy;
+    w.gnx = p->grid_nx; w.gny = p->grid_ny;
+    w.np = p->nprobe;
+    for (int k = 0; k < w.np; ++k) w.xp[k] = p->probe_x[k];
+    w.R1 = 2.0 * o->P.h;
+    w.depth = p->probe_depth;
+    w.theta.assign(p->grid_por, p->grid_por + G);
+    const int64_t n = o->n;
+    w.mass.resize(n);
+    for (int64_t i = 0; i < n; ++i) {
+        const double s = 1.0 + w.grav_c * (w.ys - o->y[i]);
+        const double r = o->y[i] < w.ys ? w.rho0 * std::pow(s, 1.0 / w.gam) : w.rho0;
+        o->rho[i] = r;
+        w.mass[i] = r * o->P.dl * o->P.dl;
+    }
+    wc_store(o, w.init);
+    w.t0 = o->t;
+    wc_solids(o);
+    return BSC_OK;
+}
+
+int orc_wcsph_set_params(orc_ctx* o, double alpha, double beta, const double* grid) {
+    if (!o || !o->wc.on) return o ? fail(o, BSC_E_INVALID, "wcsph_set_params before wcsph_setup") : BSC_E_INVALID;
+    o->wc.alpha = alpha;
+    o->wc.beta = beta;
+    if (grid) std::copy(grid, grid + o->wc.gnx * o->wc.gny, o->wc.theta.begin());
+    wc_solids(o);
+    return BSC_OK;
+}
+
+int orc_wcsph_forward(orc_ctx* o, int32_t nsteps, int32_t every, double* eta) {
+    if (!o || !o->wc.on) return o ? fail(o, BSC_E_INVALID, "wcsph_forward before wcsph_setup") : BSC_E_INVALID;
+    if (nsteps < 1 || every < 1 || !eta) return fail(o, BSC_E_INVALID, "wcsph_forward: bad arguments");
+    WcOrc& w = o->wc;
+    wc_restore(o, w.init);
+    o->t = w.t0;
+    w.nsteps = nsteps;
+    w.st.assign(nsteps + 1, {});
+    w.nn.assign(nsteps, {});
+    w.PP.assign(nsteps, {});
+    w.off.assign(nsteps, {});
+    w.ids.assign(nsteps, {});
+    for (int s = 0; s < nsteps; ++s) {
+        wc_store(o, w.st[s]);
+        wc_step(o, w.nn[s], w.PP[s]);
+        w.off[s] = o->nb_off;
+        w.ids[s] = o->nb_id;
+        wc_eta(o, o->x.data(), o->rho.data(), eta + (int64_t)s * w.np);
+    }
+    wc_store(o, w.st[nsteps]);
+    return BSC_OK;
+}
+
+int orc_wcsph_adjoint(orc_ctx* o, const double* dJ, double* grad) {
+    if (!o || !o->wc.on) return o ? fail(o, BSC_E_INVALID, "wcsph_adjoint before wcsph_setup") : BSC_E_INVALID;
+    WcOrc& w = o->wc;
+    if (w.nsteps < 1 || !dJ || !grad) return fail(o, BSC_E_INVALID, "wcsph_adjoint: run wcsph_forward first");
+    const int64_t n = o->n;
+    const int G = w.gnx * w.gny;
+    const double dt = o->dt, lam = o->P.lam, g = o->P.g, d = o->P.d50, H2 = 4.0 * o->P.h * o->P.h;
+    std::fill(grad, grad + 2 + G, 0.0);
+    // adjoint of the state after the current step: x y vx vy rho
+    std::vector<double> L(5 * n, 0.0), Ln(5 * n);
+    std::vector<double> lax(n), lay(n), lD(n), ln(n), ort(n), op(n);
+    for (int s = w.nsteps - 1; s >= 0; --s) {
+        const double* S0 = w.st[s].data();
+        const double* S1 = w.st[s + 1].data();
+        const double *x = S0, *y = S0 + n, *vx = S0 + 2 * n, *vy = S0 + 3 * n, *rho = S0 + 4 * n;
+        // the loss term of the state after step s
+        for (int64_t i = 0; i < n; ++i) {
+            if (!fluid(o, i)) continue;
+            const double V = w.mass[i] / S1[4 * n + i];
+            for (int p = 0; p < w.np; ++p) {
+                const double dd = S1[i] - w.xp[p], q = std::fabs(dd) / w.R1;
+                if (q >= 1.0) continue;
+                L[i] += dJ[(int64_t)s * w.np + p] * V * wc_w1q(q, w.R1) * (dd >= 0 ? 1.0 : -1.0) / w.R1;
+                L[4 * n + i] += dJ[(int64_t)s * w.np + p] * (-V / S1[4 * n + i]) * wc_w1(q, w.R1);
+            }
+        }
+        WcPre q;
+        wc_pre(o, y, rho, q);
+        const double* nb = w.nn[s].data();
+        const double* P = w.PP[s].data();
+        // per-particle part: position update, drag, the porosity's direct roles
+        for (int64_t i = 0; i < n; ++i) {
+            Ln[i] = Ln[n + i] = Ln[2 * n + i] = Ln[3 * n + i] = 0.0;
+            lax[i] = lay[i] = lD[i] = ln[i] = ort[i] = op[i] = 0.0;
+            if (!fluid(o, i)) continue;
+            const double ni = nb[i], vxn = S1[2 * n + i], vyn = S1[3 * n + i];
+            const double vm = std::sqrt(vx[i] * vx[i] + vy[i] * vy[i]), on = 1.0 - ni, n3 = ni * ni * ni;
+            const double R = -w.nu * w.alpha * on * on / (n3 * d * d) - w.beta * vm * on / (n3 * d);
+            const double D = 1.0 - dt * R * ni;
+            // x' = x + dt v'/n
+            Ln[i] = L[i];
+            Ln[n + i] = L[n + i];
+            const double lvx1 = L[2 * n + i] + dt * L[i] / ni, lvy1 = L[3 * n + i] + dt * L[n + i] / ni;
+            double lni = -dt * (L[i] * vxn + L[n + i] * vyn) / (ni * ni);
+            // v' = (v + dt a) / D
+            lax[i] = dt * lvx1 / D;
+            lay[i] = dt * lvy1 / D;
+            const double lDD = -(lvx1 * vxn + lvy1 * vyn) / D;
+            // D = 1 - dt R n
+            const double lR = -dt * ni * lDD;
+            lni += -dt * R * lDD;
+            const double dRdn = -w.nu * w.alpha / (d * d) * (-2.0 * on / n3 - 3.0 * on * on / (n3 * ni)) -
+                                w.beta * vm / d * (-1.0 / n3 - 3.0 * on / (n3 * ni));
+            lni += lR * dRdn;
+            Ln[2 * n + i] = lvx1 / D;
+            Ln[3 * n + i] = lvy1 / D;
+            if (vm > 0.0) {
+                const double c = lR * (-w.beta * on / (n3 * d)) / vm;
+                Ln[2 * n + i] += c * vx[i];
+                Ln[3 * n + i] += c * vy[i];
+            }
+            grad[0] += lR * (-w.nu * on * on / (n3 * d * d));
+            grad[1] += lR * (-vm * on / (n3 * d));
+            // a = -n P + visc + n g
+            lni += lax[i] * (-P[i]) + lay[i] * (-P[n + i] + g);
+            ln[i] = lni;
+            // rho' = rt + dt Drho
+            lD[i] = dt * L[4 * n + i];
+            ort[i] = L[4 * n + i];
+        }
+        // pair terms of particle i's sums, scattered to both ends
+        const std::vector<int64_t>& off = w.off[s];
+        const std::vector<int64_t>& ids = w.ids[s];
+        for (int64_t i = 0; i < n; ++i) {
+            if (!fluid(o, i)) continue;
+            const double rti = q.rt[i], pi_ = q.pp[i], ni = nb[i];
+            for (int64_t e = off[i]; e < off[i + 1]; ++e) {
+                const int64_t j = ids[e];
+                const bool fj = fluid(o, j);
+                const double dx = x[i] - x[j], dy = y[i] - y[j];
+                const double r2 = dx * dx + dy * dy, r = std::sqrt(r2);
+                const double F = wc_F(o, r), dF = wc_dF(o, r), den = r2 + lam;
+                const double G_ = F * r2 / den, dG = dF * r2 / den + F * 2.0 * r * lam / (den * den);
+                const double rtj = q.rt[j], pj = q.pp[j], mj = w.mass[j], Vj = mj / rtj;
+                const double dvx = vx[i] - vx[j], dvy = vy[i] - vy[j], dvd = dvx * dx + dvy * dy;
+                double gx = 0, gy = 0;  // adjoint of d = x_i - x_j
+                // continuity: m_j (rt_i / rt_j) F (v_ij . d)
+                {
+                    const double c = mj * rti / rtj, l = lD[i];
+                    ort[i] += l * (mj / rtj) * F * dvd;
+                    if (fj) ort[j] += l * (-mj * rti / (rtj * rtj)) * F * dvd;
+                    Ln[2 * n + i] += l * c * F * dx;
+                    Ln[3 * n + i] += l * c * F * dy;
+                    if (fj) {
+                        Ln[2 * n + j] -= l * c * F * dx;
+                        Ln[3 * n + j] -= l * c * F * dy;
+                    }
+                    gx += l * c * (F * dvx + dF / r * dvd * dx);
+                    gy += l * c * (F * dvy + dF / r * dvd * dy);
+                }
+                // delta term: c2 (rt_j - rt_i - rh_j + rh_i) (-G) V_j
+                {
+                    const double l = lD[i], del = rtj - rti - q.rh[j] + q.rh[i];
+                    ort[i] += l * w.c2 * G_ * Vj;
+                    if (fj) ort[j] += l * w.c2 * (-G_) * Vj * (1.0 - del / rtj);
+                    Ln[n + i] += l * w.c2 * q.drh[i] * (-G_) * Vj;
+                    if (fj) Ln[n + j] += l * w.c2 * q.drh[j] * G_ * Vj;
+                    gx += l * w.c2 * del * (-dG / r) * Vj * dx;
+                    gy += l * w.c2 * del * (-dG / r) * Vj * dy;
+                }
+                // pressure: -n_i m_j (p_i / rt_i^2 + p_j / rt_j^2) F d
+                {
+                    const double lad = lax[i] * dx + lay[i] * dy;
+                    const double pc = mj * (pi_ / (rti * rti) + pj / (rtj * rtj));
+                    gx += -ni * pc * (F * lax[i] + dF / r * lad * dx);
+                    gy += -ni * pc * (F * lay[i] + dF / r * lad * dy);
+                    op[i] += -ni * mj / (rti * rti) * F * lad;
+                    ort[i] += -ni * mj * (-2.0 * pi_ / (rti * rti * rti)) * F * lad;
+                    if (fj) {
+                        op[j] += -ni * mj / (rtj * rtj) * F * lad;
+                        ort[j] += -ni * mj * (-2.0 * pj / (rtj * rtj * rtj)) * F * lad;
+                    }
+                }
+                // viscosity: 2 nu V_j G (v_i - v_j)
+                {
+                    const double c = 2.0 * w.nu * Vj * G_, ldv = lax[i] * dvx + lay[i] * dvy;
+                    Ln[2 * n + i] += c * lax[i];
+                    Ln[3 * n + i] += c * lay[i];
+                    if (fj) {
+                        Ln[2 * n + j] -= c * lax[i];
+                        Ln[3 * n + j] -= c * lay[i];
+                        ort[j] += 2.0 * w.nu * (-mj / (rtj * rtj)) * G_ * ldv;
+                    }
+                    gx += 2.0 * w.nu * Vj * ldv * dG / r * dx;
+                    gy += 2.0 * w.nu * Vj * ldv * dG / r * dy;
+                }
+                Ln[i] += gx;
+                Ln[n + i] += gy;
+                if (fj) {
+                    Ln[j] -= gx;
+                    Ln[n + j] -= gy;
+                }
+            }
+            // porosity n_i = 1 - sum_s (1 - phi_s) V_s W(r_is)
+            for (int64_t sd = 0; sd < o->ns; ++sd) {
+                const double dx = x[i] - o->sx[sd], dy = y[i] - o->sy[sd], d2 = dx * dx + dy * dy;
+                if (!(d2 < H2)) continue;
+                const double r = std::sqrt(d2), F = wc_F(o, r);
+                Ln[i] += ln[i] * (-w.sw[sd] * F * dx);
+                Ln[n + i] += ln[i] * (-w.sw[sd] * F * dy);
+                if (w.sg[sd] >= 0) grad[2 + w.sg[sd]] += ln[i] * (o->sm[sd] / o->srho[sd]) * wc_W(o, r);
+            }
+        }
+        // pressure of the EOS, then the clamp rt = max(rho, rho0)
+        for (int64_t i = 0; i < n; ++i) {
+            if (!fluid(o, i)) {
+                Ln[4 * n + i] = 0.0;
+                continue;
+            }
+            const double rt = q.rt[i];
+            ort[i] += op[i] * w.B * w.gam * std::pow(rt / w.rho0, w.gam - 1.0) / w.rho0;
+            Ln[4 * n + i] = rho[i] >= w.rho0 ? ort[i] : 0.0;
+        }
+        L.swap(Ln);
+    }
+    return BSC_OK;
+}
+
+}  // extern "C"
