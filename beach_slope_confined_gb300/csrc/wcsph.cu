@@ -48,7 +48,7 @@ struct WcK {
     double alpha, beta;
     double inv_h, wend_F, wend_W;
     double gx0, gy0, gdx, gdy, por_default;
-    int gnx, gny, kmax, np;
+    int gnx, gny, kmax, np, gc;  // gc: grid cells one support can overlap
     double R1, depth;                          // probe kernel radius, probe depth
 };
 
@@ -72,6 +72,11 @@ struct WcState {
     int ck_cap = 0, seg_cap = 0, eta_cap = 0;
     double *seg = nullptr, *segn = nullptr, *segP = nullptr;  // (K+1) states; n; P (2n)
     int32_t *segnbr = nullptr, *segcnt = nullptr, *segpc = nullptr;  // lists, counts, cells
+    // what the reverse sweep reads from the recomputation, per step: the
+    // per-particle quotients, per-pair kernel values (F, F'/r, G, G'/r), the
+    // porosity gradient and the per-grid-cell kernel sums of the porosity
+    double *segpre = nullptr, *seggeo = nullptr, *segdn = nullptr, *segpgv = nullptr;
+    int32_t* segpgi = nullptr;
     // adjoint
     double *lam = nullptr, *lamn = nullptr;    // 5n each
     double *la = nullptr, *lD = nullptr, *ln = nullptr, *lvl = nullptr, *lrl = nullptr;
@@ -82,7 +87,7 @@ struct WcState {
 namespace {
 
 constexpr int WB = 128;
-constexpr int GC = 4;  // grid cells one particle's solids fall in, kept per thread
+constexpr int GCMAX = 9;  // grid cells one particle's kernel support can overlap (checked at setup)
 
 template <typename T>
 int wc_alloc(Ctx* c, WcState* w, T** p, int64_t count) {
@@ -185,39 +190,83 @@ __global__ void k_wc_copy(int64_t n, St src, St dst) {
     dst.rho[i] = src.rho[i];
 }
 
+// what the porosity pass keeps for the adjoint (null when not kept)
+struct PorKeep {
+    double* dn;    // grad n_i (2n)
+    int32_t* pgi;  // grid cell u of particle i at [u * n + i], -1 past the last
+    double* pgv;   // sum over that cell's solids of V_s W(r_is)
+};
+
 // porosity n_i from the solids in the 3x3 cells (fluid; 1 elsewhere)
-__global__ void k_wc_por(int64_t n, State S, KParams KP, WcK K, const int32_t* __restrict__ pcell,
-                         const int32_t* __restrict__ scs, const int32_t* __restrict__ scc,
-                         const double* __restrict__ sx, const double* __restrict__ sy, const double* __restrict__ sw,
-                         double* __restrict__ nout) {
+__global__ void __launch_bounds__(WB) k_wc_por(int64_t n, State S, KParams KP, WcK K, const int32_t* __restrict__ pcell,
+                                               const int32_t* __restrict__ scs, const int32_t* __restrict__ scc,
+                                               const double* __restrict__ sx, const double* __restrict__ sy,
+                                               const double* __restrict__ sw, const double* __restrict__ svol,
+                                               const int32_t* __restrict__ sg, double* __restrict__ nout, PorKeep kp) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (!is_fluid(S, i)) {
-        nout[i] = 1.0;
-        return;
+    int cg[GCMAX];
+    double cv[GCMAX];
+#pragma unroll
+    for (int u = 0; u < GCMAX; ++u) {
+        cg[u] = -1;
+        cv[u] = 0.0;
     }
-    const double xi = S.x[i], yi = S.y[i];
-    const int c = pcell[i], cx = c / KP.ny, cy = c - cx * KP.ny;
-    double frac = 0.0;
-    for (int ax = cx - 1; ax <= cx + 1; ++ax) {
-        if (ax < 0 || ax >= KP.nx) continue;
-        for (int ay = cy - 1; ay <= cy + 1; ++ay) {
-            if (ay < 0 || ay >= KP.ny) continue;
-            const int cc = ax * KP.ny + ay;
-            for (int s = scs[cc], e = scs[cc] + scc[cc]; s < e; ++s) {
-                const double dx = xi - sx[s], dy = yi - sy[s], d2 = dx * dx + dy * dy;
-                if (d2 < K.H2) frac += sw[s] * wW(K, sqrt(d2));
+    double frac = 0.0, gx = 0.0, gy = 0.0;
+    if (is_fluid(S, i)) {
+        const double xi = S.x[i], yi = S.y[i];
+        const int c = pcell[i], cx = c / KP.ny, cy = c - cx * KP.ny;
+        for (int ax = cx - 1; ax <= cx + 1; ++ax) {
+            if (ax < 0 || ax >= KP.nx) continue;
+            for (int ay = cy - 1; ay <= cy + 1; ++ay) {
+                if (ay < 0 || ay >= KP.ny) continue;
+                const int cc = ax * KP.ny + ay;
+                for (int s = scs[cc], e = scs[cc] + scc[cc]; s < e; ++s) {
+                    const double dx = xi - sx[s], dy = yi - sy[s], d2 = dx * dx + dy * dy;
+                    if (!(d2 < K.H2)) continue;
+                    const double r = sqrt(d2), W = wW(K, r);
+                    frac += sw[s] * W;
+                    if (kp.dn) {
+                        const double F = wF(K, r);
+                        gx -= sw[s] * F * dx;  // grad n = -sum sw grad W
+                        gy -= sw[s] * F * dy;
+                        const int g = sg[s];
+                        if (g < 0) continue;
+                        const double v = svol[s] * W;
+                        bool kept = false;
+#pragma unroll
+                        for (int u = 0; u < GCMAX; ++u) {
+                            if (!kept && u < K.gc && (cg[u] == g || cg[u] < 0)) {
+                                cg[u] = g;
+                                cv[u] += v;
+                                kept = true;
+                            }
+                        }
+                    }
+                }
             }
         }
     }
-    nout[i] = 1.0 - frac;
+    nout[i] = is_fluid(S, i) ? 1.0 - frac : 1.0;
+    if (kp.dn) {
+        kp.dn[i] = gx;
+        kp.dn[n + i] = gy;
+#pragma unroll
+        for (int u = 0; u < GCMAX; ++u) {
+            if (u < K.gc) {
+                kp.pgi[u * n + i] = cg[u];
+                kp.pgv[u * n + i] = cv[u];
+            }
+        }
+    }
 }
 
 // one step: next state; the porosity (in nbuf) and the pressure sum P
 // (2 per particle, for the adjoint) are kept
 __global__ void __launch_bounds__(WB) k_wc_step(int64_t n, State S, WcK K, const int32_t* __restrict__ nbr,
                                                 const int32_t* __restrict__ cnt, Pre pq,
-                                                const double* __restrict__ nbuf, St out, double* __restrict__ Pbuf) {
+                                                const double* __restrict__ nbuf, St out, double* __restrict__ Pbuf,
+                                                double* __restrict__ geo, int64_t slots) {
     const double* __restrict__ rt = pq.rt;
     const double* __restrict__ rh = pq.rh;
     const double* __restrict__ vol = pq.vol;
@@ -242,7 +291,16 @@ __global__ void __launch_bounds__(WB) k_wc_step(int64_t n, State S, WcK K, const
         const int j = nbr[ell(i, k, K.kmax)];
         const double dx = xi - S.x[j], dy = yi - S.y[j];
         const double r2 = dx * dx + dy * dy, r = sqrt(r2);
-        const double F = wF(K, r), G = F * r2 * rcp_nr(r2 + K.lam);
+        const double iden = rcp_nr(r2 + K.lam);
+        const double F = wF(K, r), G = F * r2 * iden;
+        if (geo) {  // F, F'/r, G, G'/r for the reverse sweep
+            const int64_t e = ell(i, k, K.kmax);
+            const double ir = rcp_nr(r), dF = wdF(K, r);
+            geo[e] = F;
+            geo[slots + e] = dF * ir;
+            geo[2 * slots + e] = G;
+            geo[3 * slots + e] = (dF * r2 + F * 2.0 * r * K.lam * iden) * iden * ir;
+        }
         const double rtj = rt[j], mj = S.mass[j], Vj = vol[j];
         const double dvx = vxi - S.vx[j], dvy = vyi - S.vy[j];
         Dr += rti * Vj * F * (dvx * dx + dvy * dy);  // m_j (rt_i / rt_j) F (v_ij . x_ij)
@@ -294,12 +352,19 @@ __global__ void __launch_bounds__(WB) k_wc_eta(int64_t n, const int8_t* __restri
     }
 }
 
+// one block per probe, fixed summation order
 __global__ void k_wc_eta_fin(int nb, WcK K, const double* __restrict__ part, double* __restrict__ eta) {
-    const int p = threadIdx.x;
-    if (p >= K.np) return;
+    __shared__ double sh[WB];
+    const int p = blockIdx.x;
     double s = 0.0;
-    for (int b = 0; b < nb; ++b) s += part[b * K.np + p];
-    eta[p] = s - K.depth;
+    for (int b = threadIdx.x; b < nb; b += WB) s += part[b * K.np + p];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = WB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) eta[p] = sh[0] - K.depth;
 }
 
 // ---- adjoint ---------------------------------------------------------------------
@@ -389,36 +454,28 @@ __global__ void __launch_bounds__(WB) k_wc_adj_local(int64_t n, const int8_t* __
 }
 
 // the pair part: for fluid particle k, the terms of its own sums (k as i) and
-// of its neighbours' sums (k as j), the porosity's geometry and grid terms;
-// writes the state adjoint lam_out for the state before the step
+// of its neighbours' sums (k as j), with the per-pair kernel values and the
+// porosity's gradient and per-grid-cell sums that the recomputation kept;
+// writes the state adjoint lam_out for the state before the step and the
+// block's porosity-grid partials
 __global__ void __launch_bounds__(WB) k_wc_adj_pair(
-    int64_t n, State S, WcK K, KParams KP, St s0, const int32_t* __restrict__ nbr, const int32_t* __restrict__ cnt,
-    Pre pq, const double* __restrict__ nbuf, const double* __restrict__ la,
+    int64_t n, State S, WcK K, St s0, const int32_t* __restrict__ nbr, const int32_t* __restrict__ cnt, Pre pq,
+    const double* __restrict__ geo, int64_t slots, const double* __restrict__ nbuf, const double* __restrict__ la,
     const double* __restrict__ lD, const double* __restrict__ ln, const double* __restrict__ lvl,
-    const double* __restrict__ lrl, St lam_in, St lam_out, const int32_t* __restrict__ pcell,
-    const int32_t* __restrict__ scs, const int32_t* __restrict__ scc, const double* __restrict__ sx,
-    const double* __restrict__ sy, const double* __restrict__ sw, const double* __restrict__ svol,
-    const int32_t* __restrict__ sg, double* __restrict__ part, int pstride) {
-    // grid-porosity partials: each thread keeps up to GC cells of its own,
-    // summed per cell by the block in a fixed order; a thread that meets more
-    // cells (a grid finer than the kernel support) adds the rest atomically
-    __shared__ double bins[BSC_WCSPH_MAX_GRID];
-    __shared__ double cv[GC * WB];
-    __shared__ int cg[GC * WB];
-    for (int g = threadIdx.x; g < K.gnx * K.gny; g += blockDim.x) bins[g] = 0.0;
-    int mg[GC];
-    double mv[GC];
-#pragma unroll
-    for (int u = 0; u < GC; ++u) {
-        mg[u] = -1;
-        mv[u] = 0.0;
-    }
+    const double* __restrict__ lrl, St lam_in, St lam_out, const double* __restrict__ dn,
+    const int32_t* __restrict__ pgi, const double* __restrict__ pgv, double* __restrict__ part, int pstride) {
+    // grid-porosity partials per warp, then summed over the warps in order
+    __shared__ double wb[WB / 32][BSC_WCSPH_MAX_GRID];
+    const int G = K.gnx * K.gny;
+    for (int e = threadIdx.x; e < (WB / 32) * BSC_WCSPH_MAX_GRID; e += WB) (&wb[0][0])[e] = 0.0;
     __syncthreads();
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k < n && S.tid[k] == BSC_TID_FLUID) {
-        const double xk = s0.x[k], yk = s0.y[k], vxk = s0.vx[k], vyk = s0.vy[k];
+    const bool act = k < n && S.tid[k] == BSC_TID_FLUID;
+    double lnk = 0.0;
+    if (act) {
         const double* __restrict__ rt = pq.rt;
         const double* __restrict__ rh = pq.rh;
+        const double xk = s0.x[k], yk = s0.y[k], vxk = s0.vx[k], vyk = s0.vy[k];
         const double rtk = rt[k], pk = pq.pp[k], rhk = rh[k], drk = pq.drh[k], nk = nbuf[k], mk = S.mass[k];
         const double Vk = pq.vol[k], prk = pq.pr[k], irk = 1.0 / rtk;
         const double mk_rt2 = mk * irk * irk, pk_rt3 = 2.0 * prk * irk;  // m_k / rt_k^2, 2 p_k / rt_k^3
@@ -428,11 +485,10 @@ __global__ void __launch_bounds__(WB) k_wc_adj_pair(
         double lxx = lam_in.x[k], lyy = lam_in.y[k];
         const int m = cnt[k];
         for (int q = 0; q < m; ++q) {
-            const int j = nbr[ell(k, q, K.kmax)];
+            const int64_t e = ell(k, q, K.kmax);
+            const int j = nbr[e];
             const double dx = xk - s0.x[j], dy = yk - s0.y[j];
-            const double r2 = dx * dx + dy * dy, r = sqrt(r2), ir = rcp_nr(r);
-            const double F = wF(K, r), dF = wdF(K, r), iden = rcp_nr(r2 + K.lam);
-            const double G = F * r2 * iden, dG = (dF * r2 + F * 2.0 * r * K.lam * iden) * iden;
+            const double F = geo[e], Fr = geo[slots + e], G_ = geo[2 * slots + e], Gr = geo[3 * slots + e];
             const double rtj = rt[j], prj = pq.pr[j], mj = S.mass[j], Vj = pq.vol[j];
             const double dvx = vxk - s0.vx[j], dvy = vyk - s0.vy[j], dvd = dvx * dx + dvy * dy;
             double gx = 0.0, gy = 0.0;  // adjoint of d = x_k - x_j
@@ -442,13 +498,13 @@ __global__ void __launch_bounds__(WB) k_wc_adj_pair(
                 lrt += lDk * Vj * F * dvd;
                 lvx += lDk * c1 * F * dx;
                 lvy += lDk * c1 * F * dy;
-                const double t = lDk * c1 * dF * dvd * ir;
+                const double t = lDk * c1 * Fr * dvd;
                 gx += lDk * c1 * F * dvx + t * dx;
                 gy += lDk * c1 * F * dvy + t * dy;
                 const double del = rtj - rtk - rh[j] + rhk;
-                lrt += lDk * K.c2 * G * Vj;
-                lyy += lDk * K.c2 * drk * (-G) * Vj;
-                const double u = lDk * K.c2 * del * (-dG) * Vj * ir;
+                lrt += lDk * K.c2 * G_ * Vj;
+                lyy += lDk * K.c2 * drk * (-G_) * Vj;
+                const double u = -lDk * K.c2 * del * Gr * Vj;
                 gx += u * dx;
                 gy += u * dy;
             }
@@ -456,14 +512,14 @@ __global__ void __launch_bounds__(WB) k_wc_adj_pair(
             {
                 const double lad = lax * dx + lay * dy;
                 const double pc = mj * (prk + prj);
-                gx += -nk * pc * (F * lax + dF * ir * lad * dx);
-                gy += -nk * pc * (F * lay + dF * ir * lad * dy);
+                gx += -nk * pc * (F * lax + Fr * lad * dx);
+                gy += -nk * pc * (F * lay + Fr * lad * dy);
                 lp += -nk * mj * irk * irk * F * lad;
                 lrt += nk * mj * pk_rt3 * F * lad;
                 const double vc = 2.0 * K.nu * Vj;
-                lvx += vc * G * lax;
-                lvy += vc * G * lay;
-                const double w = vc * (lax * dvx + lay * dvy) * dG * ir;
+                lvx += vc * G_ * lax;
+                lvy += vc * G_ * lay;
+                const double w = vc * (lax * dvx + lay * dvy) * Gr;
                 gx += w * dx;
                 gy += w * dy;
             }
@@ -481,31 +537,31 @@ __global__ void __launch_bounds__(WB) k_wc_adj_pair(
                 lvx += lDj * (-c1 * F * ex);
                 lvy += lDj * (-c1 * F * ey);
                 {
-                    const double t = lDj * c1 * dF * dvd * ir;
+                    const double t = lDj * c1 * Fr * dvd;
                     hx += lDj * c1 * F * dwx + t * ex;
                     hy += lDj * c1 * F * dwy + t * ey;
                 }
                 const double del = rtk - rtj - rhk + rh[j];
-                lrt += lDj * K.c2 * (-G) * Vk * (1.0 - del * irk);
-                lyy += lDj * K.c2 * drk * G * Vk;
+                lrt += lDj * K.c2 * (-G_) * Vk * (1.0 - del * irk);
+                lyy += lDj * K.c2 * drk * G_ * Vk;
                 {
-                    const double u = lDj * K.c2 * del * (-dG) * Vk * ir;
+                    const double u = -lDj * K.c2 * del * Gr * Vk;
                     hx += u * ex;
                     hy += u * ey;
                 }
                 // momentum of j
                 const double lad = lajx * ex + lajy * ey;
                 const double pc = mk * (prj + prk);
-                hx += -nj * pc * (F * lajx + dF * ir * lad * ex);
-                hy += -nj * pc * (F * lajy + dF * ir * lad * ey);
+                hx += -nj * pc * (F * lajx + Fr * lad * ex);
+                hy += -nj * pc * (F * lajy + Fr * lad * ey);
                 lp += -nj * mk_rt2 * F * lad;
                 lrt += nj * mk * pk_rt3 * F * lad;
                 const double vc = 2.0 * K.nu * Vk;
-                lvx += -vc * G * lajx;
-                lvy += -vc * G * lajy;
+                lvx += -vc * G_ * lajx;
+                lvy += -vc * G_ * lajy;
                 const double ldv = lajx * dwx + lajy * dwy;
-                lrt += -2.0 * K.nu * mk_rt2 * G * ldv;
-                const double w = vc * ldv * dG * ir;
+                lrt += -2.0 * K.nu * mk_rt2 * G_ * ldv;
+                const double w = vc * ldv * Gr;
                 hx += w * ex;
                 hy += w * ey;
                 gx -= hx;
@@ -514,38 +570,10 @@ __global__ void __launch_bounds__(WB) k_wc_adj_pair(
             lxx += gx;
             lyy += gy;
         }
-        // porosity: n_k = 1 - sum_s (1 - phi_s) V_s W(r_ks)
-        const double lnk = ln[k];
-        if (lnk != 0.0) {
-            const int c = pcell[k], cx = c / KP.ny, cy = c - cx * KP.ny;
-            for (int ax = cx - 1; ax <= cx + 1; ++ax) {
-                if (ax < 0 || ax >= KP.nx) continue;
-                for (int ay = cy - 1; ay <= cy + 1; ++ay) {
-                    if (ay < 0 || ay >= KP.ny) continue;
-                    const int cc = ax * KP.ny + ay;
-                    for (int s = scs[cc], e = scs[cc] + scc[cc]; s < e; ++s) {
-                        const double dx = xk - sx[s], dy = yk - sy[s], d2 = dx * dx + dy * dy;
-                        if (!(d2 < K.H2)) continue;
-                        const double r = sqrt(d2), F = wF(K, r);
-                        lxx += lnk * (-sw[s] * F * dx);
-                        lyy += lnk * (-sw[s] * F * dy);
-                        const int gs = sg[s];
-                        if (gs < 0) continue;
-                        const double v = lnk * svol[s] * wW(K, r);
-                        bool kept = false;
-#pragma unroll
-                        for (int u = 0; u < GC; ++u) {
-                            if (!kept && (mg[u] == gs || mg[u] < 0)) {
-                                mg[u] = gs;
-                                mv[u] += v;
-                                kept = true;
-                            }
-                        }
-                        if (!kept) atomicAdd(&bins[gs], v);
-                    }
-                }
-            }
-        }
+        // porosity n_k = 1 - sum_s (1 - phi_s) V_s W(r_ks)
+        lnk = ln[k];
+        lxx += lnk * dn[k];
+        lyy += lnk * dn[n + k];
         // pressure and the clamp
         lrt += lp * K.B * K.gam * pow(rtk / K.rho0, K.gam - 1.0) / K.rho0;
         lam_out.x[k] = lxx;
@@ -556,27 +584,46 @@ __global__ void __launch_bounds__(WB) k_wc_adj_pair(
     } else if (k < n) {
         lam_out.x[k] = lam_out.y[k] = lam_out.vx[k] = lam_out.vy[k] = lam_out.rho[k] = 0.0;
     }
-#pragma unroll
-    for (int u = 0; u < GC; ++u) {
-        cg[u * WB + threadIdx.x] = mg[u];
-        cv[u * WB + threadIdx.x] = mv[u];
+    // d n_k / d phi_g = sum over cell g's solids of V_s W(r_ks): lanes with the
+    // same cell are summed in lane order by the lowest of them
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int u = 0; u < K.gc; ++u) {
+        int g = -1;
+        double v = 0.0;
+        if (act) {
+            g = pgi[u * n + k];
+            v = lnk * pgv[u * n + k];
+        }
+        const unsigned grp = __match_any_sync(0xffffffffu, g);
+        double acc = 0.0;
+        for (int src = 0; src < 32; ++src) {
+            const double t = __shfl_sync(0xffffffffu, v, src);
+            if ((grp >> src) & 1u) acc += t;
+        }
+        if (g >= 0 && lane == __ffs(grp) - 1) wb[warp][g] += acc;
+        __syncwarp();
     }
     __syncthreads();
-    for (int g = threadIdx.x; g < K.gnx * K.gny; g += blockDim.x) {
-        double acc = bins[g];
-        for (int e = 0; e < GC * WB; ++e)
-            if (cg[e] == g) acc += cv[e];
+    for (int g = threadIdx.x; g < G; g += WB) {
+        double acc = 0.0;
+        for (int q = 0; q < WB / 32; ++q) acc += wb[q][g];
         part[(int64_t)blockIdx.x * pstride + 2 + g] = acc;
     }
 }
 
-// grad[q] += sum over blocks of part[block][q], fixed order
-__global__ void k_wc_grad(int nb, int nq, int pstride, const double* __restrict__ part, double* __restrict__ grad) {
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= nq) return;
+// grad[q] += sum over blocks of part[block][q]: one block per q, fixed order
+__global__ void k_wc_grad(int nb, int pstride, const double* __restrict__ part, double* __restrict__ grad) {
+    __shared__ double sh[WB];
+    const int q = blockIdx.x;
     double s = 0.0;
-    for (int b = 0; b < nb; ++b) s += part[(int64_t)b * pstride + q];
-    grad[q] += s;
+    for (int b = threadIdx.x; b < nb; b += WB) s += part[(int64_t)b * pstride + q];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = WB / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) sh[threadIdx.x] += sh[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) grad[q] += sh[0];
 }
 
 }  // namespace
@@ -631,35 +678,59 @@ int wc_copy(Ctx* c, St src, St dst) {
 int wc_save(Ctx* c, double* dst) { return wc_copy(c, st_ctx(c), st_of(dst, c->n)); }
 int wc_load(Ctx* c, const double* src) { return wc_copy(c, st_of(const_cast<double*>(src), c->n), st_ctx(c)); }
 
+// what the recomputation of a segment keeps of one step for the reverse sweep
+struct Keep {
+    int32_t *nbr, *cnt, *cell;  // neighbour lists, counts, particle cells
+    Pre pre;                    // per-particle quotients
+    double* geo;                // per-pair kernel values (4 x slots)
+    PorKeep por;                // porosity gradient and per-grid-cell sums
+};
+
+int64_t list_slots(const Ctx* c) { return ((c->n + 31) / 32) * 32 * (int64_t)c->K.kmax; }
+
+Keep seg_keep(WcState* w, int q, int64_t n, int64_t slots) {
+    double* pre = w->segpre + (int64_t)q * 6 * n;
+    const int gc = w->K.gc;
+    return {w->segnbr + (int64_t)q * slots,
+            w->segcnt + (int64_t)q * n,
+            w->segpc + (int64_t)q * n,
+            {pre, pre + n, pre + 2 * n, pre + 3 * n, pre + 4 * n, pre + 5 * n},
+            w->seggeo + (int64_t)q * 4 * slots,
+            {w->segdn + (int64_t)q * 2 * n, w->segpgi + (int64_t)q * gc * n, w->segpgv + (int64_t)q * gc * n}};
+}
+
 // One step on c->S; keeps the porosity and the pressure sum in nbuf and Pbuf.
-// Non-null keep_* receive the step's neighbour lists, counts and particle
-// cells (the recomputation of a segment keeps them for the reverse sweep):
-// the context's own buffers are pointed there for the step.
-int wc_step(Ctx* c, WcState* w, double* nbuf, double* Pbuf, int32_t* keep_nbr = nullptr,
-            int32_t* keep_cnt = nullptr, int32_t* keep_cell = nullptr) {
+// With `keep`, the step's lists, counts and cells are built straight into the
+// kept buffers (the context's own are pointed there for the step), and the
+// per-particle quotients, per-pair kernel values and porosity derivatives
+// are kept too.
+int wc_step(Ctx* c, WcState* w, double* nbuf, double* Pbuf, const Keep* keep = nullptr) {
     const int64_t n = c->n;
     c->t += w->K.dt;
     int32_t *own_nbr = c->nbr, *own_cnt = c->cnt, *own_cell = c->pcell;
-    if (keep_nbr) {
-        c->nbr = keep_nbr;
-        c->cnt = keep_cnt;
-        c->pcell = keep_cell;
+    if (keep) {
+        c->nbr = keep->nbr;
+        c->cnt = keep->cnt;
+        c->pcell = keep->cell;
     }
+    const Pre pre = keep ? keep->pre : wc_pre(w);
     int rc = op_piston(c);
     if (!rc) rc = cells_build(c, false);
     if (!rc) rc = op_neighbour(c);
     if (!rc) {
         const unsigned g = blocks_for(n, WB);
         const State S = wc_view(c, w);
-        k_wc_pre<<<g, WB, 0, c->stream>>>(n, S.tid, S.mass, S.y, S.rho, w->K, wc_pre(w));
+        k_wc_pre<<<g, WB, 0, c->stream>>>(n, S.tid, S.mass, S.y, S.rho, w->K, pre);
         rc = launch_check(c);
         if (!rc) {
             k_wc_por<<<g, WB, 0, c->stream>>>(n, S, c->K, w->K, c->pcell, c->scell_start, c->scell_count, c->sx,
-                                              c->sy, w->sw, nbuf);
+                                              c->sy, w->sw, c->svol, w->sg, nbuf,
+                                              keep ? keep->por : PorKeep{nullptr, nullptr, nullptr});
             rc = launch_check(c);
         }
         if (!rc) {
-            k_wc_step<<<g, WB, 0, c->stream>>>(n, S, w->K, c->nbr, c->cnt, wc_pre(w), nbuf, st_of(w->nxt, n), Pbuf);
+            k_wc_step<<<g, WB, 0, c->stream>>>(n, S, w->K, c->nbr, c->cnt, pre, nbuf, st_of(w->nxt, n), Pbuf,
+                                               keep ? keep->geo : nullptr, list_slots(c));
             rc = launch_check(c);
         }
     }
@@ -724,6 +795,11 @@ int bsc_wcsph_setup(bsc_ctx* c, const bsc_wcsph_params* p) {
     K.np = p->nprobe;
     K.R1 = 2.0 * KP.h;
     K.depth = p->probe_depth;
+    // grid cells a kernel support (diameter 4h) can overlap
+    const int ncx = std::min(p->grid_nx, (int)std::floor(4.0 * KP.h / p->grid_dx) + 2);
+    const int ncy = std::min(p->grid_ny, (int)std::floor(4.0 * KP.h / p->grid_dy) + 2);
+    K.gc = ncx * ncy;
+    if (K.gc > GCMAX) return set_err(c, BSC_E_INVALID, "wcsph_setup: porosity grid cells smaller than 2h");
     int rc;
     if ((rc = wc_alloc(c, w, &w->init, 5 * n)) || (rc = wc_alloc(c, w, &w->mass, n)) ||
         (rc = wc_alloc(c, w, &w->theta, G)) ||
@@ -770,12 +846,17 @@ int bsc_wcsph_forward(bsc_ctx* c, int32_t nsteps, int32_t every, double* eta) {
         w->eta_cap = nsteps;
     }
     if (every > w->seg_cap) {
-        const int64_t slots = ((n + 31) / 32) * 32 * (int64_t)c->K.kmax;
+        const int64_t slots = list_slots(c), gc = w->K.gc;
         if ((rc = wc_alloc(c, w, &w->seg, (int64_t)(every + 1) * 5 * n)) ||
             (rc = wc_alloc(c, w, &w->segn, (int64_t)every * n)) || (rc = wc_alloc(c, w, &w->segP, (int64_t)every * 2 * n)) ||
             (rc = wc_alloc(c, w, &w->segnbr, (int64_t)every * slots)) ||
             (rc = wc_alloc(c, w, &w->segcnt, (int64_t)every * n)) ||
-            (rc = wc_alloc(c, w, &w->segpc, (int64_t)every * n)))
+            (rc = wc_alloc(c, w, &w->segpc, (int64_t)every * n)) ||
+            (rc = wc_alloc(c, w, &w->segpre, (int64_t)every * 6 * n)) ||
+            (rc = wc_alloc(c, w, &w->seggeo, (int64_t)every * 4 * slots)) ||
+            (rc = wc_alloc(c, w, &w->segdn, (int64_t)every * 2 * n)) ||
+            (rc = wc_alloc(c, w, &w->segpgi, (int64_t)every * gc * n)) ||
+            (rc = wc_alloc(c, w, &w->segpgv, (int64_t)every * gc * n)))
             return rc;
         w->seg_cap = every;
     }
@@ -793,7 +874,7 @@ int bsc_wcsph_forward(bsc_ctx* c, int32_t nsteps, int32_t every, double* eta) {
         if ((rc = wc_step(c, w, w->segn, w->segP))) return rc;
         k_wc_eta<<<nb, WB, 0, c->stream>>>(n, c->S.tid, w->mass, st_of(w->nxt, n), w->K, w->xp, w->part);
         BSC_LAUNCH(c);
-        k_wc_eta_fin<<<1, 32, 0, c->stream>>>(nb, w->K, w->part, w->eta + (int64_t)s * w->K.np);
+        k_wc_eta_fin<<<w->K.np, WB, 0, c->stream>>>(nb, w->K, w->part, w->eta + (int64_t)s * w->K.np);
         BSC_LAUNCH(c);
     }
     BSC_CUDA(c, cudaMemcpyAsync(eta, w->eta, sizeof(double) * nsteps * w->K.np, cudaMemcpyDeviceToHost, c->stream));
@@ -815,7 +896,7 @@ int bsc_wcsph_adjoint(bsc_ctx* c, const double* dJ_deta, double* grad) {
     const int nsteps = w->nsteps, every = w->every, np = w->K.np, G = w->G;
     const unsigned nb = blocks_for(n, WB);
     const int pstride = 2 + BSC_WCSPH_MAX_GRID;
-    const int64_t slots = ((n + 31) / 32) * 32 * (int64_t)c->K.kmax;
+    const int64_t slots = list_slots(c);
     int rc;
     BSC_CUDA(c, cudaMemcpyAsync(w->dJ, dJ_deta, sizeof(double) * nsteps * np, cudaMemcpyHostToDevice, c->stream));
     BSC_CUDA(c, cudaMemsetAsync(w->lam, 0, sizeof(double) * 5 * n, c->stream));
@@ -829,9 +910,8 @@ int bsc_wcsph_adjoint(bsc_ctx* c, const double* dJ_deta, double* grad) {
         for (int s = s0; s < s1; ++s) {
             const int q = s - s0;
             if ((rc = wc_save(c, w->seg + (int64_t)q * 5 * n))) return rc;
-            if ((rc = wc_step(c, w, w->segn + (int64_t)q * n, w->segP + (int64_t)q * 2 * n,
-                              w->segnbr + (int64_t)q * slots, w->segcnt + (int64_t)q * n, w->segpc + (int64_t)q * n)))
-                return rc;
+            const Keep kq = seg_keep(w, q, n, slots);
+            if ((rc = wc_step(c, w, w->segn + (int64_t)q * n, w->segP + (int64_t)q * 2 * n, &kq))) return rc;
         }
         if ((rc = wc_save(c, w->seg + (int64_t)(s1 - s0) * 5 * n))) return rc;
         // reverse through the segment
@@ -843,22 +923,17 @@ int bsc_wcsph_adjoint(bsc_ctx* c, const double* dJ_deta, double* grad) {
             k_wc_adj_probe<<<nb, WB, 0, c->stream>>>(n, c->S.tid, w->mass, st1, w->K, w->xp,
                                                      w->dJ + (int64_t)s * np, lam);
             BSC_LAUNCH(c);
-            // the step's per-particle quantities at the state before it
             const State S = wc_view(c, w);
-            k_wc_pre<<<nb, WB, 0, c->stream>>>(n, S.tid, S.mass, st0.y, st0.rho, w->K, wc_pre(w));
-            BSC_LAUNCH(c);
+            const Keep kq = seg_keep(w, q, n, slots);
             const double* nq = w->segn + (int64_t)q * n;
             k_wc_adj_local<<<nb, WB, 0, c->stream>>>(n, c->S.tid, w->K, st0, st1, nq, w->segP + (int64_t)q * 2 * n, lam,
                                                      w->la, w->lD, w->ln, w->lvl, w->lrl, w->part, pstride);
             BSC_LAUNCH(c);
-            k_wc_adj_pair<<<nb, WB, 0, c->stream>>>(n, S, w->K, c->K, st0, w->segnbr + (int64_t)q * slots,
-                                                    w->segcnt + (int64_t)q * n, wc_pre(w), nq, w->la,
-                                                    w->lD, w->ln, w->lvl, w->lrl, lam, lamn, w->segpc + (int64_t)q * n,
-                                                    c->scell_start,
-                                                    c->scell_count, c->sx, c->sy, w->sw, c->svol, w->sg, w->part,
-                                                    pstride);
+            k_wc_adj_pair<<<nb, WB, 0, c->stream>>>(n, S, w->K, st0, kq.nbr, kq.cnt, kq.pre, kq.geo, slots, nq,
+                                                    w->la, w->lD, w->ln, w->lvl, w->lrl, lam, lamn, kq.por.dn,
+                                                    kq.por.pgi, kq.por.pgv, w->part, pstride);
             BSC_LAUNCH(c);
-            k_wc_grad<<<1, 2 + BSC_WCSPH_MAX_GRID, 0, c->stream>>>(nb, 2 + G, pstride, w->part, w->grad);
+            k_wc_grad<<<2 + G, WB, 0, c->stream>>>(nb, pstride, w->part, w->grad);
             BSC_LAUNCH(c);
             std::swap(w->lam, w->lamn);
         }

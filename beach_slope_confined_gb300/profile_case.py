@@ -7,6 +7,11 @@ full steps with every PPE solve capped at ``maxit`` Krylov iterations, so a
 profiler sees a few launches of each kernel of the step on the full-size
 state.  A capped solve reports BSC_E_NOT_CONVERGED, which is expected here
 and ignored; any other error raises.  Prints ``ok`` and the particle count.
+
+    python -m beach_slope_confined_gb300.profile_case c4 fp64 --wcsph 20 --every 10
+
+runs the WCSPH calibration workload instead: a forward run of 20 steps with
+checkpoints every 10, then the adjoint of a probe functional.
 """
 from __future__ import annotations
 
@@ -24,9 +29,24 @@ def main(argv=None):
     ap.add_argument("maxit", nargs="?", type=int, default=10)
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--precond", default="none", choices=("none", "mg"))
+    ap.add_argument("--wcsph", type=int, default=0, help="WCSPH forward + adjoint steps instead of ISPH steps")
+    ap.add_argument("--every", type=int, default=10, help="WCSPH checkpoint interval")
     args = ap.parse_args(argv)
     spec = sc.config_spec(args.config)
     scen = sc.build(spec)
+    if args.wcsph > 0:
+        import numpy as np
+
+        g = Solver(sc.make_params(spec, scen.bounds, precision="fp64"))
+        setup_tank(g, scen)
+        wp, _grid = sc.wcsph_params(spec, scen)
+        g.wcsph_setup(wp)
+        g.wcsph_forward(args.wcsph, args.every)
+        g.wcsph_adjoint(np.ones((args.wcsph, len(spec.probes))))
+        g.synchronize()
+        g.close()
+        print("ok", scen.n)
+        return
     # the inner-solve settings of bench.py for each preconditioner
     mg = args.precond == "mg"
     P = sc.make_params(spec, scen.bounds, precision=args.precision, tol=1e-8, maxit=args.maxit,
