@@ -276,15 +276,21 @@ int bsc_csr_solve_noalloc(const bsc_params* p, int32_t n, const int32_t* rowptr,
 /* ---- differentiable WCSPH step and its adjoint ------------------------------ */
 /* A weakly compressible step on the uploaded state (fluid, walls, piston and
  * porous solids of the ISPH context; FP64 context, Wendland C2 kernel):
- * Tait EOS clamped at zero pressure, continuity with delta-SPH diffusion and
- * the hydrostatic correction (wcsph.f90:13-129), symmetric pressure gradient,
- * Morris viscosity, gravity, implicit Darcy-Forchheimer drag and the
- * position update.  The calibrated parameters are the drag coefficients and
- * the porosity of a grid of cells over the slope (each solid takes the
- * porosity of the cell it lies in; solids outside the grid keep por).  The
- * adjoint returns the gradient of any loss of the probe elevations, with the
- * neighbour lists of every step frozen, recomputing each segment of
- * ckpt_every steps from a checkpoint. */
+ * Tait EOS clamped at zero pressure (dentopress, wcsph.f90:35-63),
+ * continuity with delta-SPH diffusion and the hydrostatic correction
+ * (calmasscons and updateden, wcsph.f90:65-154), symmetric pressure gradient,
+ * Morris viscosity, gravity, implicit Darcy-Forchheimer drag (the Ergun form
+ * of porous.f90:192-212) and the position update.  The reference's module
+ * holds only those formulae and is not part of its build; these entry points
+ * replace a WCSPH step loop built on them.  The calibrated parameters are the
+ * drag coefficients and the porosity of a grid of cells over the slope (each
+ * solid takes the porosity of the cell it lies in; solids outside the grid
+ * keep por).  Grid cells must be at least 2h on a side, so that one kernel
+ * support overlaps at most nine of them.  The adjoint returns the gradient of
+ * any loss of the probe elevations, with the neighbour lists of every step
+ * frozen, recomputing each segment of ckpt_every steps from a checkpoint; a
+ * segment keeps about 4.5 kmax + 30 doubles per particle per step in device
+ * memory. */
 #define BSC_WCSPH_MAX_GRID 256
 #define BSC_WCSPH_MAX_PROBES 16
 typedef struct bsc_wcsph_params {
