@@ -175,7 +175,7 @@ static int alloc_for(Ctx* c, int64_t n) {
         if ((rc = dalloc(c, &tw, 6 * n))) return rc;
         c->f_vol = tw; c->f_nu = tw + n; c->f_nut = tw + 2 * n; c->f_tke = tw + 3 * n; c->f_varts = tw + 4 * n;
         c->f_q = tw + 5 * n;
-        if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->avalf, slots)) ||
+        if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->ellf, slots)) ||
             (rc = dalloc(c, &c->avalh, slots)))
             return rc;
     }

@@ -262,7 +262,7 @@ struct Ctx {
 
     // PPE
     double* aval = nullptr;       // FP64 off-diagonals (ELL layout)
-    float* avalf = nullptr;       // FP32 off-diagonals (mixed)
+    int2* ellf = nullptr;         // FP32 off-diagonals with their columns, packed (mixed)
     __half* avalh = nullptr;      // FP16 off-diagonals (mixed): the V-cycle's fine-level sweeps
     double* b = nullptr;
     float* bf = nullptr;

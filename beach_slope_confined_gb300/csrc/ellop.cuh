@@ -17,7 +17,7 @@ struct EllOp {
     const int32_t* nbr;
     const int32_t* cnt;
     int kmax;
-    int unroll = 0;  // 1: four entries per round (four gathers in flight)
+    int unroll = 0;  // 1: eight, then four entries per round (that many gathers in flight)
     const void* key() const { return aval; }
     // the column stride of the ELL layout is 32 slots
     template <typename X, typename A>
@@ -26,6 +26,21 @@ struct EllOp {
         const int m = cnt[i];
         const int64_t e0 = ell(i, 0, kmax);
         int k = 0;
+        for (; unroll && k + 8 <= m; k += 8) {
+            const int64_t e = e0 + (int64_t)k * 32;
+            int j[8];
+            T a[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                j[u] = nbr[e + 32 * u];
+                a[u] = aval[e + 32 * u];
+            }
+            X xv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) xv[u] = x[j[u]];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += (A)a[u] * (A)xv[u];
+        }
         for (; unroll && k + 4 <= m; k += 4) {
             const int64_t e = e0 + (int64_t)k * 32;
             const int j0 = nbr[e], j1 = nbr[e + 32], j2 = nbr[e + 64], j3 = nbr[e + 96];
@@ -39,6 +54,48 @@ struct EllOp {
         for (; k < m; ++k) {
             const int64_t e = e0 + (int64_t)k * 32;
             s += (A)aval[e] * (A)x[nbr[e]];
+        }
+        return s;
+    }
+};
+
+// The mixed path's FP32 copy of I + N: each stored entry's column and value
+// packed in one 8-byte word, so an entry is one load (the same 8 bytes per
+// entry as separate column and value arrays, half the load instructions).
+struct EllPackF {
+    const int2* ent;
+    const int32_t* cnt;
+    int kmax;
+    const void* key() const { return ent; }
+    template <typename X, typename A>
+    __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
+        A s = (A)x[i];
+        const int m = cnt[i];
+        const int64_t e0 = ell(i, 0, kmax);
+        int k = 0;
+        for (; k + 8 <= m; k += 8) {
+            int2 p[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) p[u] = ent[e0 + (int64_t)(k + u) * 32];
+            X xv[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) xv[u] = x[p[u].x];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) s += (A)__int_as_float(p[u].y) * (A)xv[u];
+        }
+        for (; k + 4 <= m; k += 4) {
+            int2 p[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) p[u] = ent[e0 + (int64_t)(k + u) * 32];
+            X xv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xv[u] = x[p[u].x];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) s += (A)__int_as_float(p[u].y) * (A)xv[u];
+        }
+        for (; k < m; ++k) {
+            const int2 p = ent[e0 + (int64_t)k * 32];
+            s += (A)__int_as_float(p.y) * (A)x[p.x];
         }
         return s;
     }

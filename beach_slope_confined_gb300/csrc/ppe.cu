@@ -40,7 +40,7 @@ template <typename R, bool FAST>
 __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                         const typename Vec2<R>::type* __restrict__ gw,
                                                         const int32_t* __restrict__ cnt, R* __restrict__ aval,
-                                                        float* __restrict__ avalf, __half* __restrict__ avalh,
+                                                        int2* __restrict__ ellf, __half* __restrict__ avalh,
                                                         double* __restrict__ b, const double* __restrict__ q,
                                                         const double* __restrict__ usx, const double* __restrict__ usy,
                                                         double dt) {
@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
         // zero-neighbour guard: identity row, b = 0 (the reference divides by 0)
         for (int k = 0; k < m; ++k) {
             aval[ell(i, k, K.kmax)] = 0;
-            if (avalf) avalf[ell(i, k, K.kmax)] = 0.f;
+            if (ellf) ellf[ell(i, k, K.kmax)] = make_int2(nbr[ell(i, k, K.kmax)], 0);
             if (avalh) avalh[ell(i, k, K.kmax)] = __float2half_rn(0.f);
         }
         b[i] = 0.0;
@@ -130,9 +130,9 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
         const int64_t e = ell(i, k, K.kmax);
         const R v = aval[e] * inv;
         aval[e] = v;
-        if (avalf) {  // the mixed path's inner-sweep copy (rounded on the integer pipe) and V-cycle copy
+        if (ellf) {  // the mixed path's inner-sweep copy (rounded on the integer pipe) and V-cycle copy
             const float vf = f32_of(v);
-            avalf[e] = vf;
+            ellf[e] = make_int2(nbr[e], __float_as_int(vf));
             avalh[e] = __float2half_rn(vf);
         }
     }
@@ -160,10 +160,10 @@ int op_ppe_assemble(Ctx* c) {
     // mixed path keeps an FP32 copy for its inner sweeps
     if (c->mixed && !c->exact_div)
         k_assemble<double, true><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
-                                                                c->avalf, c->avalh, c->b, q, ux, uy, c->dt);
+                                                                c->ellf, c->avalh, c->b, q, ux, uy, c->dt);
     else
         k_assemble<double, false><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
-                                                                 c->mixed ? c->avalf : nullptr,
+                                                                 c->mixed ? c->ellf : nullptr,
                                                                  c->mixed ? c->avalh : nullptr, c->b, q, ux, uy, c->dt);
     BSC_LAUNCH(c);
     c->have_csr = true;
@@ -981,7 +981,7 @@ int run_fgmres_ir(Ctx* c, int64_t n, bsc_solve_info* si) {
     const int m = c->ir_m;
     const FgLayout F{m};
     const EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
-    const EllOp<float> Af{c->avalf, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+    const EllPackF Af{c->ellf, c->cnt, c->K.kmax};
     double* x = c->S.p;
     double* w = c->tv;
     const int budget = std::max(50, std::min(1000, P.maxit / std::max(1, P.max_outer)));
@@ -1004,7 +1004,7 @@ int run_fgmres_ir(Ctx* c, int64_t n, bsc_solve_info* si) {
             Work<float> wk{c->xf, c->rf, c->sf, c->rhf, c->pf, c->vf, c->tf, c->bf, nullptr};
             int it = 0;
             double rri = 0.0;
-            rc = run_bicgstab<EllOp<float>, float>(c, n, Af, wk, P.inner_tol, 0, std::min(budget, P.maxit - inner),
+            rc = run_bicgstab<EllPackF, float>(c, n, Af, wk, P.inner_tol, 0, std::min(budget, P.maxit - inner),
                                                    &it, &rri, zj);
             if (rc && rc != BSC_E_BREAKDOWN) return rc;
             inner += it;
@@ -1222,7 +1222,7 @@ __global__ void k_fgf_next(int64_t n, const float* __restrict__ w, float* __rest
     GRID_LOOP(i, n) vn[i] = w[i] * inv;
 }
 
-__global__ void __launch_bounds__(RED_BLOCK) k_spmv_f(int64_t n, EllOp<float> A, const float* __restrict__ z,
+__global__ void __launch_bounds__(RED_BLOCK) k_spmv_f(int64_t n, EllPackF A, const float* __restrict__ z,
                                                        float* __restrict__ w, const Scalars* __restrict__ sc) {
     if (fg_skip(sc)) return;
     GRID_LOOP(i, n) w[i] = A.template row<float, float>(i, z);
@@ -1289,7 +1289,7 @@ int run_fgmres_ir_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
     const int m = mg.m;
     const FgLayout F{m};
     const EllOp<double> A{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
-    const EllOp<float> Af{c->avalf, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+    const EllPackF Af{c->ellf, c->cnt, c->K.kmax};
     double* x = c->S.p;
     float *V = mg.Vf, *Z = mg.Zf, *w = mg.wf, *rf = mg.rf;
     // each inner solve asks for the reduction still needed (with a margin),
