@@ -52,6 +52,9 @@ COMMON_SIGNATURES = {
     "comp_vel": [_VP],
     "comp_pos": [_VP],
     "opt2_shift": [_VP],
+    "scalart": [_VP],
+    "scalarupdate": [_VP, ctypes.c_double],
+    "densityupdate": [_VP],
     "timestep": [_VP, _PD],
     "step": [_VP, ctypes.c_int32, ctypes.POINTER(SolveInfo)],
     "get_neighbors": [_VP, _P64, _P32],
@@ -184,6 +187,9 @@ class Context:
     def comp_vel(self): self._call("comp_vel")
     def comp_pos(self): self._call("comp_pos")
     def opt2_shift(self): self._call("opt2_shift")
+    def scalart(self): self._call("scalart")
+    def scalarupdate(self, stime: float): self._call("scalarupdate", float(stime))
+    def densityupdate(self): self._call("densityupdate")
 
     def ppesolve(self, check: bool = True) -> SolveInfo:
         info = SolveInfo()

@@ -121,7 +121,7 @@ static void free_all(Ctx* c) {
 static int alloc_state(Ctx* c, State& S, int64_t n) {
     double** f[N_DBL_FIELDS] = {&S.x, &S.y, &S.vx, &S.vy, &S.xs, &S.ys, &S.vxs, &S.vys, &S.p, &S.rho, &S.oden,
                                 &S.mass, &S.por, &S.gradvx, &S.nut, &S.tke, &S.resist, &S.varts, &S.vel, &S.xrest,
-                                &S.vol, &S.L0, &S.L1, &S.L2, &S.L3};
+                                &S.vol, &S.L0, &S.L1, &S.L2, &S.L3, &S.con, &S.ovol, &S.cdiff};
     for (int k = 0; k < N_DBL_FIELDS; ++k)
         if (int rc = dalloc(c, f[k], n)) return rc;
     if (int rc = dalloc(c, &S.tid, n)) return rc;
@@ -170,6 +170,7 @@ static int alloc_for(Ctx* c, int64_t n) {
     // FP64 grad W and PPE values in both precisions; the mixed path adds FP32
     // copies for its FP32 pair sums and inner Krylov sweeps
     if ((rc = dalloc(c, &c->gw, slots)) || (rc = dalloc(c, &c->aval, slots))) return rc;
+    if (c->P.salinity && (rc = dalloc(c, &c->ndist, slots))) return rc;
     if (c->mixed) {
         float* tw = nullptr;
         if ((rc = dalloc(c, &tw, 6 * n))) return rc;
@@ -238,10 +239,12 @@ static int setup_grid(Ctx* c, const double* hx, const double* hy, int64_t n) {
     return BSC_OK;
 }
 
-__global__ void k_derive_after_upload(int64_t n, State S) {
+__global__ void k_derive_after_upload(int64_t n, State S, int ovol_given) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     S.vol[i] = S.mass[i] / S.rho[i];
+    if (!ovol_given) S.ovol[i] = S.mass[i] / S.oden[i];  // internal.f90:103: ovol = fmass / rho
+    S.cdiff[i] = 0.0;
     S.id[i] = (int32_t)i;
 }
 
@@ -302,13 +305,16 @@ static void dt_rule(Ctx* c, double umax, double numax) {
     else
         dt = std::min(std::min(sig1 * dl / umax, sig1 * (dl * dl) / ((mu / rho) + numax)), 0.0050);
     if (!std::isfinite(numax)) numax = 0.0;
+    // salinity sub-steps cover the next step's dt: the rule's dt, or the
+    // fixed dt of the benchmark mode
+    const double dtn = P.dt_mode == BSC_DT_ADAPTIVE ? dt : c->dt;
     double dtsol = sig1 * (dl * dl) / (P.diffusivity + numax / P.tschmidt);
     int solsteps = 1;
-    if (dtsol < dt) {
-        solsteps = (int)std::ceil(dt / dtsol);
-        dtsol = dt / solsteps;
+    if (dtsol < dtn) {
+        solsteps = (int)std::ceil(dtn / dtsol);
+        dtsol = dtn / solsteps;
     }
-    c->dtsol = dtsol < dt ? dtsol : dt;
+    c->dtsol = dtsol < dtn ? dtsol : dtn;
     c->solsteps = solsteps;
     c->umax = umax;
     c->numax = numax;
@@ -372,7 +378,7 @@ int bsc_default_params(bsc_params* p, double dl) {
     p->dt = (double)0.001f;
     p->sig1 = 0.2;
     p->tschmidt = 1.0;
-    p->diffusivity = 1e-9;
+    p->diffusivity = (double)1e-9f;  // `Dm=1e-9`, a default-real literal (integrator.f90:915, scalar.f90:118)
     p->restart = 150 > 64 ? 64 : 150;
     p->maxit = 150;
     p->tol_mode = BSC_TOL_REL_R0;
@@ -386,6 +392,11 @@ int bsc_default_params(bsc_params* p, double dl) {
     p->mg_scale = 1.8;
     p->mg_sweeps = 2;
     p->mg_coarse_max = MG_COARSE_MAX;
+    p->disp_long = 0.0025;     // scalar.f90:118
+    p->disp_trans = 0.00025;
+    p->buffer_con = 0.5;       // scalar.f90:260-264
+    p->buffer_con_xmax = 1.6;
+    p->salinity = 0;
     return BSC_OK;
 }
 
@@ -526,7 +537,8 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
         (rc = up(S.oden, s->oden, 0)) || (rc = up(S.mass, s->mass, 0)) || (rc = up(S.por, s->porosity, 1.0)) ||
         (rc = up(S.gradvx, s->gradvx, 0)) || (rc = up(S.nut, s->nut, 0)) || (rc = up(S.tke, s->tke, 0)) ||
         (rc = up(S.resist, s->resist, 0)) || (rc = up(S.varts, s->varts, 0)) || (rc = up(S.vel, s->vel, 0)) ||
-        (rc = up(S.xrest, s->xrest ? s->xrest : s->x, 0)))
+        (rc = up(S.xrest, s->xrest ? s->xrest : s->x, 0)) || (rc = up(S.con, s->con, 0)) ||
+        (s->ovol && (rc = up(S.ovol, s->ovol, 0))))
         return rc;
     if (s->L) {
         cudaStream_t cs = c->copy_stream[nq++ % Ctx::NCOPY];
@@ -541,7 +553,7 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
     BSC_CUDA(c, cudaMemcpyAsync(S.tid, s->tid, n, cudaMemcpyHostToDevice, c->copy_stream[nq++ % Ctx::NCOPY]));
     BSC_CUDA(c, cudaMemcpyAsync(S.flags, s->flags, n, cudaMemcpyHostToDevice, c->copy_stream[nq++ % Ctx::NCOPY]));
     if ((rc = copy_join(c))) return rc;
-    k_derive_after_upload<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, S);
+    k_derive_after_upload<<<blocks_for(n, 256), 256, 0, c->stream>>>(n, S, s->ovol != nullptr);
     BSC_LAUNCH(c);
     c->have_state = true;
     c->have_lists = c->have_csr = false;
@@ -634,7 +646,8 @@ int bsc_download_state(bsc_ctx* c, bsc_state_view* s) {
         (rc = dn(S.por, T.por, s->porosity)) || (rc = dn(S.gradvx, T.gradvx, s->gradvx)) ||
         (rc = dn(S.nut, T.nut, s->nut)) || (rc = dn(S.tke, T.tke, s->tke)) ||
         (rc = dn(S.resist, T.resist, s->resist)) || (rc = dn(S.varts, T.varts, s->varts)) ||
-        (rc = dn(S.vel, T.vel, s->vel)) || (rc = dn(S.xrest, T.xrest, s->xrest)))
+        (rc = dn(S.vel, T.vel, s->vel)) || (rc = dn(S.xrest, T.xrest, s->xrest)) || (rc = dn(S.con, T.con, s->con)) ||
+        (rc = dn(S.ovol, T.ovol, s->ovol)))
         return rc;
     if (s->L) {
         cudaStream_t cs = c->copy_stream[nq++ % Ctx::NCOPY];
@@ -738,6 +751,19 @@ int bsc_step(bsc_ctx* c, int32_t nsteps, bsc_solve_info* last) {
         StageTimer tm_(c, slot);         \
         if ((rc = (expr))) return rc;    \
     } while (0)
+        if (c->P.salinity) {
+            // phase 3 of main.f90:198-260: solsteps salinity sub-steps on the
+            // lists of the previous step (built here on the first step)
+            if (!c->have_lists) {
+                RUN(BSC_T_CELLSHIFT, cells_build(c, true));
+                RUN(BSC_T_NEIGHBOUR, op_neighbour(c));
+            }
+            if (!(c->dtsol > 0.0)) RUN(BSC_T_TIMESTEP, timestep_host(c));
+            for (int k = 0; k < c->solsteps; ++k) {
+                RUN(BSC_T_SCALAR, op_scalart(c));
+                RUN(BSC_T_SCALAR, op_scalarupdate(c, c->dtsol));
+            }
+        }
         RUN(BSC_T_PISTON, op_piston(c));
         RUN(BSC_T_PROJECTION, op_projection(c));
         RUN(BSC_T_CELLSHIFT, cells_build(c, true));
@@ -765,11 +791,15 @@ int bsc_step(bsc_ctx* c, int32_t nsteps, bsc_solve_info* last) {
         RUN(BSC_T_FREESURF, op_freesurf(c));
         RUN(BSC_T_EFFPOR, op_effpor(c));
         RUN(BSC_T_SHIFT, op_opt2_shift(c));
-        if (c->P.dt_mode == BSC_DT_ADAPTIVE) {
+        if (c->P.salinity) RUN(BSC_T_SCALAR, op_densityupdate(c));
+        // the host needs umax and numax for an adaptive dt, and numax for
+        // the salinity sub-steps; otherwise the reduction stays on the device
+        if (c->P.dt_mode == BSC_DT_ADAPTIVE || c->P.salinity) {
             RUN(BSC_T_TIMESTEP, timestep_host(c));
         } else {
             RUN(BSC_T_TIMESTEP, op_timestep_reduce(c));
         }
+        if (c->P.salinity) RUN(BSC_T_EDDYVIS, op_eddyvis(c));
 #undef RUN
     }
     int rc = check_flags(c);

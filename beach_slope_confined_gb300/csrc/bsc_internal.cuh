@@ -35,11 +35,12 @@ struct State {
     double *x, *y, *vx, *vy, *xs, *ys, *vxs, *vys, *p, *rho, *oden, *mass;
     double *por, *gradvx, *nut, *tke, *resist, *varts, *vel, *xrest, *vol;
     double *L0, *L1, *L2, *L3;
+    double *con, *ovol, *cdiff;  // salinity, original volume, salinity rate
     int8_t* tid;
     uint8_t* flags;
     int32_t* id;
 };
-constexpr int N_DBL_FIELDS = 25;
+constexpr int N_DBL_FIELDS = 28;
 
 // ---- neighbour list (ELL, 32-slot slices) ----------------------------------
 __host__ __device__ inline int64_t ell(int64_t i, int k, int kmax) {
@@ -255,6 +256,7 @@ struct Ctx {
     // neighbour lists
     int32_t* nbr = nullptr;
     double2* gw = nullptr;        // FP64 grad W
+    double* ndist = nullptr;      // pair distance per slot (salinity: scalart's radial)
     float2* gwf = nullptr;        // FP32 grad W (mixed)
     int32_t* cnt = nullptr;
     int32_t* d_flag = nullptr;    // device error flags (capacity, nonfinite)
@@ -371,6 +373,9 @@ int op_eddyvis(Ctx* c);
 int op_int_vel(Ctx* c, const double* d_umax);
 int op_comp_vel(Ctx* c);
 int op_opt2_shift(Ctx* c);
+int op_scalart(Ctx* c);
+int op_scalarupdate(Ctx* c, double stime);
+int op_densityupdate(Ctx* c);
 int op_timestep_reduce(Ctx* c);
 int op_probe_eta(Ctx* c, int np, const double* xp, double depth, double* eta);
 // ppe.cu

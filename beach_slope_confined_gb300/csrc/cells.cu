@@ -171,7 +171,7 @@ FieldPtrs fields_of(State& s) {
     FieldPtrs f;
     double* a[N_DBL_FIELDS] = {s.x, s.y, s.vx, s.vy, s.xs, s.ys, s.vxs, s.vys, s.p, s.rho, s.oden, s.mass, s.por,
                                s.gradvx, s.nut, s.tke, s.resist, s.varts, s.vel, s.xrest, s.vol, s.L0, s.L1, s.L2,
-                               s.L3};
+                               s.L3, s.con, s.ovol, s.cdiff};
     for (int k = 0; k < N_DBL_FIELDS; ++k) f.d[k] = a[k];
     return f;
 }

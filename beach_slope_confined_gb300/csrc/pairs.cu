@@ -15,43 +15,9 @@
 #include <cmath>
 
 #include "bsc_internal.cuh"
+#include "sph_kernel.cuh"
 
 namespace bsc {
-
-// ---- smoothing kernel --------------------------------------------------------
-// grad_i W = F(r) (x_i - x_j).  Hybrid (kernel.f90:94-162):
-//   r <  h: F = A (9r/h^3 - 12/h^2) + B (3r/h^3 - 6/(r h))
-//   r >= h: F = -(A + B) (3/(r h)) (2 - r/h)^2
-// with A = 0.1*10/(28*3.14 h^2), B = 0.9/(3*3.14 h^2) (3.14 is the
-// reference's single-precision literal).  Wendland C2 (kernel.f90:102-103):
-//   F = -35/(4*3.14 h^4) (1 - r/(2h))^3.
-template <typename R>
-__device__ __forceinline__ R grad_factor(const KParams& K, R r) {
-    const R q = r * (R)K.inv_h;
-    if (K.kernel == BSC_KERNEL_WENDLAND_C2) {
-        R a = (R)1 - (R)0.5 * q;
-        return -(R)K.wend_F * (a * a * a);
-    }
-    // A (9r/h^3 - 12/h^2) + B (3r/h^3 - 6/(rh)) = (9A+3B) r/h^3 - 12A/h^2 - 6B/(rh)
-    const R inv_rh = (R)K.inv_h / r;
-    if (q < (R)1) return (R)K.hyb_n1 * r - (R)K.hyb_n0 - (R)K.hyb_n2 * inv_rh;
-    R a = (R)2 - q;
-    return -(R)K.hyb_f * inv_rh * (a * a);
-}
-
-// W(r) (kernel.f90:34-66 and the Wendland comment at :42-43)
-template <typename R>
-__device__ __forceinline__ R kern_w(const KParams& K, R r) {
-    const R q = r * (R)K.inv_h;
-    if (K.kernel == BSC_KERNEL_WENDLAND_C2) {
-        R a = (R)1 - (R)0.5 * q, a2 = a * a;
-        return (R)K.wend_W * ((R)1 + (R)2 * q) * (a2 * a2);
-    }
-    const R A = (R)K.hyb_A, B = (R)K.hyb_B;
-    if (q < (R)1) return A * ((R)4 - (R)6 * q * q + (R)3 * q * q * q) + B * (q * q * q - (R)6 * q + (R)6);
-    R a = (R)2 - q;
-    return (A + B) * (a * a * a);
-}
 
 // vis(oden) of porous.f90:12-30 / integrator.f90:12-30
 __device__ __forceinline__ double vis_of(double oden) {
@@ -101,7 +67,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                                                          const float2* __restrict__ posf,
                                                          int32_t* __restrict__ nbr, double2* __restrict__ gw,
                                                          float2* __restrict__ gwf, const float* __restrict__ f_vol,
-                                                         int32_t* __restrict__ cnt, int32_t* __restrict__ flag) {
+                                                         double* __restrict__ ndist, int32_t* __restrict__ cnt,
+                                                         int32_t* __restrict__ flag) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double xi = S.x[i], yi = S.y[i];
@@ -132,6 +99,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
             nbr[e] = j;
             gw[e] = {gx64, gy64};
             if (gwf) gwf[e] = {(float)gx, (float)gy};
+            if (ndist) ndist[e] = r;
         }
         ++count;
         const R vj = F32 ? (R)f_vol[j] : (R)S.vol[j];
@@ -227,12 +195,12 @@ int op_neighbour(Ctx* c) {
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
         k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
-                                                          c->pcell, c->posf, c->nbr, c->gw, c->gwf, c->f_vol, c->cnt,
-                                                          c->d_flag);
+                                                          c->pcell, c->posf, c->nbr, c->gw, c->gwf, c->f_vol, c->ndist,
+                                                          c->cnt, c->d_flag);
     else
         k_neighbour<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count,
                                                            c->sorted, c->pcell, c->posf, c->nbr, c->gw, nullptr,
-                                                           nullptr, c->cnt, c->d_flag);
+                                                           nullptr, c->ndist, c->cnt, c->d_flag);
     BSC_LAUNCH(c);
     c->have_lists = true;
     return BSC_OK;

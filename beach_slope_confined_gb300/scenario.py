@@ -80,6 +80,8 @@ class TankSpec:
     csh: float = 0.2
     dt: float = 1e-4
     probes: tuple = (1.0, 1.5, 2.0, 2.5)
+    salinity_front: float = 3.0  # initial salinity 0.5 tanh((x - front) / width)
+    salinity_width: float = 0.1
 
 
 def irregular_piston(total_amp: float = 0.03, modes: int = 8, tmin: float = 0.8,
@@ -338,6 +340,8 @@ class Params(ctypes.Structure):
         ("precond", _I), ("piston_amp", _D * 8), ("piston_period", _D * 8),
         ("piston_phase", _D * 8), ("piston_ramp", _D), ("xmin", _D), ("xmax", _D), ("ymin", _D),
         ("ymax", _D), ("mg_omega", _D), ("mg_scale", _D), ("mg_sweeps", _I), ("mg_coarse_max", _I),
+        ("disp_long", _D), ("disp_trans", _D), ("buffer_con", _D), ("buffer_con_xmax", _D),
+        ("salinity", _I),
     ]
 
 
@@ -346,7 +350,8 @@ class StateView(ctypes.Structure):
         (f, _PD) for f in ("x", "y", "vx", "vy", "xs", "ys", "vxs", "vys", "p",
                            "rho", "oden", "mass", "porosity", "gradvx", "nut",
                            "tke", "resist", "varts", "vel", "L", "xrest")
-    ] + [("tid", ctypes.POINTER(ctypes.c_int8)), ("flags", ctypes.POINTER(ctypes.c_uint8))]
+    ] + [("tid", ctypes.POINTER(ctypes.c_int8)), ("flags", ctypes.POINTER(ctypes.c_uint8)),
+         ("con", _PD), ("ovol", _PD)]
 
 
 class SolveInfo(ctypes.Structure):
@@ -355,7 +360,7 @@ class SolveInfo(ctypes.Structure):
 
 
 class Timing(ctypes.Structure):
-    _fields_ = [("ms", _D * 24), ("calls", ctypes.c_int64 * 24),
+    _fields_ = [("ms", _D * 32), ("calls", ctypes.c_int64 * 32),
                 ("kernel_launches", ctypes.c_int64)]
 
 
@@ -397,7 +402,7 @@ def wcsph_params(spec: "TankSpec", scen: "Scenario", alpha: float = None, beta: 
 
 STATE_FIELDS = ("x", "y", "vx", "vy", "xs", "ys", "vxs", "vys", "p", "rho", "oden",
                 "mass", "porosity", "gradvx", "nut", "tke", "resist", "varts", "vel",
-                "xrest")
+                "xrest", "con", "ovol")
 
 SOLVERS = {"bicgstab": 0, "fgmres": 1}
 PRECONDS = {"none": 0, "mg": 1}
@@ -408,7 +413,7 @@ def make_params(spec: TankSpec, bounds=None, *, precision="fp64", solver="bicgst
                 tol=1e-8, maxit=2000, restart=30, max_neighbors=48,
                 reorder_every=20, tol_mode=0, dt_mode=0, inner_tol=1e-4,
                 max_outer=20, precond="none", mg_omega=0.82, mg_scale=1.8, mg_sweeps=2,
-                mg_coarse_max=128) -> Params:
+                mg_coarse_max=128, salinity=False) -> Params:
     """bsc_params for a tank case (constants of initialize.f90:19-56 where the
     benchmark does not override them)."""
     p = Params()
@@ -438,7 +443,7 @@ def make_params(spec: TankSpec, bounds=None, *, precision="fp64", solver="bicgst
     p.dt = spec.dt
     p.sig1 = 0.2
     p.tschmidt = 1.0
-    p.diffusivity = 1e-9
+    p.diffusivity = float(np.float32(1e-9))  # the reference's `Dm=1e-9` is a default-real literal
     p.restart = restart
     p.maxit = maxit
     p.tol_mode = tol_mode
@@ -454,6 +459,9 @@ def make_params(spec: TankSpec, bounds=None, *, precision="fp64", solver="bicgst
     p.precond = PRECONDS[precond]
     p.mg_omega, p.mg_scale = mg_omega, mg_scale
     p.mg_sweeps, p.mg_coarse_max = mg_sweeps, mg_coarse_max
+    p.disp_long, p.disp_trans = 0.0025, 0.00025  # scalar.f90:118
+    p.buffer_con, p.buffer_con_xmax = 0.5, 1.6
+    p.salinity = 1 if salinity else 0
     if bounds is not None:
         p.xmin, p.xmax, p.ymin, p.ymax = bounds
     return p
@@ -486,6 +494,13 @@ def state_arrays(scen: Scenario) -> Dict[str, np.ndarray]:
         d[f] = np.zeros(n)
     d["porosity"] = np.ones(n)
     d["L"] = np.tile(np.array([1.0, 0.0, 0.0, 1.0]), n)
+    # A saline wedge on the beach side (fluid only), in the reference's
+    # convention: con runs from -0.5 (fresh, oden = rho0) to 0.5 (sea water,
+    # oden = rho0 rel_den) through densityupdate (scalar.f90:293). ovol is
+    # derived on upload as mass / oden.
+    sp = scen.spec
+    d["con"] = np.where(scen.tid == TID_FLUID,
+                        0.5 * np.tanh((scen.x - sp.salinity_front) / sp.salinity_width), 0.0)
     return d
 
 

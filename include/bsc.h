@@ -125,6 +125,12 @@ typedef struct bsc_params {
     double  mg_scale;            /* scaling of the coarse-grid correction          */
     int32_t mg_sweeps;           /* pre- and post-smoothing sweeps per level       */
     int32_t mg_coarse_max;       /* cells of the coarsest level (dense solve)      */
+    /* salinity transport (scalar.f90:114-305) */
+    double  disp_long, disp_trans;   /* dispersivities al, at (scalar.f90:118)     */
+    double  buffer_con;          /* concentration held on inflow buffers ...       */
+    double  buffer_con_xmax;     /* ... left of this x (scalar.f90:260-264)        */
+    int32_t salinity;            /* 1: bsc_step runs the phase-3 step of           *
+                                  * main.f90:198-260 with salinity sub-steps       */
 } bsc_params;
 
 /* Host-side particle state, structure of arrays, n entries each, id order.
@@ -142,6 +148,9 @@ typedef struct bsc_state_view {
     double  *xrest;              /* piston particles: x at zero stroke           */
     int8_t  *tid;
     uint8_t *flags;
+    double  *con;                /* salinity concentration (plist%con)            */
+    double  *ovol;               /* original volume (plist%ovol); NULL on upload: *
+                                  * mass / oden                                   */
 } bsc_state_view;
 
 typedef struct bsc_solve_info {
@@ -154,7 +163,7 @@ typedef struct bsc_solve_info {
     double  b_norm;              /* ||b||                                       */
 } bsc_solve_info;
 
-#define BSC_TIMING_SLOTS 24
+#define BSC_TIMING_SLOTS 32
 typedef struct bsc_timing {
     /* cumulative device milliseconds per stage since the last reset, measured
      * with CUDA events on the context stream */
@@ -175,7 +184,9 @@ enum {
      * the phases of every FGMRES iteration instead: fine-level pre-smoothing
      * and restriction, coarse levels, fine-level post-smoothing, the SpMV,
      * and the orthogonalisation */
-    BSC_T_BICG_1, BSC_T_BICG_2, BSC_T_BICG_3, BSC_T_BICG_4, BSC_T_BICG_5
+    BSC_T_BICG_1, BSC_T_BICG_2, BSC_T_BICG_3, BSC_T_BICG_4, BSC_T_BICG_5,
+    /* salinity transport: scalart, scalarupdate and densityupdate */
+    BSC_T_SCALAR
 };
 
 typedef struct bsc_ctx bsc_ctx;
@@ -223,7 +234,16 @@ int bsc_timestep(bsc_ctx* ctx, double* dt_inout); /* integrator.f90:908-976  */
 /* Move the piston wall particles to x_p(t) at the context time (greenfield:
  * the reference has no wavemaker). */
 int bsc_piston(bsc_ctx* ctx);
-/* The whole main.f90:41-65 sequence, nsteps times (t += dt first). */
+/* Salinity transport (scalar.f90; needs params.salinity = 1, which makes the
+ * neighbour search keep each pair's distance for scalart). */
+int bsc_scalart(bsc_ctx* ctx);                    /* scalar.f90:114-240      */
+int bsc_scalarupdate(bsc_ctx* ctx, double stime); /* scalar.f90:242-275      */
+int bsc_densityupdate(bsc_ctx* ctx);              /* scalar.f90:277-305      */
+/* The whole main.f90:41-65 sequence, nsteps times (t += dt first).  With
+ * params.salinity = 1, the phase-3 sequence of main.f90:198-260 instead:
+ * solsteps x (scalart, scalarupdate(dtsol)) first, densityupdate after
+ * opt2_shift, eddyvis after timestep (the open-boundary buffers of that
+ * loop are not part of this library). */
 int bsc_step(bsc_ctx* ctx, int32_t nsteps, bsc_solve_info* last);
 
 /* ---- parity and diagnostics hooks --------------------------------------- */

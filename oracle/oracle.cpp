@@ -79,6 +79,7 @@ struct Orc {
     int64_t n = 0;
     // particle records (plist, particle.f90:31-47)
     std::vector<double> x, y, vx, vy, xs, ys, vxs, vys, p, rho, oden, mass, xrest;
+    std::vector<double> con, ovol, cdiff;  // salinity (plist%con, %ovol; pplist%cdiff)
     std::vector<int8_t> tid;
     std::vector<uint8_t> flags;
     std::vector<int64_t> matid;
@@ -537,6 +538,10 @@ int orc_upload_state(orc_ctx* o, const bsc_state_view* s) {
     cp(o->tke, s->tke, 0); cp(o->resist, s->resist, 0); cp(o->varts, s->varts, 0);
     cp(o->vel, s->vel, 0);
     cp(o->xrest, s->xrest ? s->xrest : s->x, 0);
+    cp(o->con, s->con, 0);
+    o->ovol.assign(n, 0.0);
+    for (int64_t k = 0; k < n; ++k) o->ovol[k] = s->ovol ? s->ovol[k] : o->mass[k] / o->oden[k];  // internal.f90:103
+    o->cdiff.assign(n, 0.0);
     o->coff.assign(4 * n, 0.0);
     if (s->L) std::memcpy(o->coff.data(), s->L, sizeof(double) * 4 * n);
     else for (int64_t k = 0; k < n; ++k) { o->coff[4 * k] = 1.0; o->coff[4 * k + 3] = 1.0; }
@@ -595,6 +600,7 @@ int orc_download_state(orc_ctx* o, bsc_state_view* s) {
     cp(s->p, o->p); cp(s->rho, o->rho); cp(s->oden, o->oden); cp(s->mass, o->mass);
     cp(s->porosity, o->por); cp(s->gradvx, o->gradvx); cp(s->nut, o->nut); cp(s->tke, o->tke);
     cp(s->resist, o->resist); cp(s->varts, o->varts); cp(s->vel, o->vel); cp(s->xrest, o->xrest);
+    cp(s->con, o->con); cp(s->ovol, o->ovol);
     if (s->L) std::memcpy(s->L, o->coff.data(), sizeof(double) * 4 * n);
     if (s->tid) std::memcpy(s->tid, o->tid.data(), n);
     if (s->flags) std::memcpy(s->flags, o->flags.data(), n);
@@ -1131,13 +1137,16 @@ int orc_timestep(orc_ctx* o, double* dt_inout) {
     else
         dt = std::min(std::min(sig1 * (dl) / umax, sig1 * ((dl) * (dl)) / ((mu / rho) + numax)), 0.0050);
     if (!std::isfinite(numax)) numax = 0.0;
+    // integrator.f90:964-972; the sub-steps cover the next step's dt (the
+    // rule's, or the fixed dt of the benchmark mode)
+    const double dtn = o->P.dt_mode == BSC_DT_ADAPTIVE ? dt : o->dt;
     double dtsol = sig1 * (dl * dl) / (o->P.diffusivity + numax / o->P.tschmidt);
     int solsteps = 1;
-    if (dtsol < dt) {
-        solsteps = (int)std::ceil(dt / dtsol);
-        dtsol = dt / solsteps;
+    if (dtsol < dtn) {
+        solsteps = (int)std::ceil(dtn / dtsol);
+        dtsol = dtn / solsteps;
     }
-    dtsol = (dtsol < dt) ? dtsol : dt;
+    dtsol = (dtsol < dtn) ? dtsol : dtn;
     o->dtsol = dtsol;
     o->solsteps = solsteps;
     if (o->P.dt_mode == BSC_DT_ADAPTIVE) o->dt = dt;
@@ -1153,11 +1162,106 @@ int orc_get_dt_rule(orc_ctx* o, double* umax, double* numax, double* dtsol, int3
     return BSC_OK;
 }
 
-// main.f90:41-65
+// scalar.f90:114-240 scalart: the dispersion flux of every fluid particle.
+// The kernel gradient takes the distance stored by the neighbour search and
+// the current positions, as hWabx(x, plist(k), dist(m), h1) does.
+int orc_scalart(orc_ctx* o) {
+    if (!o->have_lists) return fail(o, BSC_E_INVALID, "scalart before neighbour");
+    const double al = o->P.disp_long, at = o->P.disp_trans, Dm = o->P.diffusivity, tor = 1.0;
+    const double tsc = o->P.tschmidt, h = o->P.h, lam = o->P.lam;
+    const double cap = 0.12 * (o->P.dl * o->P.dl) / o->dt;
+    const double nut_min = (double)1e-6f;  // `nut < 1e-6`, a default-real literal
+    auto live = [o](int64_t k) { return o->tid[k] == BSC_TID_FLUID && !has(o->flags[k], BSC_FLAG_DEAD); };
+    auto clampD = [Dm, cap](double D) {
+        D = (D > 0.0) ? D : Dm;      // merge(D, Dm, D > 0): a NaN gives Dm
+        return (D <= cap) ? D : cap;  // merge(D, cap, D <= cap)
+    };
+#pragma omp parallel for schedule(dynamic, 256)
+    for (int64_t i = 0; i < o->n; ++i) {
+        if (!live(i)) continue;
+        o->cdiff[i] = 0.0;
+        const double con1 = o->con[i];
+        const double vi = std::sqrt(o->vx[i] * o->vx[i] + o->vy[i] * o->vy[i]);
+        const double ni = o->por[i];
+        const double Dxi = clampD(Dm + ((al * (o->vx[i] * o->vx[i])) + (at * (o->vy[i] * o->vy[i])) +
+                                        ((al - at) * o->vx[i] * o->vy[i])) / (vi * ni));
+        const double Dyi = clampD(Dm + ((at * (o->vx[i] * o->vx[i])) + (al * (o->vy[i] * o->vy[i])) +
+                                        ((al - at) * o->vx[i] * o->vy[i])) / (vi * ni));
+        double cd = 0.0;
+        for (int64_t e = o->nb_off[i]; e < o->nb_off[i + 1]; ++e) {
+            const int64_t j = o->nb_id[e];
+            if (!live(j)) continue;
+            const double con2 = o->con[j];
+            const double vj = std::sqrt(o->vx[j] * o->vx[j] + o->vy[j] * o->vy[j]);
+            const double nj = o->por[j];
+            const double Dxj = clampD(Dm + ((al * (o->vx[j] * o->vx[j])) + (at * (o->vy[j] * o->vy[j])) +
+                                            ((al - at) * o->vx[j] * o->vy[j])) / (vj * nj));
+            const double Dyj = clampD(Dm + ((at * (o->vx[j] * o->vx[j])) + (al * (o->vy[j] * o->vy[j])) +
+                                            ((al - at) * o->vx[j] * o->vy[j])) / (vj * nj));
+            double t1x, t1y;
+            if ((ni >= 0.8) || (nj >= 0.8)) {
+                if ((o->nut[i] < nut_min) && (o->nut[j] < nut_min)) {
+                    t1x = Dm + (o->nut[i] + o->nut[j]) * 0.50 / tsc;
+                } else {
+                    t1x = 2 * (((Dm + o->nut[i] / tsc) * (Dm + o->nut[j] / tsc)) /
+                               ((Dm + o->nut[i] / tsc) + (Dm + o->nut[j] / tsc)));
+                }
+                t1y = t1x;
+            } else {
+                t1x = 2.0 * tor * Dxi * Dxj / (Dxi + Dxj);
+                t1y = 2.0 * tor * Dyi * Dyj / (Dyi + Dyj);
+            }
+            const double t3 = (o->ovol[i]) * (ni + nj) / (ni * nj);
+            const double r = o->nb_dist[e];
+            const double gx = Wab_grad(o, o->x[i] - o->x[j], r, h), gy = Wab_grad(o, o->y[i] - o->y[j], r, h);
+            cd = cd + (t1x * t3 * (con1 - con2) * (o->x[i] - o->x[j]) * gx / (r * r + lam)) +
+                 (t1y * t3 * (con1 - con2) * (o->y[i] - o->y[j]) * gy / (r * r + lam));
+        }
+        o->cdiff[i] = cd;
+    }
+    return BSC_OK;
+}
+
+// scalar.f90:242-275
+int orc_scalarupdate(orc_ctx* o, double stime) {
+    for (int64_t i = 0; i < o->n; ++i) {
+        if (o->tid[i] != BSC_TID_FLUID || has(o->flags[i], BSC_FLAG_DEAD)) continue;
+        o->con[i] = o->con[i] + o->cdiff[i] * stime;
+        if (has(o->flags[i], BSC_FLAG_BUFFER) && o->x[i] < o->P.buffer_con_xmax) o->con[i] = o->P.buffer_con;
+    }
+    return BSC_OK;
+}
+
+// scalar.f90:277-305, with rhomin = rho (initialize.f90:22) and
+// rhomax = rho rel_den (setup.f90:19)
+int orc_densityupdate(orc_ctx* o) {
+    const double rhomin = o->P.rho0, rhomax = o->P.rho0 * o->P.rel_den;
+    for (int64_t i = 0; i < o->n; ++i) {
+        if (o->tid[i] != BSC_TID_FLUID || has(o->flags[i], BSC_FLAG_DEAD)) continue;
+        o->oden[i] = 0.5 * (rhomax + rhomin) + o->con[i] * (rhomax - rhomin);
+        o->mass[i] = o->oden[i] * o->ovol[i];
+        o->rho[i] = o->oden[i] * o->por[i];
+    }
+    return BSC_OK;
+}
+
+// main.f90:41-65; with salinity, the phase-3 loop of main.f90:198-260
+// (without its open-boundary buffers)
 int orc_step(orc_ctx* o, int32_t nsteps, bsc_solve_info* last) {
     for (int s = 0; s < nsteps; ++s) {
         o->t = o->t + o->dt;
         int st;
+        if (o->P.salinity) {
+            if (!o->have_lists) {
+                orc_cellshift(o, 0);
+                orc_neighbour(o);
+            }
+            if (!(o->dtsol > 0.0)) orc_timestep(o, nullptr);
+            for (int k = 0; k < o->solsteps; ++k) {  // main.f90:210-215
+                orc_scalart(o);
+                orc_scalarupdate(o, o->dtsol);
+            }
+        }
         orc_piston(o);
         orc_projection(o);
         orc_cellshift(o, 0);
@@ -1175,7 +1279,9 @@ int orc_step(orc_ctx* o, int32_t nsteps, bsc_solve_info* last) {
         orc_freesurf(o);
         orc_effpor(o);
         orc_opt2_shift(o);
+        if (o->P.salinity) orc_densityupdate(o);
         orc_timestep(o, nullptr);
+        if (o->P.salinity) orc_eddyvis(o);
     }
     return BSC_OK;
 }
