@@ -170,7 +170,7 @@ static int alloc_for(Ctx* c, int64_t n) {
     // FP64 grad W and PPE values in both precisions; the mixed path adds FP32
     // copies for its FP32 pair sums and inner Krylov sweeps
     if ((rc = dalloc(c, &c->gw, slots)) || (rc = dalloc(c, &c->aval, slots))) return rc;
-    if (c->P.salinity && (rc = dalloc(c, &c->ndist, slots))) return rc;
+    if (c->P.salinity && ((rc = dalloc(c, &c->ndist, slots)) || (rc = dalloc(c, &c->sdisp, 4 * n)))) return rc;
     if (c->mixed) {
         float* tw = nullptr;
         if ((rc = dalloc(c, &tw, 6 * n))) return rc;

@@ -257,6 +257,7 @@ struct Ctx {
     int32_t* nbr = nullptr;
     double2* gw = nullptr;        // FP64 grad W
     double* ndist = nullptr;      // pair distance per slot (salinity: scalart's radial)
+    double* sdisp = nullptr;      // salinity: D_x, D_y, Dm + nu_t/Sc, 1/n per particle (4n)
     float2* gwf = nullptr;        // FP32 grad W (mixed)
     int32_t* cnt = nullptr;
     int32_t* d_flag = nullptr;    // device error flags (capacity, nonfinite)

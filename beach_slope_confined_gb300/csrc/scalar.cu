@@ -9,8 +9,8 @@
 //   for fluid neighbours j: the harmonic mean of D_i and D_j per axis, or,
 //   where either porosity is >= 0.8, the Schmidt-scaled eddy diffusivity
 //   (arithmetic mean when both nu_t < 1e-6, harmonic otherwise);
-//   cdiff_i = sum_j t1 ovol_i (n_i + n_j) / (n_i n_j) (c_i - c_j)
-//             [(x_i - x_j) dW/dx + (y_i - y_j) dW/dy] / (r^2 + lam)
+//   cdiff_i = sum_j ovol_i (n_i + n_j) / (n_i n_j) (c_i - c_j)
+//             [t1x (x_i - x_j) dW/dx + t1y (y_i - y_j) dW/dy] / (r^2 + lam)
 // with the kernel gradient evaluated, as hWabx/hWaby do, at the distance
 // stored by the neighbour search and the current positions (the particles
 // have moved by opt2_shift since the search).  The neighbour search keeps
@@ -42,16 +42,30 @@ __device__ __forceinline__ double disp(double Dm, double a1, double a2, double a
     return D;
 }
 
+// per particle: D_x, D_y and the eddy term Dm + nu_t / Sc, the same values
+// scalart forms for a particle as i and as j (one division and root each,
+// instead of per pair)
+__global__ void k_scalar_pre(int64_t n, State S, ScalarK C, double* __restrict__ Dx, double* __restrict__ Dy,
+                             double* __restrict__ E, double* __restrict__ inv_n) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double vx = S.vx[i], vy = S.vy[i], v = sqrt(vx * vx + vy * vy), ni = S.por[i];
+    const double amx = C.al - C.at;
+    Dx[i] = disp(C.Dm, C.al, C.at, amx, vx, vy, v, ni, C.cap);
+    Dy[i] = disp(C.Dm, C.at, C.al, amx, vx, vy, v, ni, C.cap);
+    E[i] = C.Dm + S.nut[i] / C.tsc;
+    inv_n[i] = 1.0 / ni;
+}
+
 __global__ void k_scalart(int64_t n, State S, KParams K, ScalarK C, const int32_t* __restrict__ nbr,
-                          const double* __restrict__ ndist, const int32_t* __restrict__ cnt) {
+                          const double* __restrict__ ndist, const int32_t* __restrict__ cnt,
+                          const double* __restrict__ Dx, const double* __restrict__ Dy,
+                          const double* __restrict__ E, const double* __restrict__ inv_n) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (S.tid[i] != BSC_TID_FLUID || (S.flags[i] & BSC_FLAG_DEAD)) return;
     const double con1 = S.con[i], ni = S.por[i], nuti = S.nut[i], oi = S.ovol[i];
-    const double vxi = S.vx[i], vyi = S.vy[i], vi = sqrt(vxi * vxi + vyi * vyi);
-    const double amx = C.al - C.at;
-    const double Dxi = disp(C.Dm, C.al, C.at, amx, vxi, vyi, vi, ni, C.cap);
-    const double Dyi = disp(C.Dm, C.at, C.al, amx, vxi, vyi, vi, ni, C.cap);
+    const double Dxi = Dx[i], Dyi = Dy[i], Ei = E[i], ini = inv_n[i];
     const double xi = S.x[i], yi = S.y[i];
     double cd = 0.0;
     const int m = cnt[i];
@@ -59,28 +73,29 @@ __global__ void k_scalart(int64_t n, State S, KParams K, ScalarK C, const int32_
         const int64_t e = ell(i, k, K.kmax);
         const int j = nbr[e];
         if (S.tid[j] != BSC_TID_FLUID || (S.flags[j] & BSC_FLAG_DEAD)) continue;
-        const double con2 = S.con[j], nj = S.por[j], nutj = S.nut[j];
-        const double vxj = S.vx[j], vyj = S.vy[j], vj = sqrt(vxj * vxj + vyj * vyj);
-        const double Dxj = disp(C.Dm, C.al, C.at, amx, vxj, vyj, vj, nj, C.cap);
-        const double Dyj = disp(C.Dm, C.at, C.al, amx, vxj, vyj, vj, nj, C.cap);
+        const double con2 = S.con[j], nj = S.por[j];
         double t1x, t1y;
         if (ni >= 0.8 || nj >= 0.8) {
+            const double nutj = S.nut[j];
             if (nuti < SC_NUT_MIN && nutj < SC_NUT_MIN) {
                 t1x = C.Dm + (nuti + nutj) * 0.50 / C.tsc;
             } else {
-                const double a = C.Dm + nuti / C.tsc, b = C.Dm + nutj / C.tsc;
-                t1x = 2 * ((a * b) / (a + b));
+                const double Ej = E[j];
+                t1x = 2 * ((Ei * Ej) / (Ei + Ej));
             }
             t1y = t1x;
         } else {
+            const double Dxj = Dx[j], Dyj = Dy[j];
             t1x = 2.0 * SC_TOR * Dxi * Dxj / (Dxi + Dxj);
             t1y = 2.0 * SC_TOR * Dyi * Dyj / (Dyi + Dyj);
         }
-        const double t3 = oi * (ni + nj) / (ni * nj);
-        const double r = ndist[e], den = r * r + K.lam;
+        // t3 = ovol_i (n_i + n_j) / (n_i n_j), written with the reciprocals
+        const double t3 = oi * (ini + inv_n[j]);
+        const double r = ndist[e];
         const double dx = xi - S.x[j], dy = yi - S.y[j];
         const double F = grad_factor<double>(K, r);  // dW/dx = F (x_i - x_j) at the stored distance
-        cd = cd + (t1x * t3 * (con1 - con2) * dx * (F * dx) / den) + (t1y * t3 * (con1 - con2) * dy * (F * dy) / den);
+        const double q = t3 * (con1 - con2) * F / (r * r + K.lam);
+        cd += q * (t1x * (dx * dx) + t1y * (dy * dy));
     }
     S.cdiff[i] = cd;
 }
@@ -113,7 +128,11 @@ int op_scalart(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "scalart before neighbour");
     const bsc_params& P = c->P;
     const ScalarK C{P.diffusivity, P.disp_long, P.disp_trans, P.tschmidt, 0.12 * (P.dl * P.dl) / c->dt};
-    k_scalart<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, c->K, C, c->nbr, c->ndist, c->cnt);
+    double *Dx = c->sdisp, *Dy = c->sdisp + c->n, *E = c->sdisp + 2 * c->n, *inv_n = c->sdisp + 3 * c->n;
+    k_scalar_pre<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, C, Dx, Dy, E, inv_n);
+    BSC_LAUNCH(c);
+    k_scalart<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, c->K, C, c->nbr, c->ndist, c->cnt, Dx, Dy,
+                                                             E, inv_n);
     BSC_LAUNCH(c);
     return BSC_OK;
 }

@@ -40,7 +40,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s at 1M (mixed vs FP64, PPE res 1e-8); adjoint/forward time"
 CONFIG = "c3"
-T_STEP, T_PPE_SOLVE, T_SPMV = 15, 8, 16
+T_STEP, T_PPE_SOLVE, T_SPMV, T_SCALAR = 15, 8, 16, 24
 
 
 # --------------------------------------------------------------------------
@@ -412,6 +412,40 @@ def run_wcsph(reps: int = 2):
             "finite_differences": fd}
 
 
+def run_salinity(args):
+    """The c3 tank with salinity transport: the phase-3 step of
+    main.f90:198-260 (salinity sub-steps before the projection,
+    densityupdate after the shift, eddyvis after the time step) on the mixed
+    multigrid path. Stage events time the step and the salinity stages."""
+    from beach_slope_confined_gb300 import Solver, scenario as sc, setup_tank
+
+    spec = sc.config_spec(args.config)
+    scen = sc.build(spec)
+    P = sc.make_params(spec, scen.bounds, precision="mixed", solver=args.solver, tol=1e-8, maxit=40000,
+                       inner_tol=args.inner_tol, max_outer=60, precond=args.precond, restart=args.restart,
+                       salinity=True)
+    g = Solver(P)
+    setup_tank(g, scen)
+    for _ in range(args.warmup):
+        g.step(1)
+    g.synchronize()
+    g.reset_timings()
+    for _ in range(args.steps):
+        g.step(1)
+    g.synchronize()
+    t = g.timings()
+    s = g.download_state()
+    g.close()
+    fl = scen.tid == sc.TID_FLUID
+    step_ms = t.ms[T_STEP] / args.steps
+    return {"workload": f"{args.config} tank with the saline wedge con = 0.5 tanh((x - {spec.salinity_front}) / "
+                        f"{spec.salinity_width}), mixed multigrid path, phase-3 step",
+            "ms_per_step": step_ms, "particle_steps_per_s": scen.n_fluid / (step_ms * 1e-3),
+            "salinity_ms_per_step": t.ms[T_SCALAR] / args.steps,
+            "salinity_launches_per_step": t.calls[T_SCALAR] / args.steps,
+            "con_range": [float(s["con"][fl].min()), float(s["con"][fl].max())]}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,6 +463,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-wcsph", action="store_true", help="skip the WCSPH forward/adjoint workload (c4)")
+    ap.add_argument("--no-salinity", action="store_true", help="skip the salinity-transport step measurement")
     ap.add_argument("--cpu-iters", type=float, default=1350.0,
                     help="PPE iterations per step the reference arm's sample is scaled to")
     args = ap.parse_args()
@@ -500,6 +535,7 @@ def main():
                              "peak": hbm, "unit": "GB/s", "frac": (a64 / hbm) if a64 else None,
                              "traffic": (t64 * f["n"]) if t64 else None}}
     wc = None if args.no_wcsph else run_wcsph()
+    sal = None if args.no_salinity else run_salinity(args)
     cpu = None
     if not args.no_cpu:
         if ref_iters:
@@ -537,6 +573,7 @@ def main():
         "fp64_bound_kernels": fp64_bound_kernels(),
         "wcsph_adjoint_forward_ratio": wc["ratio"] if wc else None,
         "wcsph": wc,
+        "salinity": sal,
     }
     print(json.dumps(line), flush=True)
     dist.close()
