@@ -14,6 +14,7 @@ and the CPU restatement side by side.
 from __future__ import annotations
 
 import ctypes
+import os
 from typing import Dict, Optional, Tuple
 
 import numpy as np
@@ -67,6 +68,8 @@ OPTIONAL_SIGNATURES = {
     "get_timings": [_VP, ctypes.POINTER(Timing)],
     "reset_timings": [_VP],
     "synchronize": [_VP],
+    "snapshot_begin": [_VP, ctypes.c_char_p, ctypes.c_int64],
+    "snapshot_wait": [_VP],
     "wcsph_setup": [_VP, ctypes.POINTER(WcsphParams)],
     "wcsph_set_params": [_VP, ctypes.c_double, ctypes.c_double, _PD],
     "wcsph_forward": [_VP, ctypes.c_int32, ctypes.c_int32, _PD],
@@ -245,6 +248,18 @@ class Context:
     def synchronize(self):
         if "synchronize" in self._fn:
             self._call("synchronize")
+
+    # -- text snapshots (output.f90 `combined`) ---------------------------------
+    def snapshot(self, directory: str, index: int, wait: bool = True):
+        """Write <directory>/fluid/fluid_<index>.txt, buffer/buffer_<index>.txt
+        and fluid/dead_<index>.txt; with wait=False the files are written by a
+        host thread while later calls run (snapshot_wait joins it)."""
+        self._call("snapshot_begin", os.fsencode(directory), int(index))
+        if wait:
+            self.snapshot_wait()
+
+    def snapshot_wait(self):
+        self._call("snapshot_wait")
 
     # -- the differentiable WCSPH step (bsc_wcsph_*) ----------------------------
     def wcsph_setup(self, wp: WcsphParams):

@@ -105,6 +105,7 @@ static uint64_t spread_bits(uint32_t v) {
 static void free_all(Ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     wc_free(c);
+    snap_free(c);
     for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
     c->graphs.clear();
     for (void* p : c->allocs) cudaFree(p);

@@ -208,7 +208,8 @@ struct Mg {
     std::vector<void*> allocs;
 };
 
-struct WcState;  // the differentiable WCSPH step (wcsph.cu)
+struct WcState;    // the differentiable WCSPH step (wcsph.cu)
+struct SnapState;  // text snapshots in flight (snapshot.cu)
 
 struct Ctx {
     bsc_params P{};
@@ -308,6 +309,7 @@ struct Ctx {
     // host<->device state copies spread over several streams (several copy
     // engines at once), forked from and joined back into `stream`
     WcState* wc = nullptr;        // WCSPH forward/adjoint state, after bsc_wcsph_setup
+    SnapState* snap = nullptr;    // snapshot staging and its writer thread
     static constexpr int NCOPY = 4;
     cudaStream_t copy_stream[NCOPY] = {};
     cudaEvent_t copy_ev[NCOPY + 1] = {};
@@ -386,6 +388,7 @@ int op_ppe_solve(Ctx* c, bsc_solve_info* info);
 // z = M v to an FP64 vector (FP64 or FP32 arithmetic); release the buffers
 int mg_setup(Ctx* c);
 void wc_free(Ctx* c);
+void snap_free(Ctx* c);
 int mg_vcycle_f64(Ctx* c, const double* v, double* z);
 int mg_vcycle_f32(Ctx* c, const float* v, float* z);
 void mg_free(Ctx* c);

@@ -435,6 +435,20 @@ def run_salinity(args):
     g.synchronize()
     t = g.timings()
     s = g.download_state()
+    # an output.f90 `combined` snapshot, written by the library's host thread
+    # while the next step runs
+    import tempfile
+    with tempfile.TemporaryDirectory() as tmp:
+        g.synchronize()
+        t0 = time.perf_counter()
+        g.snapshot(tmp, 0, wait=False)
+        t1 = time.perf_counter()
+        g.step(1)
+        g.synchronize()
+        t2 = time.perf_counter()
+        g.snapshot_wait()
+        t3 = time.perf_counter()
+        snap_bytes = sum(os.path.getsize(os.path.join(dp, f)) for dp, _, fs in os.walk(tmp) for f in fs)
     g.close()
     fl = scen.tid == sc.TID_FLUID
     step_ms = t.ms[T_STEP] / args.steps
@@ -443,7 +457,9 @@ def run_salinity(args):
             "ms_per_step": step_ms, "particle_steps_per_s": scen.n_fluid / (step_ms * 1e-3),
             "salinity_ms_per_step": t.ms[T_SCALAR] / args.steps,
             "salinity_launches_per_step": t.calls[T_SCALAR] / args.steps,
-            "con_range": [float(s["con"][fl].min()), float(s["con"][fl].max())]}
+            "con_range": [float(s["con"][fl].min()), float(s["con"][fl].max())],
+            "snapshot": {"bytes": snap_bytes, "queue_ms": 1e3 * (t1 - t0), "step_after_ms": 1e3 * (t2 - t1),
+                         "written_after_ms": 1e3 * (t3 - t0)}}
 
 
 def main():

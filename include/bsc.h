@@ -246,6 +246,17 @@ int bsc_densityupdate(bsc_ctx* ctx);              /* scalar.f90:277-305      */
  * loop are not part of this library). */
 int bsc_step(bsc_ctx* ctx, int32_t nsteps, bsc_solve_info* last);
 
+/* ---- text snapshots (output.f90:188-234 `combined`) --------------------- */
+/* Queue a snapshot of the current state: <dir>/fluid/fluid_<index>.txt,
+ * <dir>/buffer/buffer_<index>.txt and <dir>/fluid/dead_<index>.txt, one line
+ * per fluid particle in id order, x y p (F10.3) vx vy (ES10.3) con+0.5
+ * (F10.5).  Returns once the device-side gather and copy are queued; a host
+ * thread formats and writes the files while later calls run.  A second call
+ * waits for the first. */
+int bsc_snapshot_begin(bsc_ctx* ctx, const char* dir, int64_t index);
+/* Wait for the queued snapshot; returns its write error, if any. */
+int bsc_snapshot_wait(bsc_ctx* ctx);
+
 /* ---- parity and diagnostics hooks --------------------------------------- */
 /* Neighbour sets of the last bsc_neighbour call: offsets[n+1], ids sorted
  * ascending per particle.  ids may be NULL to query offsets[n] first. */
