@@ -31,6 +31,7 @@ def main(argv=None):
     ap.add_argument("--precond", default="none", choices=("none", "mg"))
     ap.add_argument("--wcsph", type=int, default=0, help="WCSPH forward + adjoint steps instead of ISPH steps")
     ap.add_argument("--every", type=int, default=10, help="WCSPH checkpoint interval")
+    ap.add_argument("--salinity", action="store_true", help="the phase-3 step with salinity transport")
     args = ap.parse_args(argv)
     spec = sc.config_spec(args.config)
     scen = sc.build(spec)
@@ -50,7 +51,8 @@ def main(argv=None):
     # the inner-solve settings of bench.py for each preconditioner
     mg = args.precond == "mg"
     P = sc.make_params(spec, scen.bounds, precision=args.precision, tol=1e-8, maxit=args.maxit,
-                       inner_tol=1e-5 if mg else 0.1, max_outer=40 if mg else 4, precond=args.precond, restart=40)
+                       inner_tol=1e-5 if mg else 0.1, max_outer=40 if mg else 4, precond=args.precond, restart=40,
+                       salinity=args.salinity)
     g = Solver(P)
     setup_tank(g, scen)
     for _ in range(args.steps):
