@@ -73,16 +73,17 @@ def default_params(dl: float) -> Params:
 
 def selftest(n: int = 1 << 22):
     """bsc_selftest: (FP32 rounding mismatches, largest FP32 ulp difference,
-    largest relative error of the Newton-Raphson reciprocal) over n inputs."""
+    largest relative errors of the Newton-Raphson reciprocal and of the
+    Newton square root) over n inputs."""
     f = lib().bsc_selftest
     f.argtypes = [ctypes.c_int64, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
-                  ctypes.POINTER(ctypes.c_double)]
+                  ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
     f.restype = ctypes.c_int
-    a, b, c = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
-    rc = f(int(n), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+    a, b, c, d = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_double()
+    rc = f(int(n), ctypes.byref(a), ctypes.byref(b), ctypes.byref(c), ctypes.byref(d))
     if rc:
         raise BscError(rc, "selftest", "")
-    return a.value, b.value, c.value
+    return a.value, b.value, c.value, d.value
 
 
 def measure_peaks():

@@ -102,6 +102,20 @@ __device__ __forceinline__ double rcp_nr(double x) {
     return fma(y0, fma(-x, y0, 1.0), y0);
 }
 
+// sqrt(x) for x > 0 in FP32's normal range: an FP32 seed of 1/sqrt(x) (the
+// rounding on the integer pipe, the reciprocal root on the special-function
+// unit) and one coupled Newton step in FP64, Goldschmidt's iteration as set
+// out by Markstein (IA-64 and Elementary Functions, 2000):
+//   r0 = x y0, h0 = y0 / 2, e = 1/2 - r0 h0, r = r0 + r0 e.
+// The relative error is about 3/2 e0^2 for a seed error e0 (~2^-22): within
+// 2^-42.  Four FP64 operations.
+__device__ __forceinline__ double sqrt_nr(double x) {
+    const double y0 = f64_of(rsqrtf(f32_of(x)));
+    const double r0 = x * y0, h0 = 0.5 * y0;
+    const double e = fma(-r0, h0, 0.5);
+    return fma(r0, e, r0);
+}
+
 // an FGMRES cycle has stopped (converged, broken down or at its restart
 // length): the kernels of iterations queued past that point return at once
 __device__ __forceinline__ bool fg_skip(const Scalars* sc) { return sc->done || sc->tmp[2] != 0.0; }

@@ -85,7 +85,10 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
         const double dx = xi - S.x[j], dy = yi - S.y[j];
         const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
         if (!(d2 < K.H2x)) return;  // exactly sqrt(d2) < 2h, no FMA contraction
-        const double r = __dsqrt_rn(d2);
+        // the mixed path's root by Newton from an FP32 seed (within 2^-42;
+        // the FP64 pipe is this kernel's bound), the FP64 path's correctly
+        // rounded
+        const double r = sizeof(R) == 4 ? (d2 > 0.0 ? sqrt_nr(d2) : 0.0) : __dsqrt_rn(d2);
         // grad W per pair in FP64 (stored in FP64, and in FP32 for the FP32
         // pair sums of the mixed path); the M sum runs in R
         const double F = grad_factor<double>(K, r);

@@ -122,7 +122,7 @@ __device__ double selftest_value(unsigned long long k) {
 }
 
 __global__ void k_selftest(long long n, unsigned long long* res) {
-    unsigned long long mism = 0, ulp = 0, rel = 0;
+    unsigned long long mism = 0, ulp = 0, rel = 0, srel = 0;
     for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n;
          k += (long long)gridDim.x * blockDim.x) {
         const double x = selftest_value((unsigned long long)k);
@@ -132,22 +132,27 @@ __global__ void k_selftest(long long n, unsigned long long* res) {
         ulp = max(ulp, (unsigned long long)d);
         const double r = fabs(fma(bsc::rcp_nr(x), x, -1.0));  // relative error of 1/x
         rel = max(rel, (unsigned long long)__double_as_longlong(r));
+        const double ax = fabs(x), sx = sqrt(ax);                 // relative error of sqrt_nr
+        const double sr = fabs(bsc::sqrt_nr(ax) - sx) / sx;
+        srel = max(srel, (unsigned long long)__double_as_longlong(sr));
     }
     atomicAdd(&res[0], mism);
     atomicMax(&res[1], ulp);
     atomicMax(&res[2], rel);
+    atomicMax(&res[3], srel);
 }
 
 }  // namespace
 
-extern "C" int bsc_selftest(int64_t n, int64_t* f32_mismatches, int64_t* f32_max_ulp, double* rcp_max_rel) {
-    if (n <= 0 || !f32_mismatches || !f32_max_ulp || !rcp_max_rel) return BSC_E_INVALID;
+extern "C" int bsc_selftest(int64_t n, int64_t* f32_mismatches, int64_t* f32_max_ulp, double* rcp_max_rel,
+                            double* sqrt_max_rel) {
+    if (n <= 0 || !f32_mismatches || !f32_max_ulp || !rcp_max_rel || !sqrt_max_rel) return BSC_E_INVALID;
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return BSC_E_NOT_BUILT;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     unsigned long long* res = nullptr;
-    if (cudaMalloc(&res, 3 * sizeof(unsigned long long)) != cudaSuccess) return BSC_E_NOMEM;
-    unsigned long long h[3] = {0, 0, 0};
+    if (cudaMalloc(&res, 4 * sizeof(unsigned long long)) != cudaSuccess) return BSC_E_NOMEM;
+    unsigned long long h[4] = {0, 0, 0, 0};
     cudaMemcpy(res, h, sizeof h, cudaMemcpyHostToDevice);
     k_selftest<<<sms * 8, 256>>>((long long)n, res);
     cudaMemcpy(h, res, sizeof h, cudaMemcpyDeviceToHost);
@@ -158,5 +163,7 @@ extern "C" int bsc_selftest(int64_t n, int64_t* f32_mismatches, int64_t* f32_max
     double r;
     std::memcpy(&r, &h[2], sizeof r);
     *rcp_max_rel = r;
+    std::memcpy(&r, &h[3], sizeof r);
+    *sqrt_max_rel = r;
     return BSC_OK;
 }

@@ -359,7 +359,8 @@ int bsc_measure_peaks(double* fp64_gflops, double* fp32_gflops, double* copy_gbs
  * FP64->FP32 rounding against the hardware conversion (inputs that differ,
  * largest difference in FP32 ulps) and the Newton-Raphson reciprocal (largest
  * |x r(x) - 1|). */
-int bsc_selftest(int64_t n, int64_t* f32_mismatches, int64_t* f32_max_ulp, double* rcp_max_rel);
+int bsc_selftest(int64_t n, int64_t* f32_mismatches, int64_t* f32_max_ulp, double* rcp_max_rel,
+                 double* sqrt_max_rel);
 
 #ifdef __cplusplus
 }

@@ -55,12 +55,14 @@ def test_newton_reciprocal_assembly_matches_division():
 def test_device_arithmetic_selftest():
     """f32_of (FP64 -> FP32 rounding on the integer pipe) against the
     hardware conversion: at most one FP32 ulp apart, and apart only on exact
-    ties (rounded away from zero, not to even); rcp_nr within 2^-44."""
+    ties (rounded away from zero, not to even); rcp_nr within 2^-44 and
+    sqrt_nr within 2^-42 of CUDA's correctly rounded sqrt."""
     from beach_slope_confined_gb300 import selftest
 
     n = 1 << 22
-    mism, max_ulp, rcp_rel = selftest(n)
-    print("f32_of mismatches", mism, "max ulp", max_ulp, "rcp_nr max rel", rcp_rel)
+    mism, max_ulp, rcp_rel, sqrt_rel = selftest(n)
+    print("f32_of mismatches", mism, "max ulp", max_ulp, "rcp_nr max rel", rcp_rel, "sqrt_nr max rel", sqrt_rel)
     assert max_ulp <= 1
     assert mism <= n * 1e-4
     assert rcp_rel < 2.0 ** -44
+    assert sqrt_rel < 2.0 ** -42
