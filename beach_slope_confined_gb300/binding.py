@@ -53,6 +53,8 @@ COMMON_SIGNATURES = {
     "comp_vel": [_VP],
     "comp_pos": [_VP],
     "opt2_shift": [_VP],
+    "remove_particles": [_VP, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _P64],
+    "insert_particles": [_VP, ctypes.POINTER(StateView)],
     "scalart": [_VP],
     "scalarupdate": [_VP, ctypes.c_double],
     "densityupdate": [_VP],
@@ -105,6 +107,9 @@ def bind(lib: ctypes.CDLL, prefix: str) -> Dict[str, ctypes._CFuncPtr]:
 
 def _dp(a: np.ndarray):
     return a.ctypes.data_as(_PD)
+
+
+REMOVE_BUFFER_RIGHT, REMOVE_BUFFER_LEFT, REMOVE_OUTFLOW = 1, 2, 3
 
 
 class Context:
@@ -190,6 +195,20 @@ class Context:
     def comp_vel(self): self._call("comp_vel")
     def comp_pos(self): self._call("comp_pos")
     def opt2_shift(self): self._call("opt2_shift")
+    def remove_particles(self, rule: int, a: float, b: float = 0.0) -> int:
+        """bsc_remove_particles: REMOVE_BUFFER_RIGHT / _LEFT / REMOVE_OUTFLOW."""
+        k = ctypes.c_int64()
+        self._call("remove_particles", int(rule), float(a), float(b), ctypes.byref(k))
+        self.n = self.n - int(k.value) if self.n else self.n
+        return int(k.value)
+
+    def insert_particles(self, arrs: Dict[str, np.ndarray]):
+        """bsc_insert_particles: append particles (host SoA dictionary)."""
+        v = state_view(arrs)
+        self._call("insert_particles", ctypes.byref(v))
+        if self.n:
+            self.n += int(v.n)
+
     def scalart(self): self._call("scalart")
     def scalarupdate(self, stime: float): self._call("scalarupdate", float(stime))
     def densityupdate(self): self._call("densityupdate")

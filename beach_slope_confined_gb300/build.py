@@ -17,7 +17,7 @@ ROOT = os.path.dirname(PKG)
 CSRC = os.path.join(PKG, "csrc")
 BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libbsc.so")
-SOURCES = ["api.cu", "cells.cu", "pairs.cu", "ppe.cu", "mg.cu", "peaks.cu", "noalloc.cu", "wcsph.cu", "scalar.cu", "snapshot.cu"]
+SOURCES = ["api.cu", "cells.cu", "pairs.cu", "ppe.cu", "mg.cu", "peaks.cu", "noalloc.cu", "wcsph.cu", "scalar.cu", "snapshot.cu", "buffers.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
               "-Xptxas", "-warn-spills"]

@@ -511,9 +511,13 @@ int bsc_upload_state(bsc_ctx* c, const bsc_state_view* s) {
     StageTimer tm(c, BSC_T_UPLOAD);
     const int64_t n = s->n;
     int rc;
-    if (c->cap != n) {
+    if (c->cap < n || c->cap > 2 * n) {
         c->ncell = 0;
-        if ((rc = alloc_for(c, n))) return rc;
+        if ((rc = alloc_for(c, std::max(n, c->cap_hint)))) return rc;
+        c->cap_hint = 0;
+    } else if (c->n != n) {  // the arrays have room: drop what was sized for the old count
+        drop_graphs(c);
+        wc_free(c);
     }
     c->n = n;
     if ((rc = setup_grid(c, s->x, s->y, n))) return rc;

@@ -324,6 +324,7 @@ struct Ctx {
     // engines at once), forked from and joined back into `stream`
     WcState* wc = nullptr;        // WCSPH forward/adjoint state, after bsc_wcsph_setup
     SnapState* snap = nullptr;    // snapshot staging and its writer thread
+    int64_t cap_hint = 0;         // the next allocation's capacity (particle insertion headroom)
     static constexpr int NCOPY = 4;
     cudaStream_t copy_stream[NCOPY] = {};
     cudaEvent_t copy_ev[NCOPY + 1] = {};
@@ -378,6 +379,12 @@ struct StageTimer {
 // ---- module entry points (implemented in the .cu files) -----------------------
 // cells.cu
 int cells_build(Ctx* c, bool allow_reorder);
+int scan_exclusive(Ctx* c, const int32_t* in, int32_t* out, int n);
+// every FP64 field of a State, for kernels that move whole particles
+struct FieldPtrs {
+    double* d[N_DBL_FIELDS];
+};
+FieldPtrs fields_of(State& s);
 int solids_build(Ctx* c);
 int op_projection(Ctx* c);
 int op_piston(Ctx* c);

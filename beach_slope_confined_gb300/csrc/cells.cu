@@ -142,9 +142,6 @@ __global__ void k_sort_cells(int ncell, const int32_t* __restrict__ start, const
     }
 }
 
-struct FieldPtrs {
-    double* d[N_DBL_FIELDS];
-};
 
 __global__ void k_gather_state(int64_t n, const int32_t* __restrict__ perm, FieldPtrs src, FieldPtrs dst,
                                const int8_t* __restrict__ tid_s, int8_t* __restrict__ tid_d,

@@ -246,6 +246,25 @@ int bsc_densityupdate(bsc_ctx* ctx);              /* scalar.f90:277-305      */
  * loop are not part of this library). */
 int bsc_step(bsc_ctx* ctx, int32_t nsteps, bsc_solve_info* last);
 
+/* ---- particles leaving and entering (internal.f90:475-614) -------------- */
+enum {
+    BSC_REMOVE_BUFFER_RIGHT = 1,  /* remove_buffer1: buffer particles with x >= a */
+    BSC_REMOVE_BUFFER_LEFT = 2,   /* remove_buffer2: buffer particles with x <= a */
+    BSC_REMOVE_OUTFLOW = 3        /* cellshiftalt (integrator.f90:55-110): fluid,
+                                   * not buffer, x <= a (xlcutoff), y > b (ytcutoff) */
+};
+/* Remove the particles a rule selects, compacting the state on the device;
+ * the survivors keep their order and are renumbered 0..n'-1 in it (a
+ * download returns the host arrays minus the removed particles).  *removed
+ * (optional) receives the count.  Neighbour lists are empty until the next
+ * bsc_neighbour. */
+int bsc_remove_particles(bsc_ctx* ctx, int32_t rule, double a, double b, int64_t* removed);
+/* Append particles (insert_buffer1/2: the host picks the template particles
+ * and sets tid, mass, density, oden, ovol, con and the buffer flag); they
+ * take the ids after the last.  Fields left NULL default as in
+ * bsc_upload_state. */
+int bsc_insert_particles(bsc_ctx* ctx, const bsc_state_view* add);
+
 /* ---- text snapshots (output.f90:188-234 `combined`) --------------------- */
 /* Queue a snapshot of the current state: <dir>/fluid/fluid_<index>.txt,
  * <dir>/buffer/buffer_<index>.txt and <dir>/fluid/dead_<index>.txt, one line

@@ -1784,3 +1784,112 @@ int orc_wcsph_adjoint(orc_ctx* o, const double* dJ, double* grad) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// particles leaving and entering: internal.f90:544-614 remove_buffer1/2, the
+// outflow cut-off of cellshiftalt (integrator.f90:55-110) and the appends of
+// insert_buffer1/2 (internal.f90:475-542).  The state is rebuilt through
+// download and upload, which keeps the survivors' order.
+// ---------------------------------------------------------------------------
+namespace {
+
+struct OrcHost {
+    std::vector<std::vector<double>> f;
+    std::vector<double> L;
+    std::vector<int8_t> tid;
+    std::vector<uint8_t> fl;
+    bsc_state_view v{};
+};
+
+double* bsc_state_view::*const ORC_DBL[] = {
+    &bsc_state_view::x,       &bsc_state_view::y,      &bsc_state_view::vx,    &bsc_state_view::vy,
+    &bsc_state_view::xs,      &bsc_state_view::ys,     &bsc_state_view::vxs,   &bsc_state_view::vys,
+    &bsc_state_view::p,       &bsc_state_view::rho,    &bsc_state_view::oden,  &bsc_state_view::mass,
+    &bsc_state_view::porosity, &bsc_state_view::gradvx, &bsc_state_view::nut,  &bsc_state_view::tke,
+    &bsc_state_view::resist,  &bsc_state_view::varts,  &bsc_state_view::vel,   &bsc_state_view::xrest,
+    &bsc_state_view::con,     &bsc_state_view::ovol};
+constexpr int ORC_ND = sizeof(ORC_DBL) / sizeof(ORC_DBL[0]);
+
+void host_resize(OrcHost& h, int64_t n) {
+    h.f.assign(ORC_ND, std::vector<double>(n));
+    h.L.assign(4 * n, 0.0);
+    h.tid.assign(n, 0);
+    h.fl.assign(n, 0);
+    h.v = bsc_state_view{};
+    h.v.n = n;
+    for (int k = 0; k < ORC_ND; ++k) h.v.*ORC_DBL[k] = h.f[k].data();
+    h.v.L = h.L.data();
+    h.v.tid = h.tid.data();
+    h.v.flags = h.fl.data();
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_remove_particles(orc_ctx* o, int32_t rule, double a, double b, int64_t* removed_out) {
+    if (!o) return BSC_E_INVALID;
+    if (rule < BSC_REMOVE_BUFFER_RIGHT || rule > BSC_REMOVE_OUTFLOW)
+        return fail(o, BSC_E_INVALID, "remove_particles: unknown rule");
+    const int64_t n = o->n;
+    std::vector<char> keep(n);
+    int64_t kept = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        const bool buf = has(o->flags[i], BSC_FLAG_BUFFER);
+        bool rm = false;
+        if (rule == BSC_REMOVE_BUFFER_RIGHT) rm = buf && o->x[i] >= a;   // internal.f90:559-560
+        if (rule == BSC_REMOVE_BUFFER_LEFT) rm = buf && o->x[i] <= a;    // internal.f90:595-596
+        if (rule == BSC_REMOVE_OUTFLOW)                                 // integrator.f90:60-61
+            rm = o->tid[i] == BSC_TID_FLUID && !buf && o->x[i] <= a && o->y[i] > b;
+        keep[i] = !rm;
+        kept += !rm;
+    }
+    if (removed_out) *removed_out = n - kept;
+    if (kept == 0) return fail(o, BSC_E_INVALID, "remove_particles: the rule removes every particle");
+    if (kept == n) {
+        o->have_lists = o->have_csr = false;
+        return BSC_OK;
+    }
+    OrcHost all, out;
+    host_resize(all, n);
+    orc_download_state(o, &all.v);
+    host_resize(out, kept);
+    for (int64_t i = 0, d = 0; i < n; ++i) {
+        if (!keep[i]) continue;
+        for (int k = 0; k < ORC_ND; ++k) out.f[k][d] = all.f[k][i];
+        for (int q = 0; q < 4; ++q) out.L[4 * d + q] = all.L[4 * i + q];
+        out.tid[d] = all.tid[i];
+        out.fl[d] = all.fl[i];
+        ++d;
+    }
+    return orc_upload_state(o, &out.v);
+}
+
+int orc_insert_particles(orc_ctx* o, const bsc_state_view* a) {
+    if (!o || !a || a->n <= 0) return BSC_E_INVALID;
+    const int64_t n = o->n, m = a->n, t = n + m;
+    OrcHost all;
+    host_resize(all, t);
+    all.v.n = n;
+    orc_download_state(o, &all.v);
+    for (int k = 0; k < ORC_ND; ++k) {
+        const double* src = a->*ORC_DBL[k];
+        for (int64_t q = 0; q < m; ++q) {
+            double v = 0.0;
+            if (src) v = src[q];
+            else if (ORC_DBL[k] == &bsc_state_view::porosity) v = 1.0;
+            else if (ORC_DBL[k] == &bsc_state_view::xrest) v = a->x[q];
+            else if (ORC_DBL[k] == &bsc_state_view::ovol) v = a->mass[q] / a->oden[q];
+            all.f[k][n + q] = v;
+        }
+    }
+    for (int64_t q = 0; q < m; ++q) {
+        for (int r = 0; r < 4; ++r) all.L[4 * (n + q) + r] = a->L ? a->L[4 * q + r] : (r == 0 || r == 3 ? 1.0 : 0.0);
+        all.tid[n + q] = a->tid[q];
+        all.fl[n + q] = a->flags[q];
+    }
+    all.v.n = t;
+    return orc_upload_state(o, &all.v);
+}
+
+}  // extern "C"
