@@ -55,6 +55,7 @@ COMMON_SIGNATURES = {
     "opt2_shift": [_VP],
     "remove_particles": [_VP, ctypes.c_int32, ctypes.c_double, ctypes.c_double, _P64],
     "insert_particles": [_VP, ctypes.POINTER(StateView)],
+    "particle_count": [_VP, _P64],
     "scalart": [_VP],
     "scalarupdate": [_VP, ctypes.c_double],
     "densityupdate": [_VP],
@@ -167,6 +168,7 @@ class Context:
     def download_state(self, out: Optional[Dict[str, np.ndarray]] = None) -> Dict[str, np.ndarray]:
         """The state in id order; into `out` (arrays shaped as empty_state's,
         e.g. in pinned host memory) when given, else into new arrays."""
+        self.n = self.particle_count()
         if out is None:
             out = empty_state(self.n)
         v = state_view(out)
@@ -195,19 +197,23 @@ class Context:
     def comp_vel(self): self._call("comp_vel")
     def comp_pos(self): self._call("comp_pos")
     def opt2_shift(self): self._call("opt2_shift")
+    def particle_count(self) -> int:
+        k = ctypes.c_int64()
+        self._call("particle_count", ctypes.byref(k))
+        return int(k.value)
+
     def remove_particles(self, rule: int, a: float, b: float = 0.0) -> int:
         """bsc_remove_particles: REMOVE_BUFFER_RIGHT / _LEFT / REMOVE_OUTFLOW."""
         k = ctypes.c_int64()
         self._call("remove_particles", int(rule), float(a), float(b), ctypes.byref(k))
-        self.n = self.n - int(k.value) if self.n else self.n
+        self.n = self.particle_count()
         return int(k.value)
 
     def insert_particles(self, arrs: Dict[str, np.ndarray]):
         """bsc_insert_particles: append particles (host SoA dictionary)."""
         v = state_view(arrs)
         self._call("insert_particles", ctypes.byref(v))
-        if self.n:
-            self.n += int(v.n)
+        self.n = self.particle_count()
 
     def scalart(self): self._call("scalart")
     def scalarupdate(self, stime: float): self._call("scalarupdate", float(stime))
@@ -232,6 +238,7 @@ class Context:
 
     # -- parity hooks -------------------------------------------------------
     def get_neighbors(self) -> Tuple[np.ndarray, np.ndarray]:
+        self.n = self.particle_count()
         off = np.zeros(self.n + 1, np.int64)
         self._call("get_neighbors", off.ctypes.data_as(_P64), None)
         ids = np.zeros(int(off[-1]), np.int32)
@@ -239,6 +246,7 @@ class Context:
         return off, ids
 
     def export_csr(self):
+        self.n = self.particle_count()
         rp = np.zeros(self.n + 1, np.int64)
         self._call("export_csr", rp.ctypes.data_as(_P64), None, None, None)
         col = np.zeros(int(rp[-1]), np.int32)

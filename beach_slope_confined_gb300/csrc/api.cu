@@ -398,6 +398,8 @@ int bsc_default_params(bsc_params* p, double dl) {
     p->buffer_con = 0.5;       // scalar.f90:260-264
     p->buffer_con_xmax = 1.6;
     p->salinity = 0;
+    p->outflow = 0;
+    p->outflow_xcut = p->outflow_ycut = 0.0;
     return BSC_OK;
 }
 
@@ -792,6 +794,11 @@ int bsc_step(bsc_ctx* c, int32_t nsteps, bsc_solve_info* last) {
         RUN(BSC_T_COMP_VEL, op_comp_vel(c));
         RUN(BSC_T_COMP_POS, op_comp_pos(c));
         RUN(BSC_T_CELLSHIFT, cells_build(c, true));
+        if (c->P.outflow) {  // cellshiftalt's outflow cut-off (integrator.f90:60-61)
+            int64_t gone = 0;
+            RUN(BSC_T_CELLSHIFT, bsc_remove_particles(c, BSC_REMOVE_OUTFLOW, c->P.outflow_xcut, c->P.outflow_ycut,
+                                                      &gone));
+        }
         RUN(BSC_T_NEIGHBOUR, op_neighbour(c));
         RUN(BSC_T_FREESURF, op_freesurf(c));
         RUN(BSC_T_EFFPOR, op_effpor(c));

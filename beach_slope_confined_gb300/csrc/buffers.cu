@@ -102,6 +102,12 @@ int bsc_remove_particles(bsc_ctx* c, int32_t rule, double a, double b, int64_t* 
     return cells_build(c, false);
 }
 
+int bsc_particle_count(const bsc_ctx* c, int64_t* n) {
+    if (!c || !n) return BSC_E_INVALID;
+    *n = c->n;
+    return BSC_OK;
+}
+
 int bsc_insert_particles(bsc_ctx* c, const bsc_state_view* a) {
     if (!c || !a) return BSC_E_INVALID;
     if (!c->have_state) return set_err(c, BSC_E_INVALID, "insert_particles before upload_state");

@@ -341,7 +341,7 @@ class Params(ctypes.Structure):
         ("piston_phase", _D * 8), ("piston_ramp", _D), ("xmin", _D), ("xmax", _D), ("ymin", _D),
         ("ymax", _D), ("mg_omega", _D), ("mg_scale", _D), ("mg_sweeps", _I), ("mg_coarse_max", _I),
         ("disp_long", _D), ("disp_trans", _D), ("buffer_con", _D), ("buffer_con_xmax", _D),
-        ("salinity", _I),
+        ("salinity", _I), ("outflow", _I), ("outflow_xcut", _D), ("outflow_ycut", _D),
     ]
 
 

@@ -131,6 +131,11 @@ typedef struct bsc_params {
     double  buffer_con_xmax;     /* ... left of this x (scalar.f90:260-264)        */
     int32_t salinity;            /* 1: bsc_step runs the phase-3 step of           *
                                   * main.f90:198-260 with salinity sub-steps       */
+    int32_t outflow;             /* 1: bsc_step drops fluid, non-buffer particles  *
+                                  * with x <= outflow_xcut and y > outflow_ycut at  *
+                                  * its second cell shift (cellshiftalt,           *
+                                  * integrator.f90:55-110)                         */
+    double  outflow_xcut, outflow_ycut;  /* xlcutoff, ytcutoff (setup.f90:77-78)   */
 } bsc_params;
 
 /* Host-side particle state, structure of arrays, n entries each, id order.
@@ -264,6 +269,9 @@ int bsc_remove_particles(bsc_ctx* ctx, int32_t rule, double a, double b, int64_t
  * take the ids after the last.  Fields left NULL default as in
  * bsc_upload_state. */
 int bsc_insert_particles(bsc_ctx* ctx, const bsc_state_view* add);
+/* The current particle count (it changes with removals, insertions and the
+ * outflow cut-off of bsc_step). */
+int bsc_particle_count(const bsc_ctx* ctx, int64_t* n);
 
 /* ---- text snapshots (output.f90:188-234 `combined`) --------------------- */
 /* Queue a snapshot of the current state: <dir>/fluid/fluid_<index>.txt,

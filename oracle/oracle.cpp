@@ -1245,6 +1245,8 @@ int orc_densityupdate(orc_ctx* o) {
     return BSC_OK;
 }
 
+int orc_remove_particles(orc_ctx* o, int32_t rule, double a, double b, int64_t* removed_out);
+
 // main.f90:41-65; with salinity, the phase-3 loop of main.f90:198-260
 // (without its open-boundary buffers)
 int orc_step(orc_ctx* o, int32_t nsteps, bsc_solve_info* last) {
@@ -1275,6 +1277,11 @@ int orc_step(orc_ctx* o, int32_t nsteps, bsc_solve_info* last) {
         orc_comp_vel(o);
         orc_comp_pos(o);
         orc_cellshift(o, 1);
+        if (o->P.outflow) {  // cellshiftalt's outflow cut-off (integrator.f90:60-61)
+            int64_t gone = 0;
+            st = orc_remove_particles(o, BSC_REMOVE_OUTFLOW, o->P.outflow_xcut, o->P.outflow_ycut, &gone);
+            if (st != BSC_OK) return st;
+        }
         orc_neighbour(o);
         orc_freesurf(o);
         orc_effpor(o);
@@ -1863,6 +1870,12 @@ int orc_remove_particles(orc_ctx* o, int32_t rule, double a, double b, int64_t* 
         ++d;
     }
     return orc_upload_state(o, &out.v);
+}
+
+int orc_particle_count(const orc_ctx* o, int64_t* n) {
+    if (!o || !n) return BSC_E_INVALID;
+    *n = o->n;
+    return BSC_OK;
 }
 
 int orc_insert_particles(orc_ctx* o, const bsc_state_view* a) {

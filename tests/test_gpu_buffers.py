@@ -72,3 +72,20 @@ def test_insertion_grows_and_matches_oracle():
         assert rel_l2(a[f], b[f]) < 1e-12, f
     for f in ("vx", "vy", "p"):
         assert rel_l2(a[f], b[f]) < 1e-7, f
+
+
+def test_outflow_inside_the_step_matches_oracle():
+    spec = small_spec()
+    scen = sc.build(spec)
+    P = sc.make_params(spec, scen.bounds, tol=1e-12, maxit=20000)
+    P.outflow, P.outflow_xcut, P.outflow_ycut = 1, 0.5, 0.26  # drops the top rows near the piston
+    g, c = make_pair(scen, P, Solver)
+    n0 = g.download_state()["x"].size
+    for ctx in (g, c):
+        ctx.step(3)
+    a, b = g.download_state(), c.download_state()
+    assert a["x"].size == b["x"].size < n0
+    for f in ("x", "y"):
+        assert rel_l2(a[f], b[f]) < 1e-12, f
+    for f in ("vx", "vy", "p"):
+        assert rel_l2(a[f], b[f]) < 1e-7, f
