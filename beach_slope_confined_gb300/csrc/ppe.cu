@@ -1228,10 +1228,13 @@ __global__ void __launch_bounds__(RED_BLOCK) k_spmv_f(int64_t n, EllPackF A, con
     GRID_LOOP(i, n) w[i] = A.template row<float, float>(i, z);
 }
 
-// h_i = V_i . w for i <= j, 8 columns per pass
+// h_i = V_i . w for i <= j, 8 columns per pass; the block that finishes last
+// (ticket taken after a fence) sums the partials into column j of H, one
+// warp per dot in lane order as k_fg_hcol does
 __global__ void __launch_bounds__(RED_BLOCK) k_fgf_mdot(int64_t n, const float* __restrict__ V,
                                                          const float* __restrict__ w, int j,
-                                                         double* __restrict__ part, const Scalars* __restrict__ sc) {
+                                                         double* __restrict__ part, const Scalars* __restrict__ sc,
+                                                         unsigned* __restrict__ ticket, double* Hd, FgLayout F) {
     if (fg_skip(sc)) return;
     for (int i0 = 0; i0 <= j; i0 += 8) {
         float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -1244,6 +1247,65 @@ __global__ void __launch_bounds__(RED_BLOCK) k_fgf_mdot(int64_t n, const float* 
         }
         block_partials<8>(acc, part + (int64_t)i0 * RED_GRID);
         __syncthreads();
+    }
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int i = wp; i <= j; i += nw) {
+        double x = 0.0;
+        for (int k = lane; k < RED_GRID; k += 32) x += __ldcg(part + (int64_t)i * RED_GRID + k);
+        x = warp_sum_to_lane0(x);
+        if (lane == 0) {
+            Hd[F.hc(i)] = x;
+            Hd[F.H(i, j)] = x;
+        }
+    }
+    if (threadIdx.x == 0) *ticket = 0u;
+}
+
+// w -= sum_i h_i V_i and the partials of w.w; the block that finishes last
+// runs the Givens step of k_fg_givens (h(j+1,j) = ||w||, rotations,
+// residual estimate) and copies the scalars to the host mirror
+__global__ void __launch_bounds__(RED_BLOCK) k_fgf_maxpy_givens(int64_t n, const float* __restrict__ V,
+                                                                 float* __restrict__ w, int j, double* Hd, FgLayout F,
+                                                                 double* __restrict__ part, Scalars* sc,
+                                                                 unsigned* __restrict__ ticket, Scalars* mirror) {
+    if (fg_skip(sc)) {  // the cycle has stopped: publish the scalars as k_fg_givens does
+        if (mirror && blockIdx.x == 0 && threadIdx.x == 0) *mirror = *sc;
+        return;
+    }
+    __shared__ float h[FG_MAXM];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) h[i] = (float)Hd[F.hc(i)];
+    __syncthreads();
+    float acc = 0.f;
+    GRID_LOOP(k, n) {
+        float s = w[k];
+        for (int i = 0; i <= j; ++i) s -= h[i] * V[(int64_t)i * n + k];
+        w[k] = s;
+        acc += s * s;
+    }
+    float a[1] = {acc};
+    block_partials<1>(a, part);
+    __shared__ bool last;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    fg_givens(part, sc, Hd, F, j);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *ticket = 0u;
+        if (mirror) *mirror = *sc;
     }
 }
 
@@ -1327,13 +1389,13 @@ int run_fgmres_ir_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
                 k_spmv_f<<<blocks_for(n, B), B, 0, c->stream>>>(n, Af, zj, w, c->sc);
                 if (c->timing) record_event(c, c->ev_spmv[3 + 2 * (j & 1)]);
                 if (c->prof_iter) record_event(c, c->ev_it[4]);
-                k_fgf_mdot<<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc);
-                k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, 0, c->sc);
-                k_fgf_maxpy<<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, 1, c->part, c->sc);
-                k_fg_givens<<<1, B, 0, c->stream>>>(c->part, c->sc, c->Hd, F, j, mirror);
+                // the column of H and the Givens step finish in the last
+                // block of the dot and update kernels (no single-block launches)
+                k_fgf_mdot<<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc, c->ticket, c->Hd, F);
+                k_fgf_maxpy_givens<<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, c->part, c->sc, c->ticket, mirror);
                 k_fgf_next<<<G, B, 0, c->stream>>>(n, w, V, j, c->sc);
                 if (c->prof_iter) record_event(c, c->ev_it[5]);
-                c->launches += 6;
+                c->launches += 4;
                 BSC_CUDA(c, cudaGetLastError());
                 return BSC_OK;
             });
