@@ -550,8 +550,8 @@ __global__ void __launch_bounds__(MG_TAIL_THREADS) k_mg_tail(TailArgs<T> P) {
 // ---- V-cycle, level 0 (the PPE, unit diagonal) ---------------------------------------
 // VI: type of the right-hand side v; O: type of the result z (the last sweep)
 // two sweeps from a zero guess: x1 = w v; x2 = x1 + w (v - A x1)
-template <typename T, typename VI, typename AV>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, EllOp<AV> A, const VI* __restrict__ v, T w,
+template <typename T, typename VI, typename Op>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_pre2(int64_t n, Op A, const VI* __restrict__ v, T w,
                                                         T w1, T* __restrict__ x, const Scalars* __restrict__ sk) {
     if (mg_skip(sk)) return;
     GRID_LOOP(i, n) {
@@ -569,8 +569,8 @@ __global__ void k_mg0_scale(int64_t n, const VI* __restrict__ v, T w, T* __restr
 }
 
 // x_out = x + w (v - A x)
-template <typename T, typename VI, typename O, typename AV>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<AV> A, const VI* __restrict__ v,
+template <typename T, typename VI, typename O, typename Op>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, Op A, const VI* __restrict__ v,
                                                          const T* __restrict__ x, T w, O* __restrict__ xout,
                                                          const Scalars* __restrict__ sk) {
     if (mg_skip(sk)) return;
@@ -578,8 +578,8 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg0_sweep(int64_t n, EllOp<AV> A, 
 }
 
 // r = v - A x
-template <typename T, typename VI, typename AV>
-__global__ void __launch_bounds__(MG_BLOCK) k_mg0_resid(int64_t n, EllOp<AV> A, const VI* __restrict__ v,
+template <typename T, typename VI, typename Op>
+__global__ void __launch_bounds__(MG_BLOCK) k_mg0_resid(int64_t n, Op A, const VI* __restrict__ v,
                                                          const T* __restrict__ x, T* __restrict__ r,
                                                          const Scalars* __restrict__ sk) {
     if (mg_skip(sk)) return;
@@ -649,15 +649,17 @@ Lv<T> level_view(const MgLevel& L) {
 // flexible Krylov method whose residuals use the FP32 and FP64 operators, so
 // the FP16 rounding (2^-11 relative) can cost iterations, never accuracy;
 // it cuts the bytes of the three matrix passes per V-cycle by a quarter.
+// (The packed FP32 entries of the FP32 SpMV, one 8-byte load per entry, made
+// these passes slower: 10.29 against 10.17 ms per c3 step.)
 template <typename T>
-struct FineVal;
+struct FineOp;
 template <>
-struct FineVal<double> { using type = double; };
+struct FineOp<double> { using type = EllOp<double>; };
 template <>
-struct FineVal<float> { using type = __half; };
+struct FineOp<float> { using type = EllOp<__half>; };
 
 template <typename T>
-EllOp<typename FineVal<T>::type> fine_op(Ctx* c);
+typename FineOp<T>::type fine_op(Ctx* c);
 template <>
 EllOp<double> fine_op<double>(Ctx* c) {
     return EllOp<double>{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
@@ -752,8 +754,8 @@ template <typename T, typename VI, typename O>
 int vcycle(Ctx* c, const VI* vin, O* z) {
     Mg& mg = c->mg;
     const int64_t n = c->n;
-    using AV = typename FineVal<T>::type;
-    const EllOp<AV> A = fine_op<T>(c);
+    using AV = typename FineOp<T>::type;  // the fine operator's type
+    const AV A = fine_op<T>(c);
     const T w = (T)c->mg_w[0], w1 = (T)c->mg_w[1], sc = (T)c->P.mg_scale;
     const int nu = c->P.mg_sweeps;
     T *P0 = (T*)mg.y0, *Q0 = (T*)mg.t0, *R0 = (T*)mg.r0;
