@@ -178,7 +178,8 @@ static int alloc_for(Ctx* c, int64_t n) {
         c->f_vol = tw; c->f_nu = tw + n; c->f_nut = tw + 2 * n; c->f_tke = tw + 3 * n; c->f_varts = tw + 4 * n;
         c->f_q = tw + 5 * n;
         if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->ellf, slots)) ||
-            (rc = dalloc(c, &c->avalh, slots)))
+            (rc = dalloc(c, &c->avalh, slots)) || (rc = dalloc(c, &c->ellh, slots)) ||
+            (rc = dalloc(c, &c->ellh_ok, (n + 31) / 32)))
             return rc;
     }
     if ((rc = dalloc(c, &c->b, n))) return rc;

@@ -281,6 +281,8 @@ struct Ctx {
     // PPE
     double* aval = nullptr;       // FP64 off-diagonals (ELL layout)
     int2* ellf = nullptr;         // FP32 off-diagonals with their columns, packed (mixed)
+    uint32_t* ellh = nullptr;     // FP16 off-diagonals with 16-bit column offsets (mixed V-cycle)
+    uint8_t* ellh_ok = nullptr;   // per 32-row slice: every offset fits 16 bits
     __half* avalh = nullptr;      // FP16 off-diagonals (mixed): the V-cycle's fine-level sweeps
     double* b = nullptr;
     float* bf = nullptr;

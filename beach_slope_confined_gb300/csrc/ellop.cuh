@@ -59,6 +59,51 @@ struct EllOp {
     }
 };
 
+// The V-cycle's FP16 copy of I + N, four bytes an entry: the column as a
+// 16-bit offset from the first row of its 32-row slice and the FP16 value,
+// one load.  A slice with an offset outside 16 bits (ok == 0; rare under
+// Morton order) reads the separate column and FP16 value arrays.  A warp
+// covers one slice, so the branch is warp-uniform.
+struct EllPack16 {
+    const uint32_t* ent;
+    const uint8_t* ok;
+    const int32_t* nbr;
+    const __half* aval;
+    const int32_t* cnt;
+    int kmax;
+    const void* key() const { return ent; }
+    template <typename X, typename A>
+    __device__ __forceinline__ A row(int64_t i, const X* __restrict__ x) const {
+        A s = (A)x[i];
+        const int m = cnt[i];
+        const int64_t e0 = ell(i, 0, kmax);
+        if (ok[i >> 5]) {
+            const int64_t b = i & ~(int64_t)31;
+            int k = 0;
+            for (; k + 8 <= m; k += 8) {
+                uint32_t p[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) p[u] = ent[e0 + (int64_t)(k + u) * 32];
+                X xv[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) xv[u] = x[b + (int16_t)(p[u] & 0xffffu)];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) s += (A)__half2float(__ushort_as_half((unsigned short)(p[u] >> 16))) * (A)xv[u];
+            }
+            for (; k < m; ++k) {
+                const uint32_t p = ent[e0 + (int64_t)k * 32];
+                s += (A)__half2float(__ushort_as_half((unsigned short)(p >> 16))) * (A)x[b + (int16_t)(p & 0xffffu)];
+            }
+        } else {
+            for (int k = 0; k < m; ++k) {
+                const int64_t e = e0 + (int64_t)k * 32;
+                s += (A)__half2float(aval[e]) * (A)x[nbr[e]];
+            }
+        }
+        return s;
+    }
+};
+
 // The mixed path's FP32 copy of I + N: each stored entry's column and value
 // packed in one 8-byte word, so an entry is one load (the same 8 bytes per
 // entry as separate column and value arrays, half the load instructions).

@@ -656,7 +656,7 @@ struct FineOp;
 template <>
 struct FineOp<double> { using type = EllOp<double>; };
 template <>
-struct FineOp<float> { using type = EllOp<__half>; };
+struct FineOp<float> { using type = EllPack16; };
 
 template <typename T>
 typename FineOp<T>::type fine_op(Ctx* c);
@@ -665,8 +665,8 @@ EllOp<double> fine_op<double>(Ctx* c) {
     return EllOp<double>{c->aval, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
 }
 template <>
-EllOp<__half> fine_op<float>(Ctx* c) {
-    return EllOp<__half>{c->avalh, c->nbr, c->cnt, c->K.kmax, c->spmv_unroll};
+EllPack16 fine_op<float>(Ctx* c) {
+    return EllPack16{c->ellh, c->ellh_ok, c->nbr, c->avalh, c->cnt, c->K.kmax};
 }
 
 // approximate solve of level l >= 1 (b_l -> x_l)

@@ -149,6 +149,29 @@ __global__ void k_vs_over_por(int64_t n, State S, double* __restrict__ q, double
     uy[i] = S.vys[i] / nn;
 }
 
+// the V-cycle's packed FP16 entries (EllPack16) of the assembled rows: one
+// thread per row over whole warps (the rows of the last slice past n count as
+// fitting), each warp one 32-row slice
+__global__ void k_pack16(int64_t n, int64_t npad, const int32_t* __restrict__ nbr, const __half* __restrict__ avalh,
+                         const int32_t* __restrict__ cnt, int kmax, uint32_t* __restrict__ ent,
+                         uint8_t* __restrict__ ok) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= npad) return;  // npad and the block size are multiples of 32: whole warps
+    bool fits = true;
+    if (i < n) {
+        const int64_t b = i & ~(int64_t)31;
+        const int m = cnt[i];
+        for (int k = 0; k < m; ++k) {
+            const int64_t e = ell(i, k, kmax);
+            const int64_t d = (int64_t)nbr[e] - b;
+            fits = fits && d >= -32768 && d <= 32767;
+            ent[e] = (uint32_t)(uint16_t)(int16_t)d | ((uint32_t)__half_as_ushort(avalh[e]) << 16);
+        }
+    }
+    const unsigned all = __all_sync(0xffffffffu, fits);
+    if ((threadIdx.x & 31) == 0) ok[i >> 5] = all ? 1 : 0;
+}
+
 int op_ppe_assemble(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "ppesolve before neighbour");
     double *q = c->s, *ux = c->tv, *uy = c->v;
@@ -166,6 +189,12 @@ int op_ppe_assemble(Ctx* c) {
                                                                  c->mixed ? c->ellf : nullptr,
                                                                  c->mixed ? c->avalh : nullptr, c->b, q, ux, uy, c->dt);
     BSC_LAUNCH(c);
+    if (c->mixed) {
+        const int64_t npad = ((c->n + 31) / 32) * 32;
+        k_pack16<<<blocks_for(npad, 256), 256, 0, c->stream>>>(c->n, npad, c->nbr, c->avalh, c->cnt, c->K.kmax,
+                                                                c->ellh, c->ellh_ok);
+        BSC_LAUNCH(c);
+    }
     c->have_csr = true;
     return BSC_OK;
 }
