@@ -67,6 +67,7 @@ struct WcState {
     double *xp = nullptr, *eta = nullptr, *part = nullptr;  // probes, eta history, partials
     // forward record
     int nsteps = 0, every = 0;
+    bool last_kept = false;                    // the forward run kept its last segment
     std::vector<double> tck;
     double* ck = nullptr;                      // checkpoints (5n each)
     int ck_cap = 0, seg_cap = 0, eta_cap = 0;
@@ -863,6 +864,11 @@ int bsc_wcsph_forward(bsc_ctx* c, int32_t nsteps, int32_t every, double* eta) {
     w->nsteps = nsteps;
     w->every = every;
     w->tck.assign(nck, 0.0);
+    // the last segment keeps what the reverse sweep reads as it runs, so the
+    // adjoint recomputes one segment fewer
+    const int last0 = (nck - 1) * every;
+    const int64_t slots = list_slots(c);
+    w->last_kept = false;
     if ((rc = wc_load(c, w->init))) return rc;
     c->t = w->t0;
     const unsigned nb = blocks_for(n, WB);
@@ -871,7 +877,16 @@ int bsc_wcsph_forward(bsc_ctx* c, int32_t nsteps, int32_t every, double* eta) {
             if ((rc = wc_save(c, w->ck + (int64_t)(s / every) * 5 * n))) return rc;
             w->tck[s / every] = c->t;
         }
-        if ((rc = wc_step(c, w, w->segn, w->segP))) return rc;
+        if (s >= last0) {
+            const int q = s - last0;
+            const Keep kq = seg_keep(w, q, n, slots);
+            if ((rc = wc_save(c, w->seg + (int64_t)q * 5 * n)) ||
+                (rc = wc_step(c, w, w->segn + (int64_t)q * n, w->segP + (int64_t)q * 2 * n, &kq)))
+                return rc;
+            if (s == nsteps - 1 && (rc = wc_save(c, w->seg + (int64_t)(q + 1) * 5 * n))) return rc;
+        } else if ((rc = wc_step(c, w, w->segn, w->segP))) {
+            return rc;
+        }
         k_wc_eta<<<nb, WB, 0, c->stream>>>(n, c->S.tid, w->mass, st_of(w->nxt, n), w->K, w->xp, w->part);
         BSC_LAUNCH(c);
         k_wc_eta_fin<<<w->K.np, WB, 0, c->stream>>>(nb, w->K, w->part, w->eta + (int64_t)s * w->K.np);
@@ -885,6 +900,7 @@ int bsc_wcsph_forward(bsc_ctx* c, int32_t nsteps, int32_t every, double* eta) {
         BSC_CUDA(c, cudaMemsetAsync(c->d_flag, 0, 4 * sizeof(int32_t), c->stream));
         return set_err(c, BSC_E_CAPACITY, "wcsph_forward: neighbour-list capacity or cell grid exceeded");
     }
+    w->last_kept = true;
     return BSC_OK;
 }
 
@@ -904,16 +920,18 @@ int bsc_wcsph_adjoint(bsc_ctx* c, const double* dJ_deta, double* grad) {
     const int nseg = (nsteps + every - 1) / every;
     for (int sgi = nseg - 1; sgi >= 0; --sgi) {
         const int s0 = sgi * every, s1 = std::min(nsteps, s0 + every);
-        // recompute the segment, keeping states, lists, porosities, pressure sums
-        if ((rc = wc_load(c, w->ck + (int64_t)sgi * 5 * n))) return rc;
+        // recompute the segment, keeping states, lists, porosities, pressure
+        // sums (the last one the forward run kept)
+        const bool kept = sgi == nseg - 1 && w->last_kept;
+        if (!kept && (rc = wc_load(c, w->ck + (int64_t)sgi * 5 * n))) return rc;
         c->t = w->tck[sgi];
-        for (int s = s0; s < s1; ++s) {
+        for (int s = s0; s < s1 && !kept; ++s) {
             const int q = s - s0;
             if ((rc = wc_save(c, w->seg + (int64_t)q * 5 * n))) return rc;
             const Keep kq = seg_keep(w, q, n, slots);
             if ((rc = wc_step(c, w, w->segn + (int64_t)q * n, w->segP + (int64_t)q * 2 * n, &kq))) return rc;
         }
-        if ((rc = wc_save(c, w->seg + (int64_t)(s1 - s0) * 5 * n))) return rc;
+        if (!kept && (rc = wc_save(c, w->seg + (int64_t)(s1 - s0) * 5 * n))) return rc;
         // reverse through the segment
         for (int s = s1 - 1; s >= s0; --s) {
             const int q = s - s0;
@@ -938,6 +956,8 @@ int bsc_wcsph_adjoint(bsc_ctx* c, const double* dJ_deta, double* grad) {
             std::swap(w->lam, w->lamn);
         }
     }
+    // the segment buffers now hold the first segment
+    if (nseg > 1) w->last_kept = false;
     BSC_CUDA(c, cudaMemcpyAsync(grad, w->grad, sizeof(double) * (2 + G), cudaMemcpyDeviceToHost, c->stream));
     BSC_CUDA(c, cudaStreamSynchronize(c->stream));
     return BSC_OK;

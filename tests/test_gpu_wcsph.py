@@ -242,3 +242,16 @@ def test_adjoint_costs_at_most_three_forwards():
     print("forward %.2f ms, adjoint %.2f ms, ratio %.2f" % (1e3 * min(tf), 1e3 * min(ta), ratio))
     assert ratio <= 3.0
     g.close()
+
+
+def test_repeated_adjoint_after_one_forward():
+    """The forward run keeps its last segment for the adjoint; a second
+    adjoint of the same run (the segment buffers then hold the first
+    segment) recomputes and gives the same gradient."""
+    g, spec, scen, grid0 = wc_case()
+    w = np.random.default_rng(9).standard_normal((NSTEPS, len(spec.probes)))
+    g.wcsph_forward(NSTEPS, 30)
+    g1 = g.wcsph_adjoint(w)
+    g2 = g.wcsph_adjoint(w)
+    assert np.max(np.abs(g1 - g2)) <= 1e-12 * np.max(np.abs(g1))
+    g.close()
