@@ -416,28 +416,31 @@ __global__ void __launch_bounds__(WB) k_wc_adj_local(int64_t n, const int8_t* __
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     double ga = 0.0, gb = 0.0;
     if (i < n && tid[i] == BSC_TID_FLUID) {
+        // the quotients by n, n^3, d and D as products with reciprocals taken once
         const double ni = nbuf[i], vx = s0.vx[i], vy = s0.vy[i], vxn = s1.vx[i], vyn = s1.vy[i];
-        const double vm = sqrt(vx * vx + vy * vy), on = 1.0 - ni, n3 = ni * ni * ni, n4 = n3 * ni, d = K.d50;
-        const double R = -K.nu * K.alpha * on * on / (n3 * d * d) - K.beta * vm * on / (n3 * d);
-        const double D = 1.0 - K.dt * R * ni;
+        const double in = 1.0 / ni, in3 = in * in * in, in4 = in3 * in, id = 1.0 / K.d50;
+        const double vm = sqrt(vx * vx + vy * vy), on = 1.0 - ni;
+        const double cA = K.nu * on * on * in3 * id * id, cB = vm * on * in3 * id;  // dR/dalpha, dR/dbeta (negated)
+        const double R = -K.alpha * cA - K.beta * cB;
+        const double iD = 1.0 / (1.0 - K.dt * R * ni);
         const double lx = lam.x[i], ly = lam.y[i];
-        const double lpx = lam.vx[i] + K.dt * lx / ni, lpy = lam.vy[i] + K.dt * ly / ni;
-        double lni = -K.dt * (lx * vxn + ly * vyn) / (ni * ni);
-        const double lax = K.dt * lpx / D, lay = K.dt * lpy / D;
-        const double lDD = -(lpx * vxn + lpy * vyn) / D;
+        const double lpx = lam.vx[i] + K.dt * lx * in, lpy = lam.vy[i] + K.dt * ly * in;
+        double lni = -K.dt * (lx * vxn + ly * vyn) * in * in;
+        const double lax = K.dt * lpx * iD, lay = K.dt * lpy * iD;
+        const double lDD = -(lpx * vxn + lpy * vyn) * iD;
         const double lR = -K.dt * ni * lDD;
         lni += -K.dt * R * lDD;
-        const double dRdn = -K.nu * K.alpha / (d * d) * (-2.0 * on / n3 - 3.0 * on * on / n4) -
-                            K.beta * vm / d * (-1.0 / n3 - 3.0 * on / n4);
+        const double dRdn = -K.nu * K.alpha * id * id * (-2.0 * on * in3 - 3.0 * on * on * in4) -
+                            K.beta * vm * id * (-in3 - 3.0 * on * in4);
         lni += lR * dRdn;
-        double lvx = lpx / D, lvy = lpy / D;
+        double lvx = lpx * iD, lvy = lpy * iD;
         if (vm > 0.0) {
-            const double c = lR * (-K.beta * on / (n3 * d)) / vm;
-            lvx += c * vx;
-            lvy += c * vy;
+            const double cv = lR * (-K.beta * on * in3 * id) / vm;
+            lvx += cv * vx;
+            lvy += cv * vy;
         }
-        ga = lR * (-K.nu * on * on / (n3 * d * d));
-        gb = lR * (-vm * on / (n3 * d));
+        ga = lR * (-cA);
+        gb = lR * (-cB);
         // a = -n P + visc + n g: d a / d n = -P + g
         lni += lax * (-Pbuf[i]) + lay * (-Pbuf[n + i] + K.g);
         la[i] = lax;
