@@ -63,6 +63,7 @@ struct WcState {
     int32_t* sg = nullptr;                     // solid -> grid cell or -1
     double *rt = nullptr, *pp = nullptr, *rh = nullptr, *drh = nullptr;  // per step
     double *vol = nullptr, *pr = nullptr;      // m/rt, p/rt^2 (per step)
+    double* dpdr = nullptr;                    // dp/drt (per step)
     double* nxt = nullptr;                     // next state (5n)
     double *xp = nullptr, *eta = nullptr, *part = nullptr;  // probes, eta history, partials
     // forward record
@@ -157,7 +158,7 @@ __global__ void k_wc_solids(int64_t ns, const double* __restrict__ sx, const dou
 // clamped density, pressure, hydrostatic density and its slope, and the
 // per-particle quotients the pair loops read (volume m/rt, p/rt^2)
 struct Pre {
-    double *rt, *pp, *rh, *drh, *vol, *pr;
+    double *rt, *pp, *rh, *drh, *vol, *pr, *dpdr;  // dpdr: dp/drt of the EOS
 };
 
 __global__ void k_wc_pre(int64_t n, const int8_t* __restrict__ tid, const double* __restrict__ mass,
@@ -165,9 +166,11 @@ __global__ void k_wc_pre(int64_t n, const int8_t* __restrict__ tid, const double
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double r = tid[i] == BSC_TID_FLUID ? fmax(rho[i], K.rho0) : rho[i];
-    double p = K.B * (pow(r / K.rho0, K.gam) - 1.0);
+    const double qg = pow(r / K.rho0, K.gam);
+    double p = K.B * (qg - 1.0);
     if (p < 0.0) p = 0.0;
     const double ir = 1.0 / r;
+    o.dpdr[i] = K.B * K.gam * qg * ir;  // B gamma (rt/rho0)^(gamma-1) / rho0
     o.rt[i] = r;
     o.pp[i] = p;
     o.vol[i] = mass[i] * ir;
@@ -579,7 +582,7 @@ __global__ void __launch_bounds__(WB) k_wc_adj_pair(
         lxx += lnk * dn[k];
         lyy += lnk * dn[n + k];
         // pressure and the clamp
-        lrt += lp * K.B * K.gam * pow(rtk / K.rho0, K.gam - 1.0) / K.rho0;
+        lrt += lp * pq.dpdr[k];
         lam_out.x[k] = lxx;
         lam_out.y[k] = lyy;
         lam_out.vx[k] = lvx;
@@ -657,7 +660,7 @@ int wc_params(Ctx* c, WcState* w, double alpha, double beta, const double* grid)
 }
 
 // one forward step on c->S; keeps n and P in nbuf, Pbuf
-Pre wc_pre(WcState* w) { return {w->rt, w->pp, w->rh, w->drh, w->vol, w->pr}; }
+Pre wc_pre(WcState* w) { return {w->rt, w->pp, w->rh, w->drh, w->vol, w->pr, w->dpdr}; }
 
 // the context's state with the model's masses
 State wc_view(Ctx* c, WcState* w) {
@@ -693,12 +696,12 @@ struct Keep {
 int64_t list_slots(const Ctx* c) { return ((c->n + 31) / 32) * 32 * (int64_t)c->K.kmax; }
 
 Keep seg_keep(WcState* w, int q, int64_t n, int64_t slots) {
-    double* pre = w->segpre + (int64_t)q * 6 * n;
+    double* pre = w->segpre + (int64_t)q * 7 * n;
     const int gc = w->K.gc;
     return {w->segnbr + (int64_t)q * slots,
             w->segcnt + (int64_t)q * n,
             w->segpc + (int64_t)q * n,
-            {pre, pre + n, pre + 2 * n, pre + 3 * n, pre + 4 * n, pre + 5 * n},
+            {pre, pre + n, pre + 2 * n, pre + 3 * n, pre + 4 * n, pre + 5 * n, pre + 6 * n},
             w->seggeo + (int64_t)q * 4 * slots,
             {w->segdn + (int64_t)q * 2 * n, w->segpgi + (int64_t)q * gc * n, w->segpgv + (int64_t)q * gc * n}};
 }
@@ -810,6 +813,7 @@ int bsc_wcsph_setup(bsc_ctx* c, const bsc_wcsph_params* p) {
         (rc = wc_alloc(c, w, &w->sw, w->ns)) || (rc = wc_alloc(c, w, &w->sg, w->ns)) ||
         (rc = wc_alloc(c, w, &w->rt, n)) || (rc = wc_alloc(c, w, &w->pp, n)) || (rc = wc_alloc(c, w, &w->rh, n)) ||
         (rc = wc_alloc(c, w, &w->drh, n)) || (rc = wc_alloc(c, w, &w->vol, n)) || (rc = wc_alloc(c, w, &w->pr, n)) ||
+        (rc = wc_alloc(c, w, &w->dpdr, n)) ||
         (rc = wc_alloc(c, w, &w->nxt, 5 * n)) ||
         (rc = wc_alloc(c, w, &w->xp, BSC_WCSPH_MAX_PROBES)) ||
         (rc = wc_alloc(c, w, &w->part, (int64_t)blocks_for(n, WB) * (2 + BSC_WCSPH_MAX_GRID))) ||
@@ -856,7 +860,7 @@ int bsc_wcsph_forward(bsc_ctx* c, int32_t nsteps, int32_t every, double* eta) {
             (rc = wc_alloc(c, w, &w->segnbr, (int64_t)every * slots)) ||
             (rc = wc_alloc(c, w, &w->segcnt, (int64_t)every * n)) ||
             (rc = wc_alloc(c, w, &w->segpc, (int64_t)every * n)) ||
-            (rc = wc_alloc(c, w, &w->segpre, (int64_t)every * 6 * n)) ||
+            (rc = wc_alloc(c, w, &w->segpre, (int64_t)every * 7 * n)) ||
             (rc = wc_alloc(c, w, &w->seggeo, (int64_t)every * 4 * slots)) ||
             (rc = wc_alloc(c, w, &w->segdn, (int64_t)every * 2 * n)) ||
             (rc = wc_alloc(c, w, &w->segpgi, (int64_t)every * gc * n)) ||
