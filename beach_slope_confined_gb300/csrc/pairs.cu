@@ -449,7 +449,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
         const R varts_i = to_r<R>(S.varts[i]);
         const R inv_w0 = (R)K.inv_w0;
         const R eps6 = (R)(double)1e-6f;
-        R ax = 0, ay = 0;
+        R ax = 0, ay = 0, kx = 0, ky = 0;  // kx, ky: the SPS sum, scaled by (2/3) n_i once
         const int m = cnt[i];
         for (int k = 0; k < m; ++k) {
             const int64_t e = ell(i, k, K.kmax);
@@ -499,11 +499,14 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
             }
             ax += geo * dvx * visc;
             ay += geo * dvy * visc;
-            // SPS turbulence (:645-666)
+            // SPS turbulence (:645-666): -(2/3) n_i sum_j V_j (k_j - k_i) L grad W
             const R dk = pvol * ((F32 ? (R)f_tke[j] : (R)S.tke[j]) - tkei);
-            ax -= dk * gx * ni * (R)2 / (R)3;
-            ay -= dk * gy * ni * (R)2 / (R)3;
+            kx += dk * gx;
+            ky += dk * gy;
         }
+        const R sps = ni * (R)2 / (R)3;
+        ax -= kx * sps;
+        ay -= ky * sps;
         const double nn = S.por[i], R_ = S.resist[i];
         double vxs, vys;
         if constexpr (F32) {
