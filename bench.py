@@ -462,6 +462,48 @@ def run_salinity(args):
                          "written_after_ms": 1e3 * (t3 - t0)}}
 
 
+def run_reference_tank(args, threads: int):
+    """The reference's own tank (init + gen_boundary + gen_fluid of
+    setup.f90, boundary.f90, internal.f90) stepped on the FP64 drop-in path
+    with the reference's solver stop (FGMRES to 1e-3 of ||r0||, at most 150
+    iterations; restart 64, this library's cap), beside the oracle's step on
+    the host cores."""
+    from beach_slope_confined_gb300 import Solver, reference_geometry as rg
+
+    tank = rg.build()
+    P = rg.params(tank, solver="fgmres", tol=float(np.float32(1e-3)), maxit=150, restart=64, tol_mode=1)
+    g = Solver(P)
+    rg.setup(g, tank)
+    for _ in range(max(args.warmup, 3)):
+        g.step(1)
+    g.synchronize()
+    g.reset_timings()
+    steps = 20
+    for _ in range(steps):
+        g.step(1)
+    g.synchronize()
+    step_ms = g.timings().ms[T_STEP] / steps
+    g.close()
+    s = tank.scenario
+    nf = int(np.count_nonzero(s.tid == 3))
+    out = {"workload": f"the reference's own tank: {s.n} particles ({nf} fluid) and {s.sx.size} soil solids, "
+                       f"hybrid kernel h1={tank.constants.h1:.5f} m, FP64 path, FGMRES(64) to 1e-3 of ||r0||, at most 150 iterations",
+           "gpu_ms_per_step": step_ms, "gpu_particle_steps_per_s": nf / (step_ms * 1e-3)}
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.set_threads(threads)
+        o = oracle.context(P)
+        rg.setup(o, tank)
+        o.step(1)
+        t0 = time.perf_counter()
+        o.step(3)
+        cpu_ms = (time.perf_counter() - t0) / 3 * 1e3
+        out.update(oracle_ms_per_step=cpu_ms, oracle_threads=threads, gpu_speedup=cpu_ms / step_ms)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -480,6 +522,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-wcsph", action="store_true", help="skip the WCSPH forward/adjoint workload (c4)")
     ap.add_argument("--no-salinity", action="store_true", help="skip the salinity-transport step measurement")
+    ap.add_argument("--no-reference-tank", action="store_true", help="skip the reference's own tank")
     ap.add_argument("--cpu-iters", type=float, default=1350.0,
                     help="PPE iterations per step the reference arm's sample is scaled to")
     args = ap.parse_args()
@@ -552,6 +595,7 @@ def main():
                              "traffic": (t64 * f["n"]) if t64 else None}}
     wc = None if args.no_wcsph else run_wcsph()
     sal = None if args.no_salinity else run_salinity(args)
+    rtank = None if args.no_reference_tank else run_reference_tank(args, threads)
     cpu = None
     if not args.no_cpu:
         if ref_iters:
@@ -590,6 +634,7 @@ def main():
         "wcsph_adjoint_forward_ratio": wc["ratio"] if wc else None,
         "wcsph": wc,
         "salinity": sal,
+        "reference_tank": rtank,
     }
     print(json.dumps(line), flush=True)
     dist.close()
