@@ -467,22 +467,6 @@ def make_params(spec: TankSpec, bounds=None, *, precision="fp64", solver="bicgst
     return p
 
 
-def reference_params(dl: float) -> Params:
-    """The reference's own constants (initialize.f90:19-56, setup.f90:47-82):
-    hybrid kernel, h1 = 1.27 dl (setup.f90:47 with the fluid spacing
-    dl = 2 prrealx/sqrt(por) of internal.f90:43: h1 = dl*hfac/4), csh 0.5,
-    por 0.38, lamk 450, d50 1.02 mm, FGMRES to 1e-3 of ||r0|| with MKL's
-    default restart and iteration cap of 150."""
-    por = 0.38
-    spec = TankSpec(dx=dl, kernel=0, por=por, d50=0.00102, darcy_alpha=450.0,
-                    forch_beta=1.75 * math.sqrt(450.0 / 150.0), csh=0.5, dt=0.001)
-    p = make_params(spec, solver="fgmres", tol=float(np.float32(0.001)), maxit=150,
-                    restart=150, tol_mode=1)
-    p.h = dl * 5.08 / 4.0
-    p.lam = 0.001 * p.h * p.h
-    return p
-
-
 def state_arrays(scen: Scenario) -> Dict[str, np.ndarray]:
     """Host SoA dictionary for bsc_upload_state."""
     n = scen.n
