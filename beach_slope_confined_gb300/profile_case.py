@@ -12,6 +12,11 @@ and ignored; any other error raises.  Prints ``ok`` and the particle count.
 
 runs the WCSPH calibration workload instead: a forward run of 20 steps with
 checkpoints every 10, then the adjoint of a probe functional.
+
+    python -m beach_slope_confined_gb300.profile_case reference fp64 2000 --precond mg --steps 4
+
+runs the reference's own tank (reference_geometry.build) instead of a wave
+tank.
 """
 from __future__ import annotations
 
@@ -33,9 +38,16 @@ def main(argv=None):
     ap.add_argument("--every", type=int, default=10, help="WCSPH checkpoint interval")
     ap.add_argument("--salinity", action="store_true", help="the phase-3 step with salinity transport")
     args = ap.parse_args(argv)
-    spec = sc.config_spec(args.config)
-    scen = sc.build(spec)
-    if args.wcsph > 0:
+    tank = None
+    if args.config == "reference":
+        from . import reference_geometry as rg
+
+        tank = rg.build()
+        scen = tank.scenario
+    else:
+        spec = sc.config_spec(args.config)
+        scen = sc.build(spec)
+    if args.wcsph > 0 and tank is None:
         import numpy as np
 
         g = Solver(sc.make_params(spec, scen.bounds, precision="fp64"))
@@ -50,11 +62,14 @@ def main(argv=None):
         return
     # the inner-solve settings of bench.py for each preconditioner
     mg = args.precond == "mg"
-    P = sc.make_params(spec, scen.bounds, precision=args.precision, tol=1e-8, maxit=args.maxit,
-                       inner_tol=1e-5 if mg else 0.1, max_outer=40 if mg else 4, precond=args.precond, restart=40,
-                       salinity=args.salinity)
-    g = Solver(P)
-    setup_tank(g, scen)
+    kw = dict(precision=args.precision, tol=1e-8, maxit=args.maxit, inner_tol=1e-5 if mg else 0.1,
+              max_outer=40 if mg else 4, precond=args.precond, restart=40, salinity=args.salinity)
+    if tank is None:
+        g = Solver(sc.make_params(spec, scen.bounds, **kw))
+        setup_tank(g, scen)
+    else:
+        g = Solver(rg.params(tank, solver="fgmres", **kw))
+        rg.setup(g, tank)
     for _ in range(args.steps):
         try:
             g.step(1)
