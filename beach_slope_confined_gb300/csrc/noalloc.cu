@@ -12,13 +12,16 @@
 // The Krylov work vectors, reduction partials, solver scalars and the
 // last-block ticket live in one file-scope __device__ array of fixed size
 // (rows <= BSC_NOALLOC_MAX_ROWS).  Host code only names the array; its device
-// address comes from cudaGetSymbolAddress, looked up once per device by the
-// first call made with that device current.  Every call shares the array and
+// address on the current device comes from cudaGetSymbolAddress.  The lookup
+// is repeated on every call (a host-side table lookup once the module is
+// loaded), so an address never outlives the context it came from: after a
+// cudaDeviceReset the module loads again, possibly elsewhere.  Under CUDA's
+// lazy module loading the first call on a device loads this module, which is
+// when the array's memory is committed.  Every call shares the array and
 // leaves its contents behind, so the ticket and the scalars are cleared at
 // the start of each call; two calls whose work overlaps on the GPU (two
-// streams, or two host threads) race on the array.
-#include <mutex>
-
+// streams, or two host threads) race on the array, and on the one host-side
+// copy of the solver scalars, which is process-wide.
 #include "bsc_internal.cuh"
 
 namespace bsc {
@@ -33,39 +36,36 @@ constexpr size_t kOffHd = kOffPart + round256(8 * RED_GRID * sizeof(double));  /
 constexpr size_t kOffSc = kOffHd + round256(64 * sizeof(double));    // device scalars
 constexpr size_t kOffTicket = kOffSc + round256(sizeof(Scalars));    // last-block ticket
 constexpr size_t kScratchBytes = kOffTicket + 256;
-constexpr int kMaxDevices = 64;
 
-std::mutex g_setup_mutex;
-unsigned char* g_scratch_addr[kMaxDevices] = {};  // device address of g_scratch, per device
-Scalars g_host_scalars;                           // host copy read between iteration batches
+Scalars g_host_scalars;  // host copy read between iteration batches (process-wide)
 
 }  // namespace
 
-// the scratch itself: about 6.3 MB of device memory, reserved with the module
+// the scratch itself: about 6.3 MB of device memory on every device that
+// loads this module, held until the process exits
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-// device address of g_scratch on the current device (first call per device)
-static int scratch_address(int dev, unsigned char** out) {
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    if (!g_scratch_addr[dev]) {
-        void* ptr = nullptr;
-        if (cudaGetSymbolAddress(&ptr, g_scratch) != cudaSuccess || !ptr) {
-            (void)cudaGetLastError();
-            return BSC_E_CUDA;
-        }
-        g_scratch_addr[dev] = static_cast<unsigned char*>(ptr);
+// device address of g_scratch on the current device
+static int scratch_address(unsigned char** out) {
+    void* ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_scratch) != cudaSuccess || !ptr) {
+        (void)cudaGetLastError();
+        return BSC_E_CUDA;
     }
-    *out = g_scratch_addr[dev];
+    *out = static_cast<unsigned char*>(ptr);
     return BSC_OK;
 }
 
-static bool device_pointer(const void* p) {
+// true for memory the kernels on device `dev` may read and write directly:
+// device memory of that device, or managed memory
+static bool device_pointer(const void* p, int dev) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         (void)cudaGetLastError();
         return false;
     }
-    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+    if (a.type == cudaMemoryTypeManaged) return true;
+    return a.type == cudaMemoryTypeDevice && a.device == dev;
 }
 
 }  // namespace bsc
@@ -84,12 +84,15 @@ int bsc_csr_solve_noalloc(const bsc_params* p, int32_t n, const int32_t* rowptr,
         (void)cudaGetLastError();
         return BSC_E_NOT_BUILT;
     }
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return BSC_E_CUDA;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return BSC_E_CUDA;
+    }
     const void* ptrs[] = {rowptr, col, val, b, x};
     for (const void* q : ptrs)
-        if (!device_pointer(q)) return BSC_E_INVALID;
+        if (!device_pointer(q, dev)) return BSC_E_INVALID;
     unsigned char* base = nullptr;
-    int rc = scratch_address(dev, &base);
+    int rc = scratch_address(&base);
     if (rc) return rc;
 
     Ctx c;  // a view on the scratch: owns nothing, frees nothing

@@ -191,7 +191,11 @@ enum {
      * and the orthogonalisation */
     BSC_T_BICG_1, BSC_T_BICG_2, BSC_T_BICG_3, BSC_T_BICG_4, BSC_T_BICG_5,
     /* salinity transport: scalart, scalarupdate and densityupdate */
-    BSC_T_SCALAR
+    BSC_T_SCALAR,
+    /* single kernels inside their stages, for the FP64-pipe rooflines: the
+     * neighbour search, the PPE assembly, the int_vel pair sum, the porosity
+     * sum and the shift's pair sum */
+    BSC_T_K_NEIGHBOUR, BSC_T_K_ASSEMBLE, BSC_T_K_INT_VEL, BSC_T_K_EFFPOR, BSC_T_K_SHIFT
 };
 
 typedef struct bsc_ctx bsc_ctx;
@@ -314,18 +318,23 @@ int bsc_csr_solve(const bsc_params* p, int32_t n, const int32_t* rowptr,
  * a program whose own pool or caching allocator holds the GPU's memory, where
  * a library's cudaMalloc could fail and its cudaFree would stall the device.
  * No counterpart in the reference: it exists for such hosts only.
- *  - rowptr, col, val, b, x are DEVICE pointers owned by the caller; x holds
- *    the initial guess on entry and the solution on return.  Work is queued
- *    on `stream` (NULL: the legacy default stream) and the call returns once
- *    it has finished.
+ *  - rowptr, col, val, b, x are DEVICE pointers owned by the caller, all on
+ *    the current device (or managed memory); x holds the initial guess on
+ *    entry and the solution on return.  Work is queued on `stream` (NULL: the
+ *    legacy default stream) and the call returns once it has finished.
  *  - Nothing is allocated: the work vectors live in a fixed device array of
  *    the library sized for n <= BSC_NOALLOC_MAX_ROWS rows (about 6.3 MB).
- *    Larger n returns BSC_E_CAPACITY; host pointers, a solver other than
- *    BSC_SOLVER_BICGSTAB, or n <= 0 return BSC_E_INVALID.
- *  - The first call on each device looks up that array's device address;
- *    make it before any stream capture begins.
- *  - All calls share the array: calls whose work overlaps on the GPU (other
- *    streams, other host threads) race and must be serialised by the caller. */
+ *    Larger n returns BSC_E_CAPACITY; host pointers, pointers into another
+ *    device's memory, a solver other than BSC_SOLVER_BICGSTAB, or n <= 0
+ *    return BSC_E_INVALID.
+ *  - Under CUDA's default lazy module loading the array's memory is
+ *    committed by the first call on each device: make that call before the
+ *    host reserves its pool (or set CUDA_MODULE_LOADING=EAGER, which commits
+ *    it when the library's device code loads), and before any stream capture
+ *    begins.  Each call looks up the array's address on the current device.
+ *  - All calls share the array, and one process-wide host copy of the solver
+ *    scalars: calls whose work overlaps on the GPU (other streams, other host
+ *    threads) race and must be serialised by the caller. */
 #define BSC_NOALLOC_MAX_ROWS 131072
 int bsc_csr_solve_noalloc(const bsc_params* p, int32_t n, const int32_t* rowptr,
                           const int32_t* col, const double* val, const double* b,
