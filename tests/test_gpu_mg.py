@@ -49,7 +49,10 @@ def test_mg_cuts_iterations():
 
 
 def test_mg_mixed_against_fp64():
-    spec = small_spec(dx=0.01)
+    """The mixed path (FP32 V-cycle and inner FGMRES inside FP64 refinement)
+    against the FP64 path, two steps of the moving c1 tank: the same residual,
+    every field within 1e-6 (relative L2), the eddy viscosity included."""
+    spec = small_spec(dx=0.01, piston_ramp=0.0)
     scen = sc.build(spec)
     out, infos = {}, {}
     for prec in ("fp64", "mixed"):
@@ -58,11 +61,11 @@ def test_mg_mixed_against_fp64():
         infos[prec] = g.step(2)
         out[prec] = g.download_state()
     assert infos["mixed"].converged and infos["mixed"].rel_residual <= 1e-8
-    errs = {f: rel_l2(out["mixed"][f], out["fp64"][f]) for f in ("x", "y", "vx", "vy", "p", "porosity")}
+    errs = {f: rel_l2(out["mixed"][f], out["fp64"][f])
+            for f in ("x", "y", "vx", "vy", "p", "rho", "porosity", "nut", "tke", "vel")}
     print("mixed vs fp64 relative L2 (multigrid):", errs)
-    assert errs["x"] < 1e-9 and errs["y"] < 1e-9
-    assert errs["porosity"] < 1e-6
-    assert errs["p"] < 1e-6 and errs["vx"] < 1e-5 and errs["vy"] < 1e-5
+    for f, e in errs.items():
+        assert e < 1e-6, (f, e)
 
 
 def test_mg_deterministic():

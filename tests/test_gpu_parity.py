@@ -172,9 +172,11 @@ def test_capacity_overflow_is_reported():
 
 @pytest.mark.parametrize("solver", ["bicgstab", "fgmres"])
 def test_mixed_against_fp64(solver):
-    """FP32 pair sums / inner Krylov with FP64 refinement against the FP64 path:
-    the PPE reaches the same relative residual and every field stays close."""
-    spec = small_spec(dx=0.01)
+    """FP32 pair sums / inner Krylov with FP64 refinement against the FP64 path
+    on the moving c1 tank (piston from t = 0): the PPE reaches the same
+    relative residual and every field stays within 1e-6 (relative L2) after
+    two steps, the eddy viscosity included."""
+    spec = small_spec(dx=0.01, piston_ramp=0.0)
     scen = sc.build(spec)
     out, infos = {}, {}
     for prec in ("fp64", "mixed"):
@@ -185,8 +187,8 @@ def test_mixed_against_fp64(solver):
         out[prec] = g.download_state()
     assert infos["mixed"].converged and infos["mixed"].rel_residual <= 1e-8
     assert infos["mixed"].outer >= 1
-    errs = {f: rel_l2(out["mixed"][f], out["fp64"][f]) for f in ("x", "y", "vx", "vy", "p", "porosity", "nut")}
+    errs = {f: rel_l2(out["mixed"][f], out["fp64"][f])
+            for f in ("x", "y", "vx", "vy", "p", "rho", "porosity", "nut", "tke", "vel")}
     print("mixed vs fp64 relative L2:", errs)
-    assert errs["x"] < 1e-9 and errs["y"] < 1e-9
-    assert errs["porosity"] < 1e-6
-    assert errs["p"] < 1e-6 and errs["vx"] < 1e-5 and errs["vy"] < 1e-5
+    for f, e in errs.items():
+        assert e < 1e-6, (f, e)

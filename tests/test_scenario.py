@@ -49,11 +49,43 @@ def test_porosity_field_per_cell():
     assert g.min() >= 0.35 and g.max() <= 0.45 and g.std() > 0.01
 
 
-def test_piston_ramp_starts_at_rest():
+def test_irregular_piston_ramps_in_from_rest():
+    """c5's eight-mode stroke has seeded phases; its 0.01 s start-up ramp
+    starts the wall at rest on its lattice."""
     spec = sc.config_spec("c5")
     assert len(spec.piston_amp) == 8 and abs(sum(spec.piston_amp) - 0.03) < 1e-12
     assert min(spec.piston_period) == 0.8 and max(spec.piston_period) == 2.0
-    x0, v0 = sc.piston_stroke(spec, 0.0)
-    assert x0 == 0.0 and v0 == 0.0
+    assert spec.piston_ramp == sc.STARTUP_RAMP == 0.01
+    assert sc.piston_stroke(spec, 0.0) == (0.0, 0.0)
     x1, v1 = sc.piston_stroke(spec, 10.0)
     assert abs(x1) <= 0.03
+
+
+def test_rampless_stroke_with_phases_starts_on_its_lattice():
+    """Without a ramp a stroke with nonzero phases has x_p(0) != 0: the wall's
+    rest coordinate absorbs -x_p(0), so the wall starts one spacing from the
+    fluid and moves with the stroke's velocity."""
+    spec = sc.config_spec("c5")
+    spec.piston_ramp = 0.0
+    spec.dx = 0.01  # the layout rule does not depend on resolution
+    x0, v0 = sc.piston_stroke(spec, 0.0)
+    assert x0 != 0.0 and v0 != 0.0
+    scen = sc.build(spec)
+    pist = (scen.flags & sc.FLAG_PISTON) != 0
+    inner = pist & (scen.tid == sc.TID_WALL)
+    assert np.allclose(scen.x[inner], -0.5 * spec.dx, rtol=0, atol=1e-15)
+    assert np.allclose(scen.xrest[pist], scen.x[pist] - x0, rtol=0, atol=1e-15)
+    assert np.all(scen.vx[pist] == v0)
+    # the bottom wall reaches under the piston's leftmost excursion
+    bottom = (scen.tid == sc.TID_WALL) & (scen.y < 0) & ~pist
+    assert scen.x[bottom].min() < -0.5 * spec.dx - 2 * 0.03
+
+
+def test_baseline_piston_starts():
+    for name in ("c1", "c2"):
+        spec = sc.config_spec(name)
+        assert spec.piston_ramp == 0.0
+        assert sc.piston_stroke(spec, 0.0) == (0.0, 0.02 * 2 * np.pi / 1.2)
+    spec = sc.config_spec("c3")
+    assert spec.piston_ramp == 0.01 and sc.piston_stroke(spec, 0.0) == (0.0, 0.0)
+    assert sc.piston_stroke(spec, 0.01) == sc.piston_stroke(sc.config_spec("c1"), 0.01)
