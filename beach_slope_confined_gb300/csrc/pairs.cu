@@ -196,6 +196,7 @@ int op_neighbour(Ctx* c) {
                                                          c->mixed ? c->f_vol : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
+    StageTimer tk(c, BSC_T_K_NEIGHBOUR);
     if (c->mixed)
         k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
                                                           c->pcell, c->posf, c->nbr, c->gw, c->gwf, c->f_vol, c->ndist,
@@ -321,6 +322,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
 
 int op_effpor(Ctx* c) {
     const unsigned g = blocks_for(c->n, NB_BLOCK);
+    StageTimer tk(c, BSC_T_K_EFFPOR);
     if (c->mixed)
         k_effpor<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
                                                        c->sx, c->sy, c->sposf, c->swf, c->svol, c->spor);
@@ -559,6 +561,7 @@ int op_int_vel(Ctx* c, const double* d_umax) {
     k_kin_visc<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, nu, mx ? c->f_nu : nullptr,
                                                              mx ? c->f_nut : nullptr, mx ? c->f_tke : nullptr);
     BSC_LAUNCH(c);
+    StageTimer tk(c, BSC_T_K_INT_VEL);
     if (mx)
         k_int_vel<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, nu, c->dt,
                                                         c->f_vol, c->f_nu, c->f_nut, c->f_tke, c->f_varts);
@@ -767,8 +770,11 @@ int op_opt2_shift(Ctx* c) {
     // gradient sum that cancels heavily; in FP32 it moved the mixed path's
     // velocities by ~7e-6 (relative) from the FP64 path's after 8 steps of
     // the c3 tank, in FP64 by ~1e-6, for 0.3 ms a step
-    k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, mark);
-    BSC_LAUNCH(c);
+    {
+        StageTimer tk(c, BSC_T_K_SHIFT);
+        k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, mark);
+        BSC_LAUNCH(c);
+    }
     k_shift_apply<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, mark);
     BSC_LAUNCH(c);
     return BSC_OK;

@@ -181,14 +181,17 @@ int op_ppe_assemble(Ctx* c) {
     // FP64 assembly in both paths: the PPE coefficients are sums whose FP32
     // rounding moves the pressure by ~5e-6 (relative) at 1e-8 residual; the
     // mixed path keeps an FP32 copy for its inner sweeps
-    if (c->mixed && !c->exact_div)
-        k_assemble<double, true><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
-                                                                c->ellf, c->avalh, c->b, q, ux, uy, c->dt);
-    else
-        k_assemble<double, false><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
-                                                                 c->mixed ? c->ellf : nullptr,
-                                                                 c->mixed ? c->avalh : nullptr, c->b, q, ux, uy, c->dt);
-    BSC_LAUNCH(c);
+    {
+        StageTimer tk(c, BSC_T_K_ASSEMBLE);
+        if (c->mixed && !c->exact_div)
+            k_assemble<double, true><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,
+                                                                    c->ellf, c->avalh, c->b, q, ux, uy, c->dt);
+        else
+            k_assemble<double, false><<<g, NB_BLOCK, 0, c->stream>>>(
+                c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval, c->mixed ? c->ellf : nullptr,
+                c->mixed ? c->avalh : nullptr, c->b, q, ux, uy, c->dt);
+        BSC_LAUNCH(c);
+    }
     if (c->mixed) {
         const int64_t npad = ((c->n + 31) / 32) * 32;
         k_pack16<<<blocks_for(npad, 256), 256, 0, c->stream>>>(c->n, npad, c->nbr, c->avalh, c->cnt, c->K.kmax,

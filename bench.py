@@ -1,21 +1,30 @@
 """Benchmark of the ISPH step: particle-steps/s on the ~1M-particle wave tank.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config c3]
 
 Workload: the 4.0 m x 0.6 m tank at dx = 1.2 mm (833,250 fluid particles plus
-walls; per-cell porosity 0.4 +/- 0.05 in the slope), Wendland C2 with
-h = 1.3 dx, PPE to relative residual 1e-8 (by default FGMRES preconditioned by
-the cell-multigrid V-cycle; `--precond none` runs the reference's
-unpreconditioned BiCGSTAB), fixed dt = 1e-4 s.  A step is the whole
-main.f90:41-65 sequence (two neighbour searches, porosity, eddy viscosity,
-predictor, PPE assembly + solve, projection, shifting).  The headline `value`
-is the mixed-precision path (FP32 pair sums, FP32 inner FGMRES and V-cycle,
-FP64 assembly and refinement); the plain FP64 path is reported beside it.
+walls; per-cell porosity 0.4 +/- 0.05 in the slope; the piston driven from
+t = 0), Wendland C2 with h = 1.3 dx, PPE to relative residual 1e-8 (by
+default FGMRES preconditioned by the cell-multigrid V-cycle; `--precond none`
+runs the reference's unpreconditioned BiCGSTAB), fixed dt = 1e-4 s.  A step
+is the whole main.f90:41-65 sequence (two neighbour searches, porosity, eddy
+viscosity, predictor, PPE assembly + solve, projection, shifting).  The
+headline `value` is the mixed-precision path (FP32 pair sums, FP32 inner
+FGMRES and V-cycle, FP64 assembly and refinement); the plain FP64 path is
+reported beside it.
 
 `--impl reference` times the reference algorithm on the host cores instead:
 the C++ OpenMP restatement of the Fortran routines (the Fortran itself needs
-gfortran and Intel MKL, neither present on this machine), on a bounded sample of
-the same workload.
+gfortran and Intel MKL, neither present on this machine), full steps of the same
+tank with the reference's BiCGSTAB to the same residual, W untimed and K
+timed.
+
+Other modes (one JSON line each; no timing contract):
+  --long N          N steps of the mixed and then the FP64 path from the same
+                    start: ms and PPE iterations per step, and the mixed
+                    path's relative L2 difference from the FP64 path for
+                    every field after the run;
+  --profile-case    a short bounded run for a profiler (see `profile_case`).
 
 With `--gpus N` under torchrun every rank runs an independent replica of the
 tank on its own GPU (the step does not shard across GPUs here); value = the
@@ -41,6 +50,28 @@ sys.path.insert(0, ROOT)
 METRIC = "particle-steps/s at 1M (mixed vs FP64, PPE res 1e-8); adjoint/forward time"
 CONFIG = "c3"
 T_STEP, T_PPE_SOLVE, T_SPMV, T_SCALAR = 15, 8, 16, 24
+# single-kernel slots of bsc_timing (include/bsc.h)
+T_K_NEIGHBOUR, T_K_ASSEMBLE, T_K_INT_VEL, T_K_EFFPOR, T_K_SHIFT = 25, 26, 27, 28, 29
+
+# Algorithmic FP64 flops per pair of the pair kernels, counted from the
+# formulas each kernel evaluates (an FMA is 2 flops; a division or a square
+# root is 1): kernel slot -> (FP64 path, mixed path).  Per neighbour pair:
+#   k_neighbour: offsets 2, d^2 3, root 1, grad W factor 6, grad W 2, the
+#     moment sum M 10 (mixed: M in FP32, so 14);
+#   k_assemble: offsets 2, 1/(r^2+lam) 5, L grad W 6, the coefficient 6, the
+#     diagonal 2, rho_ij 4, velocity differences 4, divergence 5, the Jacobi
+#     scaling 1 (FP64 on both paths);
+#   k_int_vel: the two harmonic viscosity means and their sum 10, offsets
+#     and r^2 5, 1/(r^2+lam) 2, L grad W 6, the coefficient 6, velocity
+#     differences 2, viscous sums 6, SPS sums 6 (mixed: the offsets and
+#     velocity differences, 4);
+#   k_shift: 16 (FP64 on both paths).
+# Per solid pair, k_effpor: offsets 2, d^2 3, root 1, W 9, the weighted sum
+# 4 (mixed: the FP64 sum of the FP32 terms, 1).
+FP64_FLOPS = {T_K_NEIGHBOUR: (24, 14), T_K_ASSEMBLE: (35, 35), T_K_INT_VEL: (43, 4), T_K_SHIFT: (16, 16),
+              T_K_EFFPOR: (19, 1)}
+KERNEL_NAMES = {T_K_NEIGHBOUR: "k_neighbour", T_K_ASSEMBLE: "k_assemble", T_K_INT_VEL: "k_int_vel",
+                T_K_SHIFT: "k_shift", T_K_EFFPOR: "k_effpor"}
 
 
 # --------------------------------------------------------------------------
@@ -214,6 +245,51 @@ def traffic_per_row(kind: str):
         return None
 
 
+def kernel_traffic(kernel: str, prec: str, n: int):
+    """DRAM bytes per launch of a pair kernel, from the committed ncu summary
+    (bytes per row, scaled to n rows)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "kernel_dram_traffic.json")) as fh:
+            return float(json.load(fh)[f"{kernel} {prec}"]["dram_bytes_per_row"]) * n
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+def solid_pairs(scen) -> int:
+    """Fluid-solid pairs within the support 2h on the initial state: the
+    pair count of effpor's porosity sum (the solids do not move, and the
+    fluid near the bed barely does over a benchmark's steps)."""
+    from scipy.spatial import cKDTree
+
+    h = scen.spec.h_factor * scen.spec.dx
+    fl = scen.tid == 3
+    if scen.sx.size == 0:
+        return 0
+    tree = cKDTree(np.column_stack([scen.sx, scen.sy]))
+    return int(tree.count_neighbors(cKDTree(np.column_stack([scen.x[fl], scen.y[fl]])), 2.0 * h * (1 - 1e-12)))
+
+
+def kernel_rooflines(t, steps: int, nnz: int, spairs: int, prec: str, fp64_peak: float):
+    """Per FP64-bound pair kernel: event-timed ms per launch, launches per
+    step, algorithmic FP64 GFLOP/s and its fraction of the measured FP64
+    peak (FMA rate)."""
+    out = []
+    col = 0 if prec == "fp64" else 1
+    for slot, name in KERNEL_NAMES.items():
+        calls = int(t.calls[slot])
+        if calls == 0:
+            continue
+        ms = t.ms[slot] / calls
+        pairs = spairs if slot == T_K_EFFPOR else nnz
+        flops = FP64_FLOPS[slot][col] * pairs
+        gf = flops / (ms * 1e-3) / 1e9
+        out.append({"kernel": f"{name}<{'double' if col == 0 else 'float'}>", "ms_per_launch": ms,
+                    "launches_per_step": calls / steps, "ms_per_step": t.ms[slot] / steps,
+                    "fp64_flops_per_launch": flops, "pairs_per_launch": pairs, "achieved_gflops": gf,
+                    "peak_gflops": fp64_peak, "frac": gf / fp64_peak if fp64_peak else None})
+    return out
+
+
 def run_ours(args, dist: Dist):
     from beach_slope_confined_gb300 import Solver, measure_peaks, scenario as sc, setup_tank
 
@@ -222,6 +298,8 @@ def run_ours(args, dist: Dist):
     nf = scen.n_fluid
     results = {}
     states = {}
+    peaks = measure_peaks()
+    spairs = solid_pairs(scen)
     for prec in ("mixed", "fp64"):
         if prec == "fp64" and args.no_fp64:
             continue
@@ -251,7 +329,8 @@ def run_ours(args, dist: Dist):
         results[prec] = dict(value=value, ms_per_step=tmax / args.steps * 1e3, wall_s=wall, nnz=nnz,
                              iters=iters, spmv_ms=spmv_ms, spmv_calls=int(t.calls[T_SPMV]),
                              solve_ms=t.ms[T_PPE_SOLVE] / args.steps, launches=int(t.kernel_launches),
-                             clocks=clk.summary(), n=scen.n)
+                             clocks=clk.summary(), n=scen.n,
+                             kernels=kernel_rooflines(t, args.steps, nnz, spairs, prec, peaks[0]))
         states[prec] = g.download_state()
         # e2e through the C ABI with host buffers in pinned memory: every
         # step uploads the state, steps, and downloads the state
@@ -279,70 +358,56 @@ def run_ours(args, dist: Dist):
         g.close()
     errs = None
     if "fp64" in states:
-        a, b = states["mixed"], states["fp64"]
-        errs = {f: float(np.linalg.norm(a[f] - b[f]) / max(np.linalg.norm(b[f]), 1e-300))
-                for f in ("x", "y", "vx", "vy", "p", "porosity", "nut")}
-    # iterations of the reference algorithm (unpreconditioned FP64 BiCGSTAB)
-    # on the first step, to scale the CPU sample of that algorithm
-    ref_iters = None
-    if args.precond != "none" and not args.no_cpu and dist.rank == 0:
-        P = sc.make_params(spec, scen.bounds, precision="fp64", solver="bicgstab", tol=1e-8, maxit=40000)
-        g = Solver(P)
-        setup_tank(g, scen)
-        ref_iters = g.step(1).iterations
-        g.close()
-    peaks = measure_peaks() if dist.rank == 0 else None
-    return scen, results, errs, peaks, ref_iters
+        errs = field_errors(states["mixed"], states["fp64"])
+    return scen, results, errs, peaks
 
 
-def cpu_sample(scen, spec, threads: int, gpu_iters: float, solver: str):
-    """Bounded sample of the reference algorithm on the host cores: one step
-    of the CPU restatement with the PPE solve capped at 20 iterations; the
-    solve time is scaled to `gpu_iters` iterations (the FP64 GPU solve of the
-    same workload).  Returns (particle-steps/s, description)."""
+ERROR_FIELDS = ("x", "y", "vx", "vy", "p", "rho", "porosity", "nut", "tke", "vel", "gradvx", "resist", "varts")
+
+
+def field_errors(a, b):
+    """Relative L2 difference of every state field of `a` from `b`, plus
+    the x displacement since the start (x - xrest): x itself is ~1 m, so its
+    relative error says little about the motion."""
+    out = {}
+    for f in ERROR_FIELDS + ("x_displacement",):
+        if f == "x_displacement":
+            u, v = a["x"] - b["xrest"], b["x"] - b["xrest"]
+        else:
+            u, v = a[f], b[f]
+        nv = np.linalg.norm(v)
+        out[f] = float(np.linalg.norm(u - v) / nv) if nv > 0 else float(np.linalg.norm(u - v))
+    return out
+
+
+def cpu_steps(scen, spec, threads: int, steps: int, warmup: int, solver: str = "bicgstab"):
+    """Full steps of the reference algorithm on the host cores: the C++
+    OpenMP restatement, PPE by the reference's BiCGSTAB (or FGMRES) to a
+    relative residual of 1e-8, no iteration cap.  `warmup` untimed steps,
+    then `steps` timed ones.  Returns (particle-steps/s, description, PPE
+    iterations of the timed steps)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     from beach_slope_confined_gb300 import scenario as sc
     from beach_slope_confined_gb300.binding import setup_tank
 
     oracle.set_threads(threads)
-    cap = 20
-    P = sc.make_params(spec, scen.bounds, solver=solver, tol=1e-8, maxit=cap)
+    P = sc.make_params(spec, scen.bounds, solver=solver, tol=1e-8, maxit=40000, restart=30)
     o = oracle.context(P)
     setup_tank(o, scen)
-    tm = {}
-
-    def timed(name, fn):
-        t0 = time.perf_counter()
-        fn()
-        tm[name] = tm.get(name, 0.0) + time.perf_counter() - t0
-
-    o.set_time(spec.dt, spec.dt)
-    for nm in ("piston", "projection", "cellshift", "resetid", "neighbour", "effpor", "eddyvis", "int_vel"):
-        timed(nm, getattr(o, nm))
-    P0 = sc.make_params(spec, scen.bounds, solver=solver, tol=1e-8, maxit=0)
-    o0 = oracle.context(P0)
+    for _ in range(warmup):
+        o.step(1)
+    iters = []
     t0 = time.perf_counter()
-    o.ppesolve(check=False)
-    t_solve_cap = time.perf_counter() - t0
-    # assembly-only cost: the same system with no iterations
-    setup_tank(o0, scen)
-    for nm in ("piston", "projection", "cellshift", "resetid", "neighbour", "effpor", "eddyvis", "int_vel"):
-        getattr(o0, nm)()
-    t0 = time.perf_counter()
-    o0.ppesolve(check=False)
-    t_asm = time.perf_counter() - t0
-    for nm in ("comp_vel", "comp_pos"):
-        timed(nm, getattr(o, nm))
-    timed("cellshift", lambda: o.cellshift(True))
-    for nm in ("neighbour", "freesurf", "effpor", "opt2_shift", "timestep"):
-        timed(nm, getattr(o, nm))
-    t_iter = max(t_solve_cap - t_asm, 0.0) / cap
-    t_step = sum(tm.values()) + t_asm + gpu_iters * t_iter
-    desc = (f"one step of the C++ OpenMP restatement on {scen.n_fluid} fluid particles, PPE {solver} capped at "
-            f"{cap} iterations ({t_iter*1e3:.2f} ms/iteration) and scaled to {gpu_iters:.0f} iterations; "
-            f"non-solver routines {sum(tm.values()):.2f} s, assembly {t_asm:.2f} s")
-    return scen.n_fluid / t_step, desc, t_step
+    for _ in range(steps):
+        info = o.step(1)
+        iters.append(int(info.iterations))
+    wall = time.perf_counter() - t0
+    o.close()
+    desc = (f"steps {warmup + 1}-{warmup + steps} of the {scen.n_fluid}-fluid-particle tank, full steps of the "
+            f"C++ OpenMP restatement on {threads} threads, PPE {solver} to rel-res 1e-8 "
+            f"({statistics.mean(iters):.0f} iterations per step), {wall / steps:.2f} s per step")
+    return scen.n_fluid * steps / wall, desc, iters
 
 
 def run_wcsph(reps: int = 2):
@@ -507,6 +572,134 @@ def run_reference_tank(args, threads: int):
     return out
 
 
+def run_long(args):
+    """`--long N`: N steps of the mixed path and then of the FP64 path from the
+    same start, with per-step device ms and PPE iterations, and the mixed
+    path's difference from the FP64 path for every field at the end."""
+    from beach_slope_confined_gb300 import Solver, scenario as sc, setup_tank
+
+    spec = sc.config_spec(args.config)
+    scen = sc.build(spec)
+    out = {"mode": "long", "config": args.config, "steps": args.long, "fluid_particles": scen.n_fluid,
+           "precond": args.precond}
+    states = {}
+    for prec in ("mixed", "fp64"):
+        P = sc.make_params(spec, scen.bounds, precision=prec, solver=args.solver, tol=1e-8, maxit=40000,
+                           inner_tol=args.inner_tol, max_outer=60, precond=args.precond, restart=args.restart)
+        g = Solver(P)
+        setup_tank(g, scen)
+        ms, its, res = [], [], []
+        for _ in range(args.long):
+            g.reset_timings()
+            info = g.step(1)
+            t = g.timings()
+            ms.append(t.ms[T_STEP])
+            its.append(int(info.iterations))
+            res.append(float(info.rel_residual))
+        states[prec] = g.download_state()
+        g.close()
+        ms, its = np.asarray(ms), np.asarray(its)
+        win = slice(args.warmup, args.warmup + args.steps)
+        blocks = [{"steps": f"{k + 1}-{min(k + 100, args.long)}", "ms_per_step": float(ms[k:k + 100].mean()),
+                   "iterations": float(its[k:k + 100].mean())} for k in range(0, args.long, 100)]
+        out[prec] = {"ms_per_step_mean": float(ms.mean()), "ms_per_step_min": float(ms.min()),
+                     "ms_per_step_max": float(ms.max()), "iterations_mean": float(its.mean()),
+                     "iterations_min": int(its.min()), "iterations_max": int(its.max()),
+                     "max_rel_residual": float(max(res)),
+                     "bench_window": {"steps": f"{args.warmup + 1}-{args.warmup + args.steps}",
+                                      "ms_per_step": float(ms[win].mean()),
+                                      "iterations": float(its[win].mean())},
+                     "per_100_steps": blocks,
+                     "particle_steps_per_s": scen.n_fluid / (ms.mean() * 1e-3)}
+    out["mixed_over_fp64_speed"] = out["fp64"]["ms_per_step_mean"] / out["mixed"]["ms_per_step_mean"]
+    out["mixed_vs_fp64_rel_l2"] = field_errors(states["mixed"], states["fp64"])
+    fl = scen.tid == sc.TID_FLUID
+    v = np.hypot(states["fp64"]["vx"][fl], states["fp64"]["vy"][fl])
+    out["fp64_state"] = {"t": args.long * spec.dt, "max_speed": float(v.max()), "mean_speed": float(v.mean())}
+    print(json.dumps(out), flush=True)
+
+
+def profile_case(args):
+    """`--profile-case`: a short, bounded run of the step for a profiler.
+
+    Builds the `--config` tank (or the reference's own tank with
+    `--config reference`), uploads it and runs `--steps` full steps of the
+    `--precision` path with every PPE solve capped at `--maxit` Krylov
+    iterations, so a profiler sees a few launches of each kernel on the
+    full-size state.  A capped solve reports BSC_E_NOT_CONVERGED, which is
+    expected here and ignored; any other error raises.  With `--wcsph K` it
+    runs the WCSPH calibration workload instead: a forward run of K steps
+    with checkpoints every `--every`, then the adjoint of a probe functional.
+    Prints `ok` and the particle count."""
+    from beach_slope_confined_gb300 import BscError, Solver, scenario as sc, setup_tank
+
+    not_converged = -5
+    tank = None
+    if args.config == "reference":
+        from beach_slope_confined_gb300 import reference_geometry as rg
+
+        tank = rg.build()
+        scen = tank.scenario
+    else:
+        spec = sc.config_spec(args.config)
+        scen = sc.build(spec)
+    if args.wcsph > 0 and tank is None:
+        g = Solver(sc.make_params(spec, scen.bounds, precision="fp64"))
+        setup_tank(g, scen)
+        wp, _grid = sc.wcsph_params(spec, scen)
+        g.wcsph_setup(wp)
+        g.wcsph_forward(args.wcsph, args.every)
+        g.wcsph_adjoint(np.ones((args.wcsph, len(spec.probes))))
+        g.synchronize()
+        g.close()
+        print("ok", scen.n)
+        return
+    mg = args.precond == "mg"
+    kw = dict(precision=args.precision, tol=1e-8, maxit=args.maxit, inner_tol=args.inner_tol,
+              max_outer=40 if mg else 4, precond=args.precond, restart=args.restart, salinity=args.salinity)
+    if tank is None:
+        g = Solver(sc.make_params(spec, scen.bounds, solver=args.solver, **kw))
+        setup_tank(g, scen)
+    else:
+        g = Solver(rg.params(tank, solver="fgmres", **kw))
+        rg.setup(g, tank)
+    for _ in range(args.steps):
+        try:
+            g.step(1)
+        except BscError as e:
+            if e.code != not_converged:
+                raise
+    g.synchronize()
+    g.close()
+    print("ok", scen.n)
+
+
+def run_reference_arm(args, dist: Dist, threads: int):
+    """`--impl reference`: the reference algorithm on the host cores (the
+    oracle, a C++ OpenMP restatement of the Fortran), full uncapped steps of
+    the same tank: W untimed, then K timed.  Rank 0 only."""
+    from beach_slope_confined_gb300 import scenario as sc
+
+    if dist.rank != 0:
+        return
+    spec = sc.config_spec(args.config)
+    scen = sc.build(spec)
+    value, desc, iters = cpu_steps(scen, spec, threads, max(1, args.steps), args.warmup, args.ref_solver)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * scen.n_fluid / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded wave tank, no dataset)",
+            "config": {"workload": f"{args.config} wave tank, dx={spec.dx} m, {scen.n_fluid} fluid particles, "
+                                   f"the reference's {args.ref_solver} PPE to rel-res 1e-8, dt={spec.dt} s",
+                       "fluid_particles": scen.n_fluid},
+            "ppe": {"iterations": iters},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+                             "sample": desc},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -515,6 +708,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=("ours", "reference"))
     ap.add_argument("--config", default=CONFIG)
     ap.add_argument("--solver", default="bicgstab", choices=("bicgstab", "fgmres"))
+    ap.add_argument("--ref-solver", default="bicgstab", choices=("bicgstab", "fgmres"),
+                    help="the reference arm's PPE solver (FGMRES restarts at 30)")
     ap.add_argument("--inner-tol", type=float, default=None,
                     help="mixed path: relative tolerance of each FP32 inner solve (default 1e-5 with the "
                          "multigrid preconditioner, 0.1 for the BiCGSTAB sweeps without it)")
@@ -523,44 +718,37 @@ def main():
     ap.add_argument("--restart", type=int, default=40)
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-steps", type=int, default=2,
+                    help="timed oracle steps of the cpu_baseline sample (after one untimed step)")
     ap.add_argument("--no-wcsph", action="store_true", help="skip the WCSPH forward/adjoint workload (c4)")
     ap.add_argument("--no-salinity", action="store_true", help="skip the salinity-transport step measurement")
     ap.add_argument("--no-reference-tank", action="store_true", help="skip the reference's own tank")
-    ap.add_argument("--cpu-iters", type=float, default=1350.0,
-                    help="PPE iterations per step the reference arm's sample is scaled to")
+    ap.add_argument("--long", type=int, default=0, help="record N steps of both paths (see the module doc)")
+    ap.add_argument("--profile-case", action="store_true", help="a bounded run for a profiler (see profile_case)")
+    ap.add_argument("--precision", default="mixed", choices=("mixed", "fp64"), help="--profile-case path")
+    ap.add_argument("--maxit", type=int, default=10, help="--profile-case: Krylov iterations per solve")
+    ap.add_argument("--wcsph", type=int, default=0, help="--profile-case: WCSPH forward + adjoint steps")
+    ap.add_argument("--every", type=int, default=10, help="--profile-case: WCSPH checkpoint interval")
+    ap.add_argument("--salinity", action="store_true", help="--profile-case: the phase-3 step with salinity")
     args = ap.parse_args()
     if args.inner_tol is None:
         args.inner_tol = 1e-5 if args.precond == "mg" else 0.1
+    if args.profile_case:
+        profile_case(args)
+        return
+    if args.long:
+        run_long(args)
+        return
     dist = Dist()
     from beach_slope_confined_gb300 import scenario as sc
 
     threads = os.cpu_count() or 1
     if args.impl == "reference":
-        if dist.rank == 0:
-            spec = sc.config_spec(args.config)
-            scen = sc.build(spec)
-            vals = []
-            for _ in range(args.warmup):
-                pass  # the sample has no warm state to build
-            for _ in range(max(1, args.steps)):
-                v, desc, t_step = cpu_sample(scen, spec, threads, args.cpu_iters, args.solver)
-                vals.append(v)
-            value = statistics.median(vals)
-            line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "particle-steps/s",
-                    "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                    "ms_per_step": 1e3 * scen.n_fluid / value, "higher_is_better": True, "scaling": "weak",
-                    "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded wave tank)",
-                    "config": {"workload": f"{args.config} wave tank, dx={spec.dx} m, {scen.n_fluid} fluid "
-                                           f"particles, BiCGSTAB to 1e-8"},
-                    "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
-                                     "kind": "port", "sample": desc},
-                    "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
-                            "d2h_bytes_per_step": 0}}
-            print(json.dumps(line), flush=True)
+        run_reference_arm(args, dist, threads)
         dist.close()
         return
 
-    scen, res, errs, peaks, ref_iters = run_ours(args, dist)
+    scen, res, errs, peaks = run_ours(args, dist)
     if dist.rank != 0:
         dist.close()
         return
@@ -577,12 +765,27 @@ def main():
         kname = "k_bicg_1<EllOp<float>,float> (FP32 ELL SpMV + dot)"
         tpr = traffic_per_row("fp32")
     achieved = byts / (m["spmv_ms"] * 1e-3) / 1e9 if m["spmv_ms"] > 0 else None
-    roofline = {"bound": "hbm", "kernel": kname,
-                "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                "frac": (achieved / hbm) if achieved else None,
-                "traffic": (tpr * m["n"]) if tpr else None,
-                "algorithmic_bytes_per_launch": byts, "avg_launch_ms": m["spmv_ms"],
-                "launches_timed": m["spmv_calls"], "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs"}
+    spmv_roof = {"bound": "hbm", "kernel": kname,
+                 "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                 "frac": (achieved / hbm) if achieved else None,
+                 "traffic": (tpr * m["n"]) if tpr else None,
+                 "algorithmic_bytes_per_launch": byts, "avg_launch_ms": m["spmv_ms"],
+                 "launches_timed": m["spmv_calls"], "ms_per_step": m["spmv_ms"] * m["spmv_calls"] / args.steps,
+                 "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs"}
+    # the roofline of the timed kernel with the largest share of the step:
+    # one of the FP64-pipe-bound pair kernels (against the measured FP64 FMA
+    # rate), or the SpMV (against the measured HBM copy bandwidth)
+    top = max(m["kernels"], key=lambda k: k["ms_per_step"]) if m["kernels"] else None
+    if top and top["ms_per_step"] > spmv_roof["ms_per_step"]:
+        roofline = {"bound": "fp64", "kernel": top["kernel"] + " (mixed path)", "achieved": top["achieved_gflops"],
+                    "peak": top["peak_gflops"], "unit": "GFLOP/s", "frac": top["frac"],
+                    "traffic": kernel_traffic(top["kernel"], "mixed", m["n"]),
+                    "algorithmic_fp64_flops_per_launch": top["fp64_flops_per_launch"],
+                    "avg_launch_ms": top["ms_per_launch"], "launches_per_step": top["launches_per_step"],
+                    "share_of_step": top["ms_per_step"] / m["ms_per_step"],
+                    "peak_source": "FP64 FMA rate measured by bsc_measure_peaks on this GPU (2 flops per FMA)"}
+    else:
+        roofline = spmv_roof
     fp64 = None
     if "fp64" in res:
         f = res["fp64"]
@@ -590,24 +793,18 @@ def main():
         a64 = b64 / (f["spmv_ms"] * 1e-3) / 1e9 if f["spmv_ms"] > 0 else None
         t64 = traffic_per_row("spmv_z_fp64" if mg else "fp64")
         fp64 = {"value": f["value"], "ms_per_step": f["ms_per_step"], "ppe_iterations": [i[0] for i in f["iters"]],
-                "solve_ms_per_step": f["solve_ms"],
-                "roofline": {"bound": "hbm",
-                             "kernel": "k_spmv_z<double>" if mg else "k_bicg_1<EllOp<double>,double>",
-                             "achieved": a64,
-                             "peak": hbm, "unit": "GB/s", "frac": (a64 / hbm) if a64 else None,
-                             "traffic": (t64 * f["n"]) if t64 else None}}
+                "solve_ms_per_step": f["solve_ms"], "kernels": f["kernels"],
+                "roofline_spmv": {"bound": "hbm",
+                                  "kernel": "k_spmv_z<double>" if mg else "k_bicg_1<EllOp<double>,double>",
+                                  "achieved": a64,
+                                  "peak": hbm, "unit": "GB/s", "frac": (a64 / hbm) if a64 else None,
+                                  "traffic": (t64 * f["n"]) if t64 else None}}
     wc = None if args.no_wcsph else run_wcsph()
     sal = None if args.no_salinity else run_salinity(args)
     rtank = None if args.no_reference_tank else run_reference_tank(args, threads)
     cpu = None
     if not args.no_cpu:
-        if ref_iters:
-            gpu_iters = float(ref_iters)
-        elif "fp64" in res and not mg:
-            gpu_iters = statistics.mean(i[0] for i in res["fp64"]["iters"])
-        else:
-            gpu_iters = args.cpu_iters
-        v, desc, _ = cpu_sample(scen, spec, threads, gpu_iters, "bicgstab")
+        v, desc, _ = cpu_steps(scen, spec, threads, args.cpu_steps, 1)
         cpu = {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port", "sample": desc}
     solver_desc = f"FGMRES({args.restart}) + cell-multigrid V-cycle" if mg else args.solver
     line = {
@@ -617,7 +814,7 @@ def main():
         "data": "synthetic (seeded wave tank, no dataset)",
         "config": {"workload": f"{args.config} wave tank 4.0x0.6 m, depth 0.30 m, dx={spec.dx} m, "
                                f"{scen.n_fluid} fluid + {scen.n - scen.n_fluid} wall particles, Wendland C2 h=1.3dx, "
-                               f"{solver_desc} PPE to rel-res 1e-8, dt={spec.dt} s",
+                               f"piston from t=0, {solver_desc} PPE to rel-res 1e-8, dt={spec.dt} s",
                    "fluid_particles": scen.n_fluid, "precond": args.precond,
                    "precision": ("mixed (FP32 pair sums and V-cycle, FP64 assembly and FGMRES)" if mg
                                  else "mixed (FP32 sweeps, FP64 refinement)"),
@@ -626,8 +823,11 @@ def main():
         "ppe": {"iterations": [i[0] for i in m["iters"]], "refinement_sweeps": [i[1] for i in m["iters"]],
                 "rel_residual": [i[2] for i in m["iters"]]},
         "fp64": fp64,
+        "mixed_over_fp64_speed": (fp64["ms_per_step"] / m["ms_per_step"]) if fp64 else None,
         "mixed_vs_fp64_rel_l2": errs,
         "roofline": roofline,
+        "roofline_spmv": spmv_roof,
+        "kernels": m["kernels"],
         "cpu_baseline": cpu,
         "e2e": m.get("e2e"),
         "clocks": m["clocks"],

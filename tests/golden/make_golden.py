@@ -40,7 +40,9 @@ def parse(src: str):
 
 
 if __name__ == "__main__":
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/reference")
+    ref = sys.argv[1]
     with open(os.path.join(ref, "solvertest.f90")) as fh:
         data = parse(fh.read())
     out = os.path.join(os.path.dirname(os.path.abspath(__file__)), "solvertest_kat.json")
