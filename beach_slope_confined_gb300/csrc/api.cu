@@ -85,6 +85,7 @@ static void derive_kparams(Ctx* c) {
     K.w0 = (P.kernel == BSC_KERNEL_WENDLAND_C2) ? K.wend_W : 4.0 * K.hyb_A + 6.0 * K.hyb_B;
     K.inv_w0 = 1.0 / K.w0;
     K.inv_h = 1.0 / h;
+    K.half_inv_h = 0.5 * K.inv_h;
     K.hyb_n1 = (9.0 * K.hyb_A + 3.0 * K.hyb_B) / (h * h * h);  // r < h: n1 r - n0 - n2/(r h)
     K.hyb_n0 = 12.0 * K.hyb_A / (h * h);
     K.hyb_n2 = 6.0 * K.hyb_B;

@@ -109,11 +109,23 @@ __device__ __forceinline__ double rcp_nr(double x) {
 //   r0 = x y0, h0 = y0 / 2, e = 1/2 - r0 h0, r = r0 + r0 e.
 // The relative error is about 3/2 e0^2 for a seed error e0 (~2^-22): within
 // 2^-42.  Four FP64 operations.
+// Three FP64 operations: h0 = y0 / 2 is formed in FP32 (exact there) and
+// widened on the integer pipe like y0.
 __device__ __forceinline__ double sqrt_nr(double x) {
-    const double y0 = f64_of(rsqrtf(f32_of(x)));
-    const double r0 = x * y0, h0 = 0.5 * y0;
+    const float yf = rsqrtf(f32_of(x));
+    const double y0 = f64_of(yf), h0 = f64_of(0.5f * yf);
+    const double r0 = x * y0;
     const double e = fma(-r0, h0, 0.5);
     return fma(r0, e, r0);
+}
+
+// a < b for non-negative doubles a and b (b finite), on the integer pipe:
+// the bit patterns of non-negative IEEE doubles order like their values, and
+// any a with the sign bit set (only a NaN can have it here) compares as not
+// below.  The pair searches take their exact d^2 < T test this way, off the
+// FP64 pipe that bounds them.
+__device__ __forceinline__ bool nonneg_below(double a, double b) {
+    return (unsigned long long)__double_as_longlong(a) < (unsigned long long)__double_as_longlong(b);
 }
 
 // an FGMRES cycle has stopped (converged, broken down or at its restart
@@ -131,7 +143,7 @@ struct KParams {
     double bxmin, bxmax;
     // kernel coefficients: grad_i W = F(r) (x_i - x_j)
     double hyb_A, hyb_B, wend_F, wend_W, w0, inv_w0;
-    double inv_h, hyb_n0, hyb_n1, hyb_n2, hyb_f;  // folded hybrid-gradient constants
+    double inv_h, half_inv_h, hyb_n0, hyb_n1, hyb_n2, hyb_f;  // 1/h, 1/(2h), folded hybrid-gradient constants
     // cell grid
     double gx0, gy0, cs;
     int nx, ny;

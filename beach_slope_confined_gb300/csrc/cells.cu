@@ -282,20 +282,26 @@ __global__ void k_piston(int64_t n, State S, double xp, double vp) {
     }
 }
 
+// x_p(t) = s0 + r(t) (s(t) - s0) with s(t) = sum_k a_k sin(w_k t + phi_k),
+// s0 = s(0) and the ramp r(t) = (1 - cos(pi t / ramp)) / 2 (1 after it): the
+// ramp takes the stroke from its starting value, so a stroke whose phases
+// put it away from zero at t = 0 starts at rest too (the wall's rest
+// coordinate carries -s0)
 int op_piston(Ctx* c) {
     const bsc_params& P = c->P;
-    double s = 0, ds = 0;
+    double s = 0, ds = 0, s0 = 0;
     for (int k = 0; k < P.piston_modes && k < BSC_MAX_PISTON_MODES; ++k) {
         double w = 2.0 * M_PI / P.piston_period[k];
         s += P.piston_amp[k] * std::sin(w * c->t + P.piston_phase[k]);
         ds += P.piston_amp[k] * w * std::cos(w * c->t + P.piston_phase[k]);
+        s0 += P.piston_amp[k] * std::sin(P.piston_phase[k]);
     }
     double r = 1.0, dr = 0.0;
     if (P.piston_ramp > 0.0 && c->t < P.piston_ramp) {
         r = 0.5 * (1.0 - std::cos(M_PI * c->t / P.piston_ramp));
         dr = 0.5 * M_PI / P.piston_ramp * std::sin(M_PI * c->t / P.piston_ramp);
     }
-    k_piston<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, r * s, dr * s + r * ds);
+    k_piston<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, s0 + r * (s - s0), dr * (s - s0) + r * ds);
     BSC_LAUNCH(c);
     return BSC_OK;
 }

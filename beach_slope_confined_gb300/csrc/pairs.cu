@@ -84,11 +84,13 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
     auto pair = [&](int j) {
         const double dx = xi - S.x[j], dy = yi - S.y[j];
         const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-        if (!(d2 < K.H2x)) return;  // exactly sqrt(d2) < 2h, no FMA contraction
+        // exactly sqrt(d2) < 2h, no FMA contraction; the comparison on the
+        // integer pipe (d2 >= 0)
+        if (!nonneg_below(d2, K.H2x)) return;
         // the mixed path's root by Newton from an FP32 seed (within 2^-42;
         // the FP64 pipe is this kernel's bound), the FP64 path's correctly
         // rounded
-        const double r = sizeof(R) == 4 ? (d2 > 0.0 ? sqrt_nr(d2) : 0.0) : __dsqrt_rn(d2);
+        const double r = sizeof(R) == 4 ? (__double_as_longlong(d2) != 0 ? sqrt_nr(d2) : 0.0) : __dsqrt_rn(d2);
         // grad W per pair in FP64 (stored in FP64, and in FP32 for the FP32
         // pair sums of the mixed path); the M sum runs in R
         const double F = grad_factor<double>(K, r);
@@ -254,38 +256,83 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
     const bool pre_i = pre_ok(pi, csf);
     R frac = 0;
     double fsum = 0.0;  // mixed path: the FP64 sum of FP32 terms
-    for (int ax = cx - 1; ax <= cx + 1; ++ax) {
-        if (ax < 0 || ax >= K.nx) continue;
-        const float shx = (float)(ax - cx) * csf;
-        for (int ay = cy - 1; ay <= cy + 1; ++ay) {
-            if (ay < 0 || ay >= K.ny) continue;
-            const float shy = (float)(ay - cy) * csf;
-            const int cc = ax * K.ny + ay;
-            const int s0 = scs[cc], s1 = s0 + scc[cc];
-            for (int s = s0; s < s1; ++s) {
-                const float2 ps = sposf[s];
-                if (pre_i && pre_ok(ps, csf)) {
-                    const float fdx = pi.x - (ps.x + shx), fdy = pi.y - (ps.y + shy);
-                    const float r2f = fdx * fdx + fdy * fdy;
-                    if (r2f > H2f) continue;
-                    if constexpr (sizeof(R) == 4) {
-                        // Mixed path: each term in FP32 (W is continuous and
-                        // vanishes at r = 2h, so the FP32 distance decides
-                        // nothing that matters; weight (1-n_s) V_s), the sum
-                        // in FP64. The FP32 running sum was the main error
-                        // of the mixed velocities (1.1e-6 against FP64 after
-                        // the benchmark's steps; 6.7e-7 with this sum, for
-                        // one FP64 add per term).
-                        if (r2f < (float)K.H2) fsum += f64_of(swf[s] * kern_w<float>(K, sqrtf(r2f)));
-                        continue;
+    // the FP64 work of one solid: the exact test and its weighted W
+    auto solid_term = [&](int s) {
+        const double dx = xi - sx[s], dy = yi - sy[s];
+        const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
+        if (!nonneg_below(d2, K.H2x)) return;  // exactly sqrt(d2) < 2h
+        // W(r) in R: an FP32 root for the FP32 sum, the exact one for FP64
+        const R r = sizeof(R) == 4 ? (R)sqrtf((float)d2) : (R)__dsqrt_rn(d2);
+        frac += ((R)1 - (R)spor[s]) * kern_w<R>(K, r) * (R)svol[s];
+    };
+    // FP64 path, two phases as in the neighbour search: the FP32 pre-test
+    // first compacts the surviving solids (in cell order) into this thread's
+    // column of shared memory, then the FP64 terms run over them on full
+    // warps.  In one pass the FP64 work sat inside the divergent candidate
+    // loop, at about half the lanes of each FP64 instruction.  The sum keeps
+    // its order, so the result is the same.  A particle with more survivors
+    // than the column holds, or far from its binned cell, takes the one pass.
+    constexpr int EP_CAP = 32;
+    __shared__ int32_t cand[sizeof(R) == 8 ? EP_CAP * NB_BLOCK : 1];
+    bool one_pass = true;
+    if constexpr (sizeof(R) == 8) {
+        if (pre_i) {
+            int nc = 0;
+            for (int ax = cx - 1; ax <= cx + 1; ++ax) {
+                if (ax < 0 || ax >= K.nx) continue;
+                const float shx = (float)(ax - cx) * csf;
+                for (int ay = cy - 1; ay <= cy + 1; ++ay) {
+                    if (ay < 0 || ay >= K.ny) continue;
+                    const float shy = (float)(ay - cy) * csf;
+                    const int cc = ax * K.ny + ay;
+                    const int s0 = scs[cc], s1 = s0 + scc[cc];
+                    for (int s = s0; s < s1; ++s) {
+                        const float2 ps = sposf[s];
+                        if (pre_ok(ps, csf)) {
+                            const float fdx = pi.x - (ps.x + shx), fdy = pi.y - (ps.y + shy);
+                            if (fdx * fdx + fdy * fdy > H2f) continue;
+                        }
+                        if (nc < EP_CAP) cand[nc * NB_BLOCK + threadIdx.x] = s;
+                        ++nc;
                     }
                 }
-                const double dx = xi - sx[s], dy = yi - sy[s];
-                const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
-                if (!(d2 < K.H2x)) continue;  // exactly sqrt(d2) < 2h
-                // W(r) in R: an FP32 root for the FP32 sum, the exact one for FP64
-                const R r = sizeof(R) == 4 ? (R)sqrtf((float)d2) : (R)__dsqrt_rn(d2);
-                frac += ((R)1 - (R)spor[s]) * kern_w<R>(K, r) * (R)svol[s];
+            }
+            if (nc <= EP_CAP) {
+                one_pass = false;
+                for (int k = 0; k < nc; ++k) solid_term(cand[k * NB_BLOCK + threadIdx.x]);
+            }
+        }
+    }
+    if (one_pass) {
+        for (int ax = cx - 1; ax <= cx + 1; ++ax) {
+            if (ax < 0 || ax >= K.nx) continue;
+            const float shx = (float)(ax - cx) * csf;
+            for (int ay = cy - 1; ay <= cy + 1; ++ay) {
+                if (ay < 0 || ay >= K.ny) continue;
+                const float shy = (float)(ay - cy) * csf;
+                const int cc = ax * K.ny + ay;
+                const int s0 = scs[cc], s1 = s0 + scc[cc];
+                for (int s = s0; s < s1; ++s) {
+                    const float2 ps = sposf[s];
+                    if (pre_i && pre_ok(ps, csf)) {
+                        const float fdx = pi.x - (ps.x + shx), fdy = pi.y - (ps.y + shy);
+                        const float r2f = fdx * fdx + fdy * fdy;
+                        if (r2f > H2f) continue;
+                        if constexpr (sizeof(R) == 4) {
+                            // Mixed path: each term in FP32 (W is continuous
+                            // and vanishes at r = 2h, so the FP32 distance
+                            // decides nothing that matters; weight
+                            // (1-n_s) V_s), the sum in FP64. The FP32 running
+                            // sum was the main error of the mixed velocities
+                            // (1.1e-6 against FP64 after the benchmark's
+                            // steps; 6.7e-7 with this sum, for one FP64 add
+                            // per term).
+                            if (r2f < (float)K.H2) fsum += f64_of(swf[s] * kern_w<float>(K, sqrtf(r2f)));
+                            continue;
+                        }
+                    }
+                    solid_term(s);
+                }
             }
         }
     }

@@ -15,11 +15,12 @@ namespace bsc {
 //   F = -35/(4*3.14 h^4) (1 - r/(2h))^3.
 template <typename R>
 __device__ __forceinline__ R grad_factor(const KParams& K, R r) {
-    const R q = r * (R)K.inv_h;
     if (K.kernel == BSC_KERNEL_WENDLAND_C2) {
-        R a = (R)1 - (R)0.5 * q;
-        return -(R)K.wend_F * (a * a * a);
+        // a = 1 - r/(2h) in one FMA; -F a^3 as (-F a) a^2: four operations
+        const R a = fma(-r, (R)K.half_inv_h, (R)1);
+        return (-(R)K.wend_F * a) * (a * a);
     }
+    const R q = r * (R)K.inv_h;
     // A (9r/h^3 - 12/h^2) + B (3r/h^3 - 6/(rh)) = (9A+3B) r/h^3 - 12A/h^2 - 6B/(rh)
     const R inv_rh = (R)K.inv_h / r;
     if (q < (R)1) return (R)K.hyb_n1 * r - (R)K.hyb_n0 - (R)K.hyb_n2 * inv_rh;

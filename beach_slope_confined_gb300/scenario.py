@@ -169,18 +169,22 @@ class Scenario:
 
 
 def piston_stroke(spec: TankSpec, t: float):
-    """x_p(t) and v_p(t) of the wavemaker: r(t) * sum_k a_k sin(w_k t + phi_k)
-    with the start-up ramp r(t) = (1 - cos(pi t / ramp)) / 2 for t < ramp."""
-    s = ds = 0.0
+    """x_p(t) and v_p(t) of the wavemaker: s0 + r(t) (s(t) - s0), with
+    s(t) = sum_k a_k sin(w_k t + phi_k), s0 = s(0) and the start-up ramp
+    r(t) = (1 - cos(pi t / ramp)) / 2 for t < ramp (1 after it, or without a
+    ramp).  The ramp takes the stroke from its starting value, so the wall
+    starts at rest."""
+    s = ds = s0 = 0.0
     for a, T, ph in zip(spec.piston_amp, spec.piston_period, spec.piston_phase):
         w = 2.0 * math.pi / T
         s += a * math.sin(w * t + ph)
         ds += a * w * math.cos(w * t + ph)
+        s0 += a * math.sin(ph)
     r, dr = 1.0, 0.0
     if spec.piston_ramp > 0.0 and t < spec.piston_ramp:
         r = 0.5 * (1.0 - math.cos(math.pi * t / spec.piston_ramp))
         dr = 0.5 * math.pi / spec.piston_ramp * math.sin(math.pi * t / spec.piston_ramp)
-    return r * s, dr * s + r * ds
+    return s0 + r * (s - s0), dr * (s - s0) + r * ds
 
 
 def kernel_w(spec: TankSpec, r: np.ndarray) -> np.ndarray:
@@ -242,9 +246,9 @@ def build(spec: TankSpec) -> Scenario:
     ny = int(math.floor(spec.depth / dx + 1e-9))
     nyw = int(math.floor(spec.height / dx + 1e-9))
     stroke = sum(abs(a) for a in spec.piston_amp)
-    # Without a ramp a stroke with nonzero phases starts away from zero; the
-    # piston's rest coordinate is then shifted by -x_p(0), so the wall starts
-    # on its lattice next to the fluid and moves by x_p(t) - x_p(0).
+    # A stroke with nonzero phases starts away from zero; the piston's rest
+    # coordinate is shifted by -x_p(0), so the wall starts on its lattice next
+    # to the fluid and moves by x_p(t) - x_p(0).
     xp_start = piston_stroke(spec, 0.0)[0]
 
     # ---- fluid lattice with seeded jitter (column-major: x outer, y inner)

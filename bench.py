@@ -297,7 +297,7 @@ def run_ours(args, dist: Dist):
     scen = sc.build(spec)
     nf = scen.n_fluid
     results = {}
-    states = {}
+    states, times = {}, {}
     peaks = measure_peaks()
     spairs = solid_pairs(scen)
     for prec in ("mixed", "fp64"):
@@ -332,6 +332,7 @@ def run_ours(args, dist: Dist):
                              clocks=clk.summary(), n=scen.n,
                              kernels=kernel_rooflines(t, args.steps, nnz, spairs, prec, peaks[0]))
         states[prec] = g.download_state()
+        times[prec] = g.get_time()
         # e2e through the C ABI with host buffers in pinned memory: every
         # step uploads the state, steps, and downloads the state
         if prec == "mixed":
@@ -358,8 +359,41 @@ def run_ours(args, dist: Dist):
         g.close()
     errs = None
     if "fp64" in states:
-        errs = field_errors(states["mixed"], states["fp64"])
+        errs = {"after_run": field_errors(states["mixed"], states["fp64"]),
+                "one_step": one_step_errors(args, spec, scen, states["fp64"], times["fp64"])}
     return scen, results, errs, peaks
+
+
+def one_step_errors(args, spec, scen, start, tdt):
+    """One mixed step against one FP64 step from the same state (the FP64
+    arm's state after its timed steps): the mixed path's error per step,
+    which the runs' difference after many steps does not show (the tank's
+    flow amplifies any perturbation, the FP64 path's own roundoff included,
+    by about e every 100 steps)."""
+    from beach_slope_confined_gb300 import Solver, setup_tank
+
+    out = {}
+    for prec in ("fp64", "mixed"):
+        P = sc_params(args, spec, scen, prec)
+        h = Solver(P)
+        setup_tank(h, scen)
+        h.upload_state(start)
+        h.set_time(*tdt)
+        h.effpor()
+        h.step(1)
+        out[prec] = h.download_state()
+        h.close()
+    e = field_errors(out["mixed"], out["fp64"])
+    e["xy_per_spacing"] = float(np.max(np.hypot(out["mixed"]["x"] - out["fp64"]["x"],
+                                                out["mixed"]["y"] - out["fp64"]["y"])) / spec.dx)
+    return e
+
+
+def sc_params(args, spec, scen, prec):
+    from beach_slope_confined_gb300 import scenario as sc
+
+    return sc.make_params(spec, scen.bounds, precision=prec, solver=args.solver, tol=1e-8, maxit=40000,
+                          inner_tol=args.inner_tol, max_outer=60, precond=args.precond, restart=args.restart)
 
 
 ERROR_FIELDS = ("x", "y", "vx", "vy", "p", "rho", "porosity", "nut", "tke", "vel", "gradvx", "resist", "varts")
@@ -377,6 +411,11 @@ def field_errors(a, b):
             u, v = a[f], b[f]
         nv = np.linalg.norm(v)
         out[f] = float(np.linalg.norm(u - v) / nv) if nv > 0 else float(np.linalg.norm(u - v))
+    # particles the two runs classify differently at the free surface (the
+    # test tr M <= 1.6 of search.f90:300-306): each one switches its pressure
+    # row, shift factor and artificial viscosity, and moves the fields far
+    # more than the arithmetic does
+    out["free_flag_mismatches"] = int(((a["flags"] ^ b["flags"]) & 1).sum())
     return out
 
 
@@ -475,6 +514,125 @@ def run_wcsph(reps: int = 2):
             "misfit": J0, "gradient_alpha_beta": [float(grad[0]), float(grad[1])],
             "gradient_porosity_grid_norm": float(np.linalg.norm(grad[2:])),
             "finite_differences": fd}
+
+
+def wcsph_check(args):
+    """`--wcsph-check`: the c4 gradient checks.
+
+    For the c4 case as configured (and, with `--wcsph-ramp R`, with the
+    piston ramp set to R seconds): the misfit J of the squared probe
+    elevations against the target run (alpha=260, beta=0.9, porosity 0.45),
+    the adjoint gradient, and
+      * central differences of alpha and beta at relative steps 1e-1 ..
+        1e-7 (two-point) and at 3e-2 (four-point): where the differences
+        agree with the adjoint, and where roundoff takes over;
+      * central differences for every porosity cell whose adjoint gradient
+        is nonzero, at the relative step of the plateau and at 1e-6;
+      * the oracle's FP64 adjoint (scatter form, every state kept) over the
+        first `--wcsph-oracle-steps` steps of the same case, against the
+        CUDA adjoint of the same shortened run.
+    One JSON line."""
+    from beach_slope_confined_gb300 import Solver, scenario as sc, setup_tank
+
+    spec = sc.config_spec("c4")
+    if args.wcsph_ramp is not None:
+        spec.piston_ramp = args.wcsph_ramp
+    scen = sc.build(spec)
+    nsteps, every = 500, 50
+    g = Solver(sc.make_params(spec, scen.bounds, precision="fp64"))
+    setup_tank(g, scen)
+    wp, grid0 = sc.wcsph_params(spec, scen)
+    g.wcsph_setup(wp)
+    g.wcsph_set_params(260.0, 0.9, np.full_like(grid0, 0.45))
+    eta_hat = g.wcsph_forward(nsteps, every)
+    a0, b0 = spec.darcy_alpha, spec.forch_beta
+
+    def misfit(a, b, grid):
+        g.wcsph_set_params(a, b, grid)
+        eta = g.wcsph_forward(nsteps, every)
+        return float(np.sum((eta - eta_hat) ** 2)), eta
+
+    J0, eta = misfit(a0, b0, grid0)
+    dJ = 2.0 * (eta - eta_hat)
+    grad = g.wcsph_adjoint(dJ)
+    out = {"mode": "wcsph-check", "piston_ramp": spec.piston_ramp, "steps": nsteps, "misfit": J0,
+           "eta_rms": float(np.sqrt(np.mean(eta ** 2))), "eta_diff_rms": float(np.sqrt(np.mean((eta - eta_hat) ** 2))),
+           "gradient_alpha_beta": [float(grad[0]), float(grad[1])]}
+
+    def fd_param(k, rs, pts=2):
+        base = (a0, b0)[k]
+        h = rs * base
+        J = {}
+        for m in ((-2, -1, 1, 2) if pts == 4 else (-1, 1)):
+            J[m] = misfit(a0 + m * h, b0, grid0)[0] if k == 0 else misfit(a0, b0 + m * h, grid0)[0]
+        if pts == 4:
+            return (8.0 * (J[1] - J[-1]) - (J[2] - J[-2])) / (12.0 * h)
+        return (J[1] - J[-1]) / (2.0 * h)
+
+    sweep = {}
+    for rs in (1e-1, 3e-2, 1e-2, 3e-3, 1e-3, 1e-4, 1e-5, 1e-6, 1e-7):
+        row = {}
+        for k, name in enumerate(("alpha", "beta")):
+            d = fd_param(k, rs)
+            row[name] = abs(float(grad[k]) - d) / abs(d) if d != 0 else None
+        sweep[f"{rs:g}"] = row
+    out["alpha_beta_sweep_rel_diff"] = sweep
+    four = {}
+    for k, name in enumerate(("alpha", "beta")):
+        d = fd_param(k, 3e-2, 4)
+        four[name] = abs(float(grad[k]) - d) / abs(d) if d != 0 else None
+    out["alpha_beta_4pt_3e-2_rel_diff"] = four
+    # the plateau: the relative step whose worse alpha/beta difference is smallest
+    plateau = min(sweep, key=lambda r: max(v for v in sweep[r].values() if v is not None))
+    out["plateau_step"] = float(plateau)
+    gp = grad[2:].reshape(grid0.shape)
+    cells = [tuple(ix) for ix in np.argwhere(np.abs(gp) > 0)]
+    por = {}
+    for rs in (float(plateau), 1e-6):
+        diffs = []
+        for (iy, ix) in cells:
+            h = rs * grid0[iy, ix]
+            gm, gpl = grid0.copy(), grid0.copy()
+            gm[iy, ix] -= h
+            gpl[iy, ix] += h
+            d = (misfit(a0, b0, gpl)[0] - misfit(a0, b0, gm)[0]) / (2.0 * h)
+            diffs.append(abs(float(gp[iy, ix]) - d) / abs(d) if d != 0 else float("inf"))
+        diffs = np.asarray(diffs)
+        por[f"{rs:g}"] = {"cells": len(cells), "max_rel_diff": float(diffs.max()) if diffs.size else None,
+                          "median_rel_diff": float(np.median(diffs)) if diffs.size else None,
+                          "cells_within_1e-4": int((diffs < 1e-4).sum())}
+    out["porosity_cells"] = por
+    out["porosity_gradient_norm"] = float(np.linalg.norm(gp))
+    g.close()
+    # the oracle's FP64 adjoint on the first steps of the same case
+    ns = args.wcsph_oracle_steps
+    if ns > 0:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        oracle.set_threads(os.cpu_count() or 1)
+        res = {}
+        for side in ("cuda", "oracle"):
+            P = sc.make_params(spec, scen.bounds, precision="fp64")
+            h = Solver(P) if side == "cuda" else oracle.context(P)
+            setup_tank(h, scen)
+            h.wcsph_setup(wp)
+            h.wcsph_set_params(260.0, 0.9, np.full_like(grid0, 0.45))
+            target = h.wcsph_forward(ns, every if side == "cuda" else ns)
+            h.wcsph_set_params(a0, b0, grid0)
+            t0 = time.perf_counter()
+            e = h.wcsph_forward(ns, every if side == "cuda" else ns)
+            gr = h.wcsph_adjoint(2.0 * (e - target))
+            res[side] = (e, gr, time.perf_counter() - t0)
+            h.close()
+        (ec, gc, tc), (eo, go, to) = res["cuda"], res["oracle"]
+        out["oracle_comparison"] = {
+            "steps": ns, "eta_max_rel_diff": float(np.max(np.abs(ec - eo)) / np.max(np.abs(eo))),
+            "alpha_rel_diff": abs(float(gc[0] - go[0])) / abs(float(go[0])),
+            "beta_rel_diff": abs(float(gc[1] - go[1])) / abs(float(go[1])),
+            "porosity_grid_rel_diff": float(np.linalg.norm(gc[2:] - go[2:]) / np.linalg.norm(go[2:])),
+            "cuda_s": tc, "oracle_s": to, "oracle_threads": os.cpu_count() or 1}
+    print(json.dumps(out), flush=True)
 
 
 def run_salinity(args):
@@ -730,6 +888,10 @@ def main():
     ap.add_argument("--wcsph", type=int, default=0, help="--profile-case: WCSPH forward + adjoint steps")
     ap.add_argument("--every", type=int, default=10, help="--profile-case: WCSPH checkpoint interval")
     ap.add_argument("--salinity", action="store_true", help="--profile-case: the phase-3 step with salinity")
+    ap.add_argument("--wcsph-check", action="store_true", help="the c4 gradient checks (see wcsph_check)")
+    ap.add_argument("--wcsph-ramp", type=float, default=None, help="--wcsph-check: the piston ramp (s)")
+    ap.add_argument("--wcsph-oracle-steps", type=int, default=20,
+                    help="--wcsph-check: steps of the CUDA-vs-oracle adjoint comparison (0: skip)")
     args = ap.parse_args()
     if args.inner_tol is None:
         args.inner_tol = 1e-5 if args.precond == "mg" else 0.1
@@ -738,6 +900,9 @@ def main():
         return
     if args.long:
         run_long(args)
+        return
+    if args.wcsph_check:
+        wcsph_check(args)
         return
     dist = Dist()
     from beach_slope_confined_gb300 import scenario as sc

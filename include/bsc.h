@@ -112,12 +112,13 @@ typedef struct bsc_params {
     double  inner_tol;           /* mixed: FP32 inner solve relative tolerance     */
     int32_t max_neighbors;       /* neighbour-list capacity per particle           */
     int32_t reorder_every;       /* Morton reorder of the state every n cellshifts */
-    int32_t piston_modes;        /* piston x_p(t) = sum a_k sin(2 pi t/T_k + phi_k)*/
+    int32_t piston_modes;        /* stroke s(t) = sum a_k sin(2 pi t/T_k + phi_k)  */
     int32_t precond;             /* BSC_PRECOND_* for the PPE solve                */
     double  piston_amp[BSC_MAX_PISTON_MODES];
     double  piston_period[BSC_MAX_PISTON_MODES];
     double  piston_phase[BSC_MAX_PISTON_MODES];
-    double  piston_ramp;         /* stroke scaled by (1-cos(pi t/ramp))/2 for t<ramp */
+    double  piston_ramp;         /* x_p = s0 + r (s - s0), s0 = x_p(0), with       */
+                                 /* r = (1-cos(pi t/ramp))/2 for t < ramp, else 1  */
     double  xmin, xmax, ymin, ymax; /* cell-grid bounds; all 0 = derive at upload */
     /* cell-aggregation multigrid (BSC_PRECOND_MG) */
     double  mg_omega;            /* smoother weight; with 2 sweeps the 2nd uses    *

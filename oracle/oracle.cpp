@@ -471,20 +471,23 @@ int fgmres(const bsc_params& P, const std::vector<int64_t>& rp, const std::vecto
     return info->status;
 }
 
+// x_p(t) = s0 + r(t) (s(t) - s0), s0 = s(0): the ramp takes the stroke from
+// its starting value
 double piston_x(const bsc_params& P, double tt, double* vel) {
-    double s = 0, ds = 0;
+    double s = 0, ds = 0, s0 = 0;
     for (int k = 0; k < P.piston_modes && k < BSC_MAX_PISTON_MODES; ++k) {
         double w = 2.0 * M_PI / P.piston_period[k];
         s += P.piston_amp[k] * std::sin(w * tt + P.piston_phase[k]);
         ds += P.piston_amp[k] * w * std::cos(w * tt + P.piston_phase[k]);
+        s0 += P.piston_amp[k] * std::sin(P.piston_phase[k]);
     }
     double r = 1.0, dr = 0.0;
     if (P.piston_ramp > 0.0 && tt < P.piston_ramp) {
         r = 0.5 * (1.0 - std::cos(M_PI * tt / P.piston_ramp));
         dr = 0.5 * M_PI / P.piston_ramp * std::sin(M_PI * tt / P.piston_ramp);
     }
-    if (vel) *vel = dr * s + r * ds;
-    return r * s;
+    if (vel) *vel = dr * (s - s0) + r * ds;
+    return s0 + r * (s - s0);
 }
 
 }  // namespace

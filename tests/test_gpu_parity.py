@@ -175,17 +175,20 @@ def test_mixed_against_fp64(solver):
     """FP32 pair sums / inner Krylov with FP64 refinement against the FP64 path
     on the moving c1 tank (piston from t = 0): the PPE reaches the same
     relative residual and every field stays within 1e-6 (relative L2) after
-    two steps, the eddy viscosity included."""
+    two steps, the eddy viscosity included.  Both solve to 1e-10: at 1e-8
+    two solves of the same system already differ by up to ~1e-6 in p
+    (measured 1.1e-6 between these two arms), which is the stopping test,
+    not the arithmetic."""
     spec = small_spec(dx=0.01, piston_ramp=0.0)
     scen = sc.build(spec)
     out, infos = {}, {}
     for prec in ("fp64", "mixed"):
-        P = sc.make_params(spec, scen.bounds, precision=prec, solver=solver, tol=1e-8, maxit=20000,
-                           inner_tol=1e-2, max_outer=40)
+        P = sc.make_params(spec, scen.bounds, precision=prec, solver=solver, tol=1e-10, maxit=20000,
+                           inner_tol=1e-2, max_outer=60)
         g, _ = make_pair(scen, P, Solver)
         infos[prec] = g.step(2)
         out[prec] = g.download_state()
-    assert infos["mixed"].converged and infos["mixed"].rel_residual <= 1e-8
+    assert infos["mixed"].converged and infos["mixed"].rel_residual <= 1e-10
     assert infos["mixed"].outer >= 1
     errs = {f: rel_l2(out["mixed"][f], out["fp64"][f])
             for f in ("x", "y", "vx", "vy", "p", "rho", "porosity", "nut", "tke", "vel")}

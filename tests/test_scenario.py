@@ -50,15 +50,27 @@ def test_porosity_field_per_cell():
 
 
 def test_irregular_piston_ramps_in_from_rest():
-    """c5's eight-mode stroke has seeded phases; its 0.01 s start-up ramp
-    starts the wall at rest on its lattice."""
+    """c5's eight-mode stroke has seeded phases, so it starts at s0 != 0; the
+    0.01 s ramp takes it from s0 with zero velocity, and the wall's rest
+    coordinate carries -s0, so the wall starts at rest on its lattice."""
     spec = sc.config_spec("c5")
     assert len(spec.piston_amp) == 8 and abs(sum(spec.piston_amp) - 0.03) < 1e-12
     assert min(spec.piston_period) == 0.8 and max(spec.piston_period) == 2.0
     assert spec.piston_ramp == sc.STARTUP_RAMP == 0.01
-    assert sc.piston_stroke(spec, 0.0) == (0.0, 0.0)
+    s0 = sum(a * np.sin(p) for a, p in zip(spec.piston_amp, spec.piston_phase))
+    x0, v0 = sc.piston_stroke(spec, 0.0)
+    assert abs(x0 - s0) < 1e-15 and s0 != 0.0 and v0 == 0.0
+    # the wall's speed stays that of the stroke over the ramp: no jump
+    vmax = max(abs(sc.piston_stroke(spec, t)[1]) for t in np.linspace(0.0, 0.02, 201))
+    assert vmax < 0.03 * 2 * np.pi / 0.8
     x1, v1 = sc.piston_stroke(spec, 10.0)
     assert abs(x1) <= 0.03
+    spec.dx = 0.01
+    scen = sc.build(spec)
+    pist = (scen.flags & sc.FLAG_PISTON) != 0
+    inner = pist & (scen.tid == sc.TID_WALL)
+    assert np.allclose(scen.x[inner], -0.5 * spec.dx, rtol=0, atol=1e-15)
+    assert np.all(scen.vx[pist] == 0.0)
 
 
 def test_rampless_stroke_with_phases_starts_on_its_lattice():
