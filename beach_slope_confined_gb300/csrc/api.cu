@@ -168,7 +168,7 @@ static int alloc_for(Ctx* c, int64_t n) {
     if ((rc = dalloc(c, &c->pcell, n)) || (rc = dalloc(c, &c->pslot, n)) || (rc = dalloc(c, &c->sorted, n))) return rc;
     if ((rc = dalloc(c, &c->posf, n)) || (rc = dalloc(c, &c->lstage, 4 * n))) return rc;
     const int64_t slots = ((n + 31) / 32) * 32 * (int64_t)c->K.kmax;
-    if ((rc = dalloc(c, &c->nbr, slots)) || (rc = dalloc(c, &c->cnt, n))) return rc;
+    if ((rc = dalloc(c, &c->nbr, slots)) || (rc = dalloc(c, &c->cnt, n)) || (rc = dalloc(c, &c->cand_nc, n))) return rc;
     // FP64 grad W and PPE values in both precisions; the mixed path adds FP32
     // copies for its FP32 pair sums and inner Krylov sweeps
     if ((rc = dalloc(c, &c->gw, slots)) || (rc = dalloc(c, &c->aval, slots))) return rc;
@@ -180,7 +180,7 @@ static int alloc_for(Ctx* c, int64_t n) {
         c->f_q = tw + 5 * n;
         if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->ellf, slots)) ||
             (rc = dalloc(c, &c->avalh, slots)) || (rc = dalloc(c, &c->ellh, slots)) ||
-            (rc = dalloc(c, &c->ellh_ok, (n + 31) / 32)))
+            (rc = dalloc(c, &c->ellh_ok, (n + 31) / 32)) || (rc = dalloc(c, &c->asm_df, 5 * n)))
             return rc;
     }
     if ((rc = dalloc(c, &c->b, n))) return rc;
@@ -446,6 +446,8 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
     c->mg_w[1] = c->P.mg_sweeps == 2 ? c->P.mg_omega * ((2.0 + M_SQRT1_2) / (2.0 - M_SQRT1_2)) : c->P.mg_omega;
     if (const char* e = std::getenv("BSC_MG_W")) std::sscanf(e, "%lf,%lf", &c->mg_w[0], &c->mg_w[1]);
     if (const char* e = std::getenv("BSC_EXACT_DIV")) c->exact_div = e[0] == '1';
+    if (const char* e = std::getenv("BSC_ASSEMBLY")) c->asm_rcp = std::string(e) == "rcp";
+    if (const char* e = std::getenv("BSC_NEIGHBOUR")) c->nb_warpcell = std::string(e) == "warpcell";
     for (int k = 0; k < 6; ++k) cudaEventCreate(&c->ev_it[k]);
     for (int k = 0; k < 2; ++k) cudaEventCreateWithFlags(&c->ev_lag[k], cudaEventDisableTiming);
     for (int k = 0; k < Ctx::NCOPY; ++k) cudaStreamCreateWithFlags(&c->copy_stream[k], cudaStreamNonBlocking);

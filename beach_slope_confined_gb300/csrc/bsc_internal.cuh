@@ -286,6 +286,10 @@ struct Ctx {
     double* ndist = nullptr;      // pair distance per slot (salinity: scalart's radial)
     double* sdisp = nullptr;      // salinity: D_x, D_y, Dm + nu_t/Sc, 1/n per particle (4n)
     float2* gwf = nullptr;        // FP32 grad W (mixed)
+    float2* asm_df = nullptr;     // mixed assembly: five per-particle double-float inputs
+    bool asm_rcp = false;         // mixed assembly in FP64 with Newton reciprocals (BSC_ASSEMBLY=rcp)
+    bool nb_warpcell = false;     // BSC_NEIGHBOUR=warpcell: warp-per-cell candidate phase
+    int32_t* cand_nc = nullptr;   // its survivors per row (-1: one-pass loop)
     int32_t* cnt = nullptr;
     int32_t* d_flag = nullptr;    // device error flags (capacity, nonfinite)
     int32_t* h_flag = nullptr;    // pinned mirror

@@ -12,6 +12,7 @@
 // Every operator is templated on R, the type of the pair arithmetic: double
 // for the FP64 drop-in path, float for the mixed path (which keeps the
 // particle state, the neighbour predicate and the 2x2 inversion in FP64).
+#include <algorithm>
 #include <cmath>
 
 #include "bsc_internal.cuh"
@@ -58,7 +59,10 @@ __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __
 }
 
 // ---- search.f90:13-399 neighbour / nsearch2 ----------------------------------------
-template <typename R>
+// PRE: the candidate phase already ran (k_cand_warpcell): `cand_nc` holds
+// each row's number of survivors in its list slots, or -1 for a row that
+// takes the one-pass loop.
+template <typename R, bool PRE = false>
 __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KParams K,
                                                          const int32_t* __restrict__ cstart,
                                                          const int32_t* __restrict__ ccount,
@@ -68,7 +72,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                                                          int32_t* __restrict__ nbr, double2* __restrict__ gw,
                                                          float2* __restrict__ gwf, const float* __restrict__ f_vol,
                                                          double* __restrict__ ndist, int32_t* __restrict__ cnt,
-                                                         int32_t* __restrict__ flag) {
+                                                         int32_t* __restrict__ flag,
+                                                         const int32_t* __restrict__ cand_nc = nullptr) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double xi = S.x[i], yi = S.y[i];
@@ -115,7 +120,14 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
         m2 += gx * ry;
         m3 += gy * ry;
     };
-    if (pre_i) {
+    if constexpr (PRE) {
+        nc = cand_nc[i];
+        const bool ok = nc >= 0 && nc <= K.kmax;
+        if (ok)
+            for (int k = 0; k < nc; ++k) pair(nbr[ell(i, k, K.kmax)]);
+        else
+            nc = K.kmax + 1;  // the one-pass loop below
+    } else if (pre_i) {
         // Two phases, so the FP64 work runs on full warps: (1) the FP32
         // pre-test compacts the surviving candidates, in cell-list order,
         // into this row's list slots; (2) the FP64 pair work walks them.  A
@@ -150,7 +162,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
         if (nc <= K.kmax)
             for (int k = 0; k < nc; ++k) pair(nbr[ell(i, k, K.kmax)]);
     }
-    if (!pre_i || nc > K.kmax) {
+    if ((!PRE && !pre_i) || nc > K.kmax) {
         // far from its binned cell (no pre-test), or too many survivors: one
         // pass over the 3x3 cells
         for (int ax = cx - 1; ax <= cx + 1; ++ax) {
@@ -193,13 +205,117 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
     S.flags[i] = f;
 }
 
+// ---- warp-per-cell candidate phase (BSC_NEIGHBOUR=warpcell) ----------------------
+// One warp per cell of the grid.  The warp stages the candidates of the 3x3
+// cells around its cell in shared memory (their indices and float offsets
+// from the cell's origin), with coalesced loads of the cell lists; then, for
+// each particle of the cell in turn, its 32 lanes pre-test 32 staged
+// candidates at a time and a ballot compacts the survivors, in the same cell
+// order as the thread-per-particle kernel, into the particle's list slots.
+// k_neighbour<R, true> then runs the FP64 phase over those slots, so the
+// lists and results are the same as the one-kernel search.  A row is handed
+// to the one-pass loop (cand_nc = -1) when its cell's candidates exceed the
+// staging capacity or the particle sits too far from its binned cell.
+constexpr int WC_WARPS = 4, WC_CAP = 192;
+
+__global__ void __launch_bounds__(WC_WARPS * 32) k_cand_warpcell(int ncell, KParams K,
+                                                                   const int32_t* __restrict__ cstart,
+                                                                   const int32_t* __restrict__ ccount,
+                                                                   const int32_t* __restrict__ sorted,
+                                                                   const float2* __restrict__ posf,
+                                                                   int32_t* __restrict__ nbr,
+                                                                   int32_t* __restrict__ cand_nc) {
+    __shared__ int32_t sj[WC_WARPS][WC_CAP];
+    __shared__ float2 sp[WC_WARPS][WC_CAP];
+    const int wib = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned below = (1u << lane) - 1u;
+    const float csf = (float)K.cs;
+    const float H2f = (float)(K.H2 * (1.0 + PRE_MARGIN));
+    const float far = __int_as_float(0x7f800000);  // +inf: a candidate that skips the pre-test
+    for (int c = blockIdx.x * WC_WARPS + wib; c < ncell; c += gridDim.x * WC_WARPS) {
+        const int mc = ccount[c];
+        if (mc == 0) continue;
+        const int cx = c / K.ny, cy = c - cx * K.ny;
+        int total = 0;
+        for (int ax = cx - 1; ax <= cx + 1; ++ax) {
+            if (ax < 0 || ax >= K.nx) continue;
+            const float shx = (float)(ax - cx) * csf;
+            for (int ay = cy - 1; ay <= cy + 1; ++ay) {
+                if (ay < 0 || ay >= K.ny) continue;
+                const float shy = (float)(ay - cy) * csf;
+                const int cc = ax * K.ny + ay;
+                const int s0 = cstart[cc], m = ccount[cc];
+                for (int q = lane; q < m; q += 32) {
+                    const int idx = total + q;
+                    if (idx < WC_CAP) {
+                        const int j = sorted[s0 + q];
+                        const float2 pj = posf[j];
+                        sj[wib][idx] = j;
+                        sp[wib][idx] = pre_ok(pj, csf) ? make_float2(pj.x + shx, pj.y + shy) : make_float2(far, 0.f);
+                    }
+                }
+                total += m;
+            }
+        }
+        __syncwarp();
+        const int s0c = cstart[c];
+        for (int q = 0; q < mc; ++q) {
+            const int i = sorted[s0c + q];
+            const float2 pi = posf[i];
+            if (total > WC_CAP || !pre_ok(pi, csf)) {
+                if (lane == 0) cand_nc[i] = -1;
+                continue;
+            }
+            int nc = 0;
+            for (int base = 0; base < total; base += 32) {
+                const int k = base + lane;
+                int j = -1;
+                bool keep = false;
+                if (k < total) {
+                    j = sj[wib][k];
+                    if (j != i) {
+                        const float2 p = sp[wib][k];
+                        if (p.x == far) {
+                            keep = true;
+                        } else {
+                            const float fdx = pi.x - p.x, fdy = pi.y - p.y;
+                            keep = !(fdx * fdx + fdy * fdy > H2f);
+                        }
+                    }
+                }
+                const unsigned bal = __ballot_sync(0xffffffffu, keep);
+                if (keep) {
+                    const int pos = nc + __popc(bal & below);
+                    if (pos < K.kmax) nbr[ell(i, pos, K.kmax)] = j;
+                }
+                nc += __popc(bal);
+            }
+            if (lane == 0) cand_nc[i] = nc;
+        }
+        __syncwarp();
+    }
+}
+
 int op_neighbour(Ctx* c) {
     k_posf<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S.x, c->S.y, c->pcell, c->K, c->posf, c->S.vol,
                                                          c->mixed ? c->f_vol : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     StageTimer tk(c, BSC_T_K_NEIGHBOUR);
-    if (c->mixed)
+    if (c->nb_warpcell) {
+        const unsigned gc = (unsigned)std::min<int64_t>((c->ncell + WC_WARPS - 1) / WC_WARPS, 152 * 32);
+        k_cand_warpcell<<<gc, WC_WARPS * 32, 0, c->stream>>>((int)c->ncell, c->K, c->cell_start, c->cell_count,
+                                                              c->sorted, c->posf, c->nbr, c->cand_nc);
+        BSC_LAUNCH(c);
+        if (c->mixed)
+            k_neighbour<float, true><<<g, NB_BLOCK, 0, c->stream>>>(
+                c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, c->nbr, c->gw, c->gwf,
+                c->f_vol, c->ndist, c->cnt, c->d_flag, c->cand_nc);
+        else
+            k_neighbour<double, true><<<g, NB_BLOCK, 0, c->stream>>>(
+                c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, c->nbr, c->gw, nullptr,
+                nullptr, c->ndist, c->cnt, c->d_flag, c->cand_nc);
+    } else if (c->mixed)
         k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
                                                           c->pcell, c->posf, c->nbr, c->gw, c->gwf, c->f_vol, c->ndist,
                                                           c->cnt, c->d_flag);
@@ -755,9 +871,16 @@ int op_comp_vel(Ctx* c) {
 // (part_shift.f90:68-70), so the shift is -csh h^2 frac sum V_j grad W
 // (uncorrected), clamped per component to maxshift*dl; the velocity is
 // corrected with the unclamped shift and the corrected gradient.
+// R: type of the velocity-gradient sums of the Taylor correction.  The
+// position shift sum_j V_j grad W cancels to ~1e-3 of its terms inside the
+// fluid, so it stays FP64 on both paths.  The gradient sums only scale the
+// correction grad(v).delta, a fraction ~|delta|/L of v (1e-3 and below
+// here): on the mixed path they run in FP32 from FP64 velocity differences
+// (rounded on the integer pipe) and the FP32 grad W, so the kernel's FP64
+// work is four operations per pair instead of ten.
 template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_shift(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
-                                                     const typename Vec2<R>::type* __restrict__ gw,
+                                                     const double2* __restrict__ gw, const float2* __restrict__ gwf,
                                                      const int32_t* __restrict__ cnt, int8_t* __restrict__ mark) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -766,30 +889,45 @@ __global__ void __launch_bounds__(NB_BLOCK) k_shift(int64_t n, State S, KParams 
     if (!(S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD)))) return;
     const int m = cnt[i];
     if (m == 0) return;
+    constexpr bool F32 = sizeof(R) == 4;
     const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
     const double vxi = S.vx[i], vyi = S.vy[i];
     // the corrected gradient L grad W enters linearly and L is the row's own,
     // so L is applied once to the four sums of grad W (dv V) rather than per
-    // pair: ten FP64 operations per pair instead of sixteen
-    R sx = 0, sy = 0, ax = 0, bx = 0, ay = 0, by = 0;
+    // pair
+    double sx = 0, sy = 0;
+    R ax = 0, bx = 0, ay = 0, by = 0;
     for (int k = 0; k < m; ++k) {
         const int64_t e = ell(i, k, K.kmax);
         const int j = nbr[e];
-        const auto g = gw[e];
-        const R vj = (R)S.vol[j];
+        const double2 g = gw[e];
+        const double vj = S.vol[j];
         sx += g.x * vj;
         sy += g.y * vj;
-        const R dvx = (R)(S.vx[j] - vxi) * vj, dvy = (R)(S.vy[j] - vyi) * vj;
-        ax += g.x * dvx;
-        bx += g.y * dvx;
-        ay += g.x * dvy;
-        by += g.y * dvy;
+        R gx, gy, dvx, dvy;
+        if constexpr (F32) {
+            const float2 gf = gwf[e];
+            const float vf = f32_of(vj);
+            gx = gf.x;
+            gy = gf.y;
+            dvx = f32_of(S.vx[j] - vxi) * vf;
+            dvy = f32_of(S.vy[j] - vyi) * vf;
+        } else {
+            gx = g.x;
+            gy = g.y;
+            dvx = (S.vx[j] - vxi) * vj;
+            dvy = (S.vy[j] - vyi) * vj;
+        }
+        ax += gx * dvx;
+        bx += gy * dvx;
+        ay += gx * dvy;
+        by += gy * dvy;
     }
     const R tx1 = L0 * ax + L1 * bx, tx2 = L2 * ax + L3 * bx;
     const R ty1 = L0 * ay + L1 * by, ty2 = L2 * ay + L3 * by;
     const double frac = (fi & BSC_FLAG_FREE) ? 0.01 : 1.0;
     const double coef = -K.csh * (K.h * K.h) * frac;
-    const double xs = coef * (double)sx, ys = coef * (double)sy;
+    const double xs = coef * sx, ys = coef * sy;
     const double lim = K.maxshift * K.dl;
     const double cx = (xs == 0.0) ? 0.0 : fmin(fabs(xs), lim) * xs / fabs(xs);
     const double cy = (ys == 0.0) ? 0.0 : fmin(fabs(ys), lim) * ys / fabs(ys);
@@ -813,13 +951,16 @@ int op_opt2_shift(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "opt2_shift before neighbour");
     int8_t* mark = (int8_t*)c->pslot;  // scratch: pslot is free between cell builds
     const unsigned g = blocks_for(c->n, NB_BLOCK);
-    // FP64 on both paths: the shift adds grad(v).delta to the velocity, a
-    // gradient sum that cancels heavily; in FP32 it moved the mixed path's
-    // velocities by ~7e-6 (relative) from the FP64 path's after 8 steps of
-    // the c3 tank, in FP64 by ~1e-6, for 0.3 ms a step
+    // The position shift's sum is FP64 on both paths (with it in FP32 the
+    // mixed path's velocities moved by ~7e-6 from the FP64 path's after 8
+    // c3 steps, against ~1e-6 in FP64); on the mixed path the velocity
+    // gradient of the Taylor correction runs in FP32 (see k_shift)
     {
         StageTimer tk(c, BSC_T_K_SHIFT);
-        k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, mark);
+        if (c->mixed)
+            k_shift<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->gwf, c->cnt, mark);
+        else
+            k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, nullptr, c->cnt, mark);
         BSC_LAUNCH(c);
     }
     k_shift_apply<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, mark);

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "bsc_internal.cuh"
+#include "dfloat.cuh"
 #include "ellop.cuh"
 
 namespace bsc {
@@ -139,6 +140,160 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble(int64_t n, State S, KPara
     b[i] = ((double)fv / dt) / d;
 }
 
+// ---- the mixed path's assembly in double-float arithmetic (dfloat.cuh) -------------
+// The same coefficients as k_assemble (isph.f90:115-456, every row type),
+// with the pair arithmetic on FP32 pairs of ~48 bits instead of FP64: the
+// FP64 pipe, this kernel's bound on this GPU, is left with the two velocity
+// differences (formed exactly in FP64, then split), the split of grad W and
+// the widening of each entry, seven operations a pair instead of about
+// thirty-four.  Positions enter as offsets from the particle's own cell
+// origin, split once per particle: a coordinate of ~1 m split into two
+// floats keeps ~2^-48 m, which would cost the pair offset (~1e-3 m) about
+// 1e-12 of its accuracy; the offset keeps ~2^-48 of a cell.
+//
+// Per particle (k_asm_df_pre): offsets ox, oy from the cell origin, V = m/rho,
+// q = rho/n and the free-surface factor 1 + oden/(rho0 rel_den), as
+// double-floats, array by array.
+__global__ void k_asm_df_pre(int64_t n, State S, KParams K, const int32_t* __restrict__ pcell,
+                             const double* __restrict__ q, float2* __restrict__ pre) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
+    pre[i] = df_pack(df_of(S.x[i] - (K.gx0 + cx * K.cs)));
+    pre[n + i] = df_pack(df_of(S.y[i] - (K.gy0 + cy * K.cs)));
+    pre[2 * n + i] = df_pack(df_of(S.vol[i]));
+    pre[3 * n + i] = df_pack(df_of(q[i]));
+    pre[4 * n + i] = df_pack(df_of(1.0 + S.oden[i] * (1.0 / (K.rho0 * K.rel_den))));
+}
+
+// x_i - x_j from the offsets and the cells' column (row) difference k:
+// (o_i - o_j) + k cs
+__device__ __forceinline__ df2 df_pair_offset(df2 oi, float2 oj, int k, df2 cs) {
+    df2 d = df_sub(oi, df_unpack(oj));
+    if (k == 1) d = df_add(d, cs);
+    else if (k == -1) d = df_sub(d, cs);
+    else if (k != 0) d = df_add(d, df_mul(cs, df2{(float)k, 0.0f}));
+    return d;
+}
+
+__global__ void __launch_bounds__(NB_BLOCK) k_assemble_df(int64_t n, State S, KParams K,
+                                                           const int32_t* __restrict__ nbr,
+                                                           const double2* __restrict__ gw,
+                                                           const int32_t* __restrict__ cnt,
+                                                           const int32_t* __restrict__ pcell,
+                                                           const float2* __restrict__ pre, double* __restrict__ aval,
+                                                           int2* __restrict__ ellf, __half* __restrict__ avalh,
+                                                           double* __restrict__ b, const double* __restrict__ q,
+                                                           const double* __restrict__ usx,
+                                                           const double* __restrict__ usy, double dt) {
+    const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float2* __restrict__ pox = pre;
+    const float2* __restrict__ poy = pre + n;
+    const float2* __restrict__ pvl = pre + 2 * n;
+    const float2* __restrict__ pq = pre + 3 * n;
+    const float2* __restrict__ plamp = pre + 4 * n;
+    float2* __restrict__ vdf = reinterpret_cast<float2*>(aval);  // entries between the two passes
+    const int tid_i = S.tid[i];
+    const bool free_i = S.flags[i] & BSC_FLAG_FREE;
+    const int ci = pcell[i], cxi = ci / K.ny, cyi = ci - cxi * K.ny;
+    const df2 oxi = df_unpack(pox[i]), oyi = df_unpack(poy[i]);
+    const df2 cs = df_of(K.cs), lam = df_of(K.lam);
+    const double ni64 = S.por[i];
+    const df2 qi = df_unpack(pq[i]);
+    const df2 L0 = df_of(S.L0[i]), L1 = df_of(S.L1[i]), L2 = df_of(S.L2[i]), L3 = df_of(S.L3[i]);
+    const double usxi = usx[i], usyi = usy[i];
+    // fixed-wall rows: m_i/rho_i and v*_i/n_i; wall neighbours of fluid rows: 1/n_i
+    const df2 mi_over_rhoi = df_mul(df_of(S.mass[i]), df_rcp(df_of(S.rho[i])));
+    const df2 inv_ni = df_rcp(df_of(ni64));
+    const double vxsi = S.vxs[i], vysi = S.vys[i];
+    const double vxi_n = vxsi / ni64, vyi_n = vysi / ni64;
+    const int m = cnt[i];
+    df2 dia{0.0f, 0.0f}, fv{0.0f, 0.0f};
+    for (int k = 0; k < m; ++k) {
+        const int64_t e = ell(i, k, K.kmax);
+        const int j = nbr[e];
+        const double2 g64 = gw[e];
+        const df2 gxr = df_of(g64.x), gyr = df_of(g64.y);
+        const int tid_j = S.tid[j];
+        const int cj = pcell[j], cxj = cj / K.ny, cyj = cj - cxj * K.ny;
+        const df2 dx = df_pair_offset(oxi, pox[j], cxi - cxj, cs);
+        const df2 dy = df_pair_offset(oyi, poy[j], cyi - cyj, cs);
+        const df2 p_dist = df_rcp(df_add(df_add(df_sqr(dx), df_sqr(dy)), lam));
+        const df2 pvol = df_unpack(pvl[j]);
+        df2 val{0.0f, 0.0f};
+        if (tid_i == BSC_TID_FLUID) {
+            const df2 gx = df_add(df_mul(L0, gxr), df_mul(L1, gyr));
+            const df2 gy = df_add(df_mul(L2, gxr), df_mul(L3, gyr));
+            const df2 t = df_mul(df_mul(df_twice(pvol), df_add(df_mul(dx, gx), df_mul(dy, gy))), p_dist);
+            val = df_neg(t);
+            dia = df_add(dia, (free_i && tid_j == BSC_TID_FLUID) ? df_mul(t, df_unpack(plamp[j])) : t);
+            // divergence of the porous-weighted predicted velocity (:241-270)
+            df2 ddx, ddy;
+            if (tid_j == BSC_TID_FLUID) {
+                // 2 q_i q_j / (q_i + q_j), q = rho / n
+                const df2 qj = df_unpack(pq[j]);
+                const df2 rho_ij = df_mul(df_twice(df_mul(qi, qj)), df_rcp(df_add(qi, qj)));
+                ddx = df_mul(rho_ij, df_of(usx[j] - usxi));
+                ddy = df_mul(rho_ij, df_of(usy[j] - usyi));
+            } else {
+                ddx = df_mul(qi, df_mul(df_of(S.vxs[j] - vxsi), inv_ni));
+                ddy = df_mul(qi, df_mul(df_of(S.vys[j] - vysi), inv_ni));
+            }
+            fv = df_add(fv, df_mul(pvol, df_add(df_mul(ddx, gx), df_mul(ddy, gy))));
+        } else if (tid_i == BSC_TID_GHOST) {
+            if (tid_j <= 2) {
+                const df2 t = df_mul(df_mul(df_twice(pvol), df_add(df_mul(dx, gxr), df_mul(dy, gyr))), p_dist);
+                val = df_neg(t);
+                dia = df_add(dia, t);
+            }
+        } else if (tid_i == BSC_TID_WALL) {
+            if (tid_j == BSC_TID_FLUID) {
+                const df2 Lj0 = df_of(S.L0[j]), Lj1 = df_of(S.L1[j]), Lj2 = df_of(S.L2[j]), Lj3 = df_of(S.L3[j]);
+                const df2 gx = df_add(df_mul(Lj0, gxr), df_mul(Lj1, gyr));
+                const df2 gy = df_add(df_mul(Lj2, gxr), df_mul(Lj3, gyr));
+                const df2 t =
+                    df_mul(df_mul(df_twice(mi_over_rhoi), df_add(df_mul(dx, gx), df_mul(dy, gy))), p_dist);
+                val = df_neg(t);
+                dia = df_add(dia, t);
+                // q_j (v*_j/n_j - v*_i/n_i), the wall row's v*_i/n_i in FP64
+                const df2 qj = df_unpack(pq[j]);
+                const df2 ddx = df_mul(qj, df_of(usx[j] - vxi_n));
+                const df2 ddy = df_mul(qj, df_of(usy[j] - vyi_n));
+                fv = df_add(fv, df_mul(mi_over_rhoi, df_add(df_mul(ddx, gx), df_mul(ddy, gy))));
+            } else {
+                const df2 t = df_mul(df_mul(df_twice(pvol), df_add(df_mul(dx, gxr), df_mul(dy, gyr))), p_dist);
+                val = df_neg(t);
+                dia = df_add(dia, t);
+            }
+        }
+        vdf[e] = df_pack(val);
+    }
+    const double d = df_to_double(dia);
+    if (d == 0.0 || !isfinite(d)) {
+        // zero-neighbour guard: identity row, b = 0 (the reference divides by 0)
+        for (int k = 0; k < m; ++k) {
+            const int64_t e = ell(i, k, K.kmax);
+            aval[e] = 0.0;
+            ellf[e] = make_int2(nbr[e], 0);
+            avalh[e] = __float2half_rn(0.f);
+        }
+        b[i] = 0.0;
+        return;
+    }
+    const df2 inv = df_rcp(dia);
+    for (int k = 0; k < m; ++k) {
+        const int64_t e = ell(i, k, K.kmax);
+        const df2 v = df_mul(df_unpack(vdf[e]), inv);
+        aval[e] = df_to_double(v);
+        // the inner sweeps' FP32 copy is the high half (the FP32 rounding of
+        // the value); the V-cycle's FP16 copy is rounded from it
+        ellf[e] = make_int2(nbr[e], __float_as_int(v.hi));
+        avalh[e] = __float2half_rn(v.hi);
+    }
+    b[i] = df_to_double(df_mul(df_mul(fv, df_rcp(df_of(dt))), inv));
+}
+
 __global__ void k_vs_over_por(int64_t n, State S, double* __restrict__ q, double* __restrict__ ux,
                               double* __restrict__ uy) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -181,7 +336,15 @@ int op_ppe_assemble(Ctx* c) {
     // FP64 assembly in both paths: the PPE coefficients are sums whose FP32
     // rounding moves the pressure by ~5e-6 (relative) at 1e-8 residual; the
     // mixed path keeps an FP32 copy for its inner sweeps
-    {
+    if (c->mixed && !c->exact_div && !c->asm_rcp) {
+        // mixed path: double-float pair arithmetic (k_assemble_df)
+        k_asm_df_pre<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, q, c->asm_df);
+        BSC_LAUNCH(c);
+        StageTimer tk(c, BSC_T_K_ASSEMBLE);
+        k_assemble_df<<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->pcell, c->asm_df,
+                                                      c->aval, c->ellf, c->avalh, c->b, q, ux, uy, c->dt);
+        BSC_LAUNCH(c);
+    } else {
         StageTimer tk(c, BSC_T_K_ASSEMBLE);
         if (c->mixed && !c->exact_div)
             k_assemble<double, true><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->aval,

@@ -60,18 +60,25 @@ T_K_NEIGHBOUR, T_K_ASSEMBLE, T_K_INT_VEL, T_K_EFFPOR, T_K_SHIFT = 25, 26, 27, 28
 #     moment sum M 10 (mixed: M in FP32, so 14);
 #   k_assemble: offsets 2, 1/(r^2+lam) 5, L grad W 6, the coefficient 6, the
 #     diagonal 2, rho_ij 4, velocity differences 4, divergence 5, the Jacobi
-#     scaling 1 (FP64 on both paths);
+#     scaling 1 (mixed: k_assemble_df runs that arithmetic on FP32 pairs; its
+#     FP64 work is the two velocity differences and their splits, the split
+#     of grad W and the widening of the entry, 7);
 #   k_int_vel: the two harmonic viscosity means and their sum 10, offsets
 #     and r^2 5, 1/(r^2+lam) 2, L grad W 6, the coefficient 6, velocity
 #     differences 2, viscous sums 6, SPS sums 6 (mixed: the offsets and
 #     velocity differences, 4);
-#   k_shift: 16 (FP64 on both paths).
+#   k_shift: 16 (mixed: the position-shift sums and the velocity differences,
+#     6; the velocity-gradient sums run in FP32).
 # Per solid pair, k_effpor: offsets 2, d^2 3, root 1, W 9, the weighted sum
 # 4 (mixed: the FP64 sum of the FP32 terms, 1).
-FP64_FLOPS = {T_K_NEIGHBOUR: (24, 14), T_K_ASSEMBLE: (35, 35), T_K_INT_VEL: (43, 4), T_K_SHIFT: (16, 16),
+FP64_FLOPS = {T_K_NEIGHBOUR: (24, 14), T_K_ASSEMBLE: (35, 7), T_K_INT_VEL: (43, 4), T_K_SHIFT: (16, 6),
               T_K_EFFPOR: (19, 1)}
-KERNEL_NAMES = {T_K_NEIGHBOUR: "k_neighbour", T_K_ASSEMBLE: "k_assemble", T_K_INT_VEL: "k_int_vel",
-                T_K_SHIFT: "k_shift", T_K_EFFPOR: "k_effpor"}
+# the kernel each slot times: (FP64 path, mixed path)
+KERNEL_NAMES = {T_K_NEIGHBOUR: ("k_neighbour<double>", "k_neighbour<float>"),
+                T_K_ASSEMBLE: ("k_assemble<double>", "k_assemble_df"),
+                T_K_INT_VEL: ("k_int_vel<double>", "k_int_vel<float>"),
+                T_K_SHIFT: ("k_shift<double>", "k_shift<float>"),
+                T_K_EFFPOR: ("k_effpor<double>", "k_effpor<float>")}
 
 
 # --------------------------------------------------------------------------
@@ -245,12 +252,12 @@ def traffic_per_row(kind: str):
         return None
 
 
-def kernel_traffic(kernel: str, prec: str, n: int):
+def kernel_traffic(kernel: str, n: int):
     """DRAM bytes per launch of a pair kernel, from the committed ncu summary
-    (bytes per row, scaled to n rows)."""
+    (bytes per row of a smaller capture, scaled to n rows)."""
     try:
         with open(os.path.join(ROOT, "profiles", "kernel_dram_traffic.json")) as fh:
-            return float(json.load(fh)[f"{kernel} {prec}"]["dram_bytes_per_row"]) * n
+            return float(json.load(fh)[kernel]["dram_bytes_per_row"]) * n
     except (OSError, KeyError, ValueError):
         return None
 
@@ -283,7 +290,7 @@ def kernel_rooflines(t, steps: int, nnz: int, spairs: int, prec: str, fp64_peak:
         pairs = spairs if slot == T_K_EFFPOR else nnz
         flops = FP64_FLOPS[slot][col] * pairs
         gf = flops / (ms * 1e-3) / 1e9
-        out.append({"kernel": f"{name}<{'double' if col == 0 else 'float'}>", "ms_per_launch": ms,
+        out.append({"kernel": name[col], "ms_per_launch": ms,
                     "launches_per_step": calls / steps, "ms_per_step": t.ms[slot] / steps,
                     "fp64_flops_per_launch": flops, "pairs_per_launch": pairs, "achieved_gflops": gf,
                     "peak_gflops": fp64_peak, "frac": gf / fp64_peak if fp64_peak else None})
@@ -526,8 +533,8 @@ def wcsph_check(args):
       * central differences of alpha and beta at relative steps 1e-1 ..
         1e-7 (two-point) and at 3e-2 (four-point): where the differences
         agree with the adjoint, and where roundoff takes over;
-      * central differences for every porosity cell whose adjoint gradient
-        is nonzero, at the relative step of the plateau and at 1e-6;
+      * central differences for every porosity cell the fluid sees, at
+        relative steps 3e-2 .. 1e-6;
       * the oracle's FP64 adjoint (scatter form, every state kept) over the
         first `--wcsph-oracle-steps` steps of the same case, against the
         CUDA adjoint of the same shortened run.
@@ -586,21 +593,30 @@ def wcsph_check(args):
     plateau = min(sweep, key=lambda r: max(v for v in sweep[r].values() if v is not None))
     out["plateau_step"] = float(plateau)
     gp = grad[2:].reshape(grid0.shape)
-    cells = [tuple(ix) for ix in np.argwhere(np.abs(gp) > 0)]
+    # the cells the fluid sees: adjoint gradient above 1e-6 of the largest
+    # (the others carry ~1e-25 and their differences are exactly zero); each
+    # difference is measured against max(|fd|, 1e-2 max|fd|), as the unit test
+    # of the gradient does
+    cells = [tuple(ix) for ix in np.argwhere(np.abs(gp) > 1e-6 * np.abs(gp).max())]
     por = {}
-    for rs in (float(plateau), 1e-6):
-        diffs = []
+    for rs in (3e-2, 1e-2, 1e-3, 1e-4, 1e-5, 1e-6):
+        fds = []
         for (iy, ix) in cells:
             h = rs * grid0[iy, ix]
             gm, gpl = grid0.copy(), grid0.copy()
             gm[iy, ix] -= h
             gpl[iy, ix] += h
-            d = (misfit(a0, b0, gpl)[0] - misfit(a0, b0, gm)[0]) / (2.0 * h)
-            diffs.append(abs(float(gp[iy, ix]) - d) / abs(d) if d != 0 else float("inf"))
-        diffs = np.asarray(diffs)
+            fds.append((misfit(a0, b0, gpl)[0] - misfit(a0, b0, gm)[0]) / (2.0 * h))
+        fds = np.asarray(fds)
+        adj = np.asarray([gp[c] for c in cells])
+        floor = 1e-2 * np.abs(fds).max() if fds.size else 0.0
+        diffs = np.abs(adj - fds) / np.maximum(np.abs(fds), floor) if fds.size else np.zeros(0)
+        top = np.argsort(-np.abs(adj))[:5]
         por[f"{rs:g}"] = {"cells": len(cells), "max_rel_diff": float(diffs.max()) if diffs.size else None,
                           "median_rel_diff": float(np.median(diffs)) if diffs.size else None,
-                          "cells_within_1e-4": int((diffs < 1e-4).sum())}
+                          "cells_within_1e-4": int((diffs < 1e-4).sum()),
+                          "largest_five": [{"cell": [int(cells[k][0]), int(cells[k][1])], "adjoint": float(adj[k]),
+                                            "fd": float(fds[k])} for k in top]}
     out["porosity_cells"] = por
     out["porosity_gradient_norm"] = float(np.linalg.norm(gp))
     g.close()
@@ -944,7 +960,7 @@ def main():
     if top and top["ms_per_step"] > spmv_roof["ms_per_step"]:
         roofline = {"bound": "fp64", "kernel": top["kernel"] + " (mixed path)", "achieved": top["achieved_gflops"],
                     "peak": top["peak_gflops"], "unit": "GFLOP/s", "frac": top["frac"],
-                    "traffic": kernel_traffic(top["kernel"], "mixed", m["n"]),
+                    "traffic": kernel_traffic(top["kernel"], m["n"]),
                     "algorithmic_fp64_flops_per_launch": top["fp64_flops_per_launch"],
                     "avg_launch_ms": top["ms_per_launch"], "launches_per_step": top["launches_per_step"],
                     "share_of_step": top["ms_per_step"] / m["ms_per_step"],

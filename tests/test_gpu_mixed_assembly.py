@@ -1,10 +1,12 @@
-"""The mixed path's Newton-Raphson reciprocal (rcp_nr in bsc_internal.cuh).
+"""The mixed path's PPE assembly against the FP64 one.
 
-The mixed path's FP64 PPE assembly divides by y0 (2 - x y0) refinement of an
-FP32 reciprocal instead of the FP64 quotient; the bound is a relative error
-of about 2^-46 per quotient.  Both variants run here on the same state (the
-environment switch BSC_EXACT_DIV=1 selects the FP64 quotients) and the
-assembled, Jacobi-scaled systems are compared entry by entry.
+The mixed path assembles its FP64 system in one of two ways: by default in
+double-float arithmetic (k_assemble_df, FP32 pairs of ~48 bits, dfloat.cuh),
+or with BSC_ASSEMBLY=rcp in FP64 with Newton-Raphson reciprocals (rcp_nr in
+bsc_internal.cuh, a relative error of about 2^-46 per quotient).  Each runs
+here against the FP64 assembly with IEEE divisions (BSC_EXACT_DIV=1) on the
+same state, and the assembled, Jacobi-scaled systems are compared entry by
+entry: within 1e-12, the right-hand sides within 1e-11.
 """
 import os
 
@@ -17,19 +19,20 @@ from pairrun import small_spec
 pytestmark = pytest.mark.gpu
 
 
-def _assembled(exact: bool):
-    old = os.environ.get("BSC_EXACT_DIV")
-    os.environ["BSC_EXACT_DIV"] = "1" if exact else "0"
+def _assembled(env):
+    old = {k: os.environ.get(k) for k in ("BSC_EXACT_DIV", "BSC_ASSEMBLY")}
+    os.environ.update(env)
     try:
-        spec = small_spec()
+        spec = small_spec(piston_ramp=0.0)
         scen = sc.build(spec)
         P = sc.make_params(spec, scen.bounds, precision="mixed", tol=1e-10, maxit=20000, precond="mg")
         g = Solver(P)
     finally:
-        if old is None:
-            del os.environ["BSC_EXACT_DIV"]
-        else:
-            os.environ["BSC_EXACT_DIV"] = old
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
     setup_tank(g, scen)
     for stage in (g.piston, g.projection, g.cellshift, g.resetid, g.neighbour, g.effpor, g.eddyvis, g.int_vel):
         stage()
@@ -39,13 +42,16 @@ def _assembled(exact: bool):
     return rp, col, val, rhs
 
 
-def test_newton_reciprocal_assembly_matches_division():
-    rp_a, col_a, val_a, rhs_a = _assembled(exact=False)
-    rp_b, col_b, val_b, rhs_b = _assembled(exact=True)
+@pytest.mark.parametrize("variant", ["df", "rcp"])
+def test_mixed_assembly_matches_fp64_division(variant):
+    env = {"BSC_EXACT_DIV": "0", "BSC_ASSEMBLY": "rcp" if variant == "rcp" else "df"}
+    rp_a, col_a, val_a, rhs_a = _assembled(env)
+    rp_b, col_b, val_b, rhs_b = _assembled({"BSC_EXACT_DIV": "1", "BSC_ASSEMBLY": "df"})
     assert np.array_equal(rp_a, rp_b) and np.array_equal(col_a, col_b)
-    # each entry: a handful of quotients, each within ~2^-46
     rel = np.abs(val_a - val_b) / np.maximum(np.abs(val_b), 1e-300)
-    print("max entry rel diff", rel.max(), "rhs rel diff", np.linalg.norm(rhs_a - rhs_b) / np.linalg.norm(rhs_b))
+    rel[val_b == 0] = np.abs(val_a[val_b == 0])
+    print(variant, "max entry rel diff", rel.max(), "rhs rel diff",
+          np.linalg.norm(rhs_a - rhs_b) / np.linalg.norm(rhs_b))
     assert rel.max() < 1e-12
     assert np.linalg.norm(rhs_a - rhs_b) <= 1e-11 * np.linalg.norm(rhs_b)
     # the switch selects a different code path: some entries differ in the last bits

@@ -195,3 +195,36 @@ def test_mixed_against_fp64(solver):
     print("mixed vs fp64 relative L2:", errs)
     for f, e in errs.items():
         assert e < 1e-6, (f, e)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_warp_per_cell_search_gives_the_same_steps(precision):
+    """The warp-per-cell candidate phase (BSC_NEIGHBOUR=warpcell) writes the
+    same survivors in the same order as the one-kernel search, so three
+    whole steps come out bit for bit the same, lists included."""
+    import os
+
+    spec = small_spec(dx=0.01, piston_ramp=0.0)
+    scen = sc.build(spec)
+    out = {}
+    for variant in ("thread", "warpcell"):
+        old = os.environ.get("BSC_NEIGHBOUR")
+        os.environ["BSC_NEIGHBOUR"] = variant
+        try:
+            P = sc.make_params(spec, scen.bounds, precision=precision, tol=1e-8, maxit=20000, precond="mg")
+            g = Solver(P)
+        finally:
+            if old is None:
+                os.environ.pop("BSC_NEIGHBOUR", None)
+            else:
+                os.environ["BSC_NEIGHBOUR"] = old
+        from beach_slope_confined_gb300 import setup_tank
+
+        setup_tank(g, scen)
+        g.step(3)
+        out[variant] = (g.download_state(), g.get_neighbors())
+        g.close()
+    (a, (oa, ia)), (b, (ob, ib)) = out["thread"], out["warpcell"]
+    assert np.array_equal(oa, ob) and np.array_equal(ia, ib)
+    for f in ("x", "y", "vx", "vy", "p", "nut", "porosity"):
+        assert np.array_equal(a[f], b[f]), f
