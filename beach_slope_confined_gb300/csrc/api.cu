@@ -180,7 +180,8 @@ static int alloc_for(Ctx* c, int64_t n) {
         c->f_q = tw + 5 * n;
         if ((rc = dalloc(c, &c->gwf, slots)) || (rc = dalloc(c, &c->ellf, slots)) ||
             (rc = dalloc(c, &c->avalh, slots)) || (rc = dalloc(c, &c->ellh, slots)) ||
-            (rc = dalloc(c, &c->ellh_ok, (n + 31) / 32)) || (rc = dalloc(c, &c->asm_df, 5 * n)))
+            (rc = dalloc(c, &c->ellh_ok, (n + 31) / 32)) || (rc = dalloc(c, &c->asm_df, 5 * n)) ||
+            (rc = dalloc(c, &c->posd, n)))
             return rc;
     }
     if ((rc = dalloc(c, &c->b, n))) return rc;

@@ -287,6 +287,7 @@ struct Ctx {
     double* sdisp = nullptr;      // salinity: D_x, D_y, Dm + nu_t/Sc, 1/n per particle (4n)
     float2* gwf = nullptr;        // FP32 grad W (mixed)
     float2* asm_df = nullptr;     // mixed assembly: five per-particle double-float inputs
+    float4* posd = nullptr;       // mixed search: offsets to the cell origin as double-floats
     bool asm_rcp = false;         // mixed assembly in FP64 with Newton reciprocals (BSC_ASSEMBLY=rcp)
     bool nb_warpcell = false;     // BSC_NEIGHBOUR=warpcell: warp-per-cell candidate phase
     int32_t* cand_nc = nullptr;   // its survivors per row (-1: one-pass loop)

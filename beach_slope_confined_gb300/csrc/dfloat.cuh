@@ -86,6 +86,19 @@ __device__ __forceinline__ df2 df_rcp(df2 a) {
     return df_quick_two_sum(y, __fmul_rn(y, r));
 }
 
+// sqrt(a) for a > 0: the FP32 root r0 = a.hi / sqrt(a.hi) from the
+// reciprocal root, then one Newton correction r0 + (a - r0^2) / (2 r0) with
+// the residual formed exactly enough (r0^2 by TwoProduct; a.hi - r0^2 is
+// exact, r0^2 lying within 2^-21 of a.hi): about 2^-44 relative
+__device__ __forceinline__ df2 df_sqrt(df2 a) {
+    const float y = rsqrtf(a.hi);
+    const float r0 = __fmul_rn(a.hi, y);
+    const float p = __fmul_rn(r0, r0);
+    const float e = __fmaf_rn(r0, r0, -p);
+    const float res = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p), e), a.lo);
+    return df_quick_two_sum(r0, __fmul_rn(__fmul_rn(res, y), 0.5f));
+}
+
 // FP32 -> FP64 on the integer pipe, zero kept exact
 __device__ __forceinline__ double f64z(float f) { return f == 0.0f ? 0.0 : f64_of(f); }
 
@@ -101,5 +114,15 @@ __device__ __forceinline__ double df_to_double(df2 a) { return f64z(a.hi) + f64z
 
 __device__ __forceinline__ float2 df_pack(df2 a) { return make_float2(a.hi, a.lo); }
 __device__ __forceinline__ df2 df_unpack(float2 v) { return {v.x, v.y}; }
+
+// x_i - x_j of two particles from their offsets o to their own cells'
+// origins and the cells' column (or row) difference k: (o_i - o_j) + k cs
+__device__ __forceinline__ df2 df_pair_offset(df2 oi, float2 oj, int k, df2 cs) {
+    df2 d = df_sub(oi, df_unpack(oj));
+    if (k == 1) d = df_add(d, cs);
+    else if (k == -1) d = df_sub(d, cs);
+    else if (k != 0) d = df_add(d, df_mul(cs, df2{(float)k, 0.0f}));
+    return d;
+}
 
 }  // namespace bsc

@@ -16,6 +16,7 @@
 #include <cmath>
 
 #include "bsc_internal.cuh"
+#include "dfloat.cuh"
 #include "sph_kernel.cuh"
 
 namespace bsc {
@@ -48,14 +49,20 @@ __device__ __forceinline__ bool pre_ok(float2 p, float csf) {
 }
 
 // (mixed path: also the FP32 twin of V for the neighbour search's M sum)
+// (mixed path: also the offsets as double-floats, (hi x, lo x, hi y, lo y))
 __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
                        const int32_t* __restrict__ pcell, KParams K, float2* __restrict__ posf,
-                       const double* __restrict__ vol, float* __restrict__ f_vol) {
+                       const double* __restrict__ vol, float* __restrict__ f_vol, float4* __restrict__ posd) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
-    posf[i] = make_float2((float)(x[i] - (K.gx0 + cx * K.cs)), (float)(y[i] - (K.gy0 + cy * K.cs)));
+    const double ox = x[i] - (K.gx0 + cx * K.cs), oy = y[i] - (K.gy0 + cy * K.cs);
+    posf[i] = make_float2((float)ox, (float)oy);
     if (f_vol) f_vol[i] = (float)vol[i];
+    if (posd) {
+        const df2 dx = df_of(ox), dy = df_of(oy);
+        posd[i] = make_float4(dx.hi, dx.lo, dy.hi, dy.lo);
+    }
 }
 
 // ---- search.f90:13-399 neighbour / nsearch2 ----------------------------------------
@@ -69,6 +76,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                                                          const int32_t* __restrict__ sorted,
                                                          const int32_t* __restrict__ pcell,
                                                          const float2* __restrict__ posf,
+                                                         const float4* __restrict__ posd,
                                                          int32_t* __restrict__ nbr, double2* __restrict__ gw,
                                                          float2* __restrict__ gwf, const float* __restrict__ f_vol,
                                                          double* __restrict__ ndist, int32_t* __restrict__ cnt,
@@ -84,9 +92,73 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
     const bool pre_i = pre_ok(pi, csf);
     R m0 = 0, m1 = 0, m2 = 0, m3 = 0;
     int count = 0, nc = 0;
+    // Mixed path, Wendland kernel: the pair's geometry and grad W in
+    // double-float arithmetic (dfloat.cuh) from the double-float offsets to
+    // the cells' origins.  r^2 comes out within ~1e-12 of the r^2 of the
+    // FP64 positions (the offsets keep 2^-48 of a cell; the FP64 cell
+    // origins round by ~4e-16 m), and the FP64 test rounds d^2 by ~4e-16 of
+    // itself, so wherever r^2 lies more than 1e-10 of T from the threshold
+    // the two agree: only candidates inside that band take the exact FP64
+    // test, and the sets stay those of the FP64 predicate.  Per pair the
+    // FP64 pipe keeps the widening of the stored grad W (2 operations, ~14
+    // before).  Particles far from their binned cell (no pre-test) take the
+    // FP64 work below.
+    [[maybe_unused]] const bool use_df = sizeof(R) == 4 && posd && K.kernel == BSC_KERNEL_WENDLAND_C2 && pre_i;
+    [[maybe_unused]] df2 oxi{0.f, 0.f}, oyi{0.f, 0.f};
+    [[maybe_unused]] df2 cs_df{0.f, 0.f}, T_df{0.f, 0.f}, hih{0.f, 0.f}, mwF{0.f, 0.f};
+    [[maybe_unused]] float band = 0.f;
+    if constexpr (sizeof(R) == 4) {
+        if (use_df) {
+            const float4 oi = posd[i];
+            oxi = {oi.x, oi.y};
+            oyi = {oi.z, oi.w};
+            cs_df = df_of(K.cs);
+            T_df = df_of(K.H2x);
+            hih = df_of(K.half_inv_h);
+            mwF = df_of(-K.wend_F);
+            band = (float)(1e-10 * K.H2);
+        }
+    }
     // the FP64 work of one candidate: the exact test, grad W, the list entry
     // and the M sum
     auto pair = [&](int j) {
+        if constexpr (sizeof(R) == 4) {
+            if (use_df) {
+                const float4 oj = posd[j];
+                if (pre_ok(make_float2(oj.x, oj.z), csf)) {
+                    const int cj = pcell[j], cxj = cj / K.ny, cyj = cj - cxj * K.ny;
+                    const df2 ddx = df_pair_offset(oxi, make_float2(oj.x, oj.y), cx - cxj, cs_df);
+                    const df2 ddy = df_pair_offset(oyi, make_float2(oj.z, oj.w), cy - cyj, cs_df);
+                    const df2 r2 = df_add(df_sqr(ddx), df_sqr(ddy));
+                    const float side = df_sub(r2, T_df).hi;
+                    bool in = side < -band;
+                    if (!in && !(side > band)) {  // within the band: the FP64 predicate decides
+                        const double dx = xi - S.x[j], dy = yi - S.y[j];
+                        in = nonneg_below(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), K.H2x);
+                    }
+                    if (!in) return;
+                    const df2 r = r2.hi > 0.f ? df_sqrt(r2) : df2{0.f, 0.f};
+                    const df2 a = df_sub(df2{1.f, 0.f}, df_mul(r, hih));
+                    const df2 F = df_mul(df_mul(mwF, a), df_sqr(a));  // -F_W (1 - r/2h)^3
+                    const df2 gx = df_mul(F, ddx), gy = df_mul(F, ddy);
+                    if (count < K.kmax) {
+                        const int64_t e = ell(i, count, K.kmax);
+                        nbr[e] = j;
+                        gw[e] = {df_to_double(gx), df_to_double(gy)};
+                        gwf[e] = {gx.hi, gy.hi};
+                        if (ndist) ndist[e] = df_to_double(r);
+                    }
+                    ++count;
+                    const float vj = f_vol[j];
+                    const float rx = -vj * ddx.hi, ry = -vj * ddy.hi;  // m_j (x_j - x_i) / rho_j
+                    m0 += gx.hi * rx;
+                    m1 += gy.hi * rx;
+                    m2 += gx.hi * ry;
+                    m3 += gy.hi * ry;
+                    return;
+                }
+            }
+        }
         const double dx = xi - S.x[j], dy = yi - S.y[j];
         const double d2 = __dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy));
         // exactly sqrt(d2) < 2h, no FMA contraction; the comparison on the
@@ -298,7 +370,7 @@ __global__ void __launch_bounds__(WC_WARPS * 32) k_cand_warpcell(int ncell, KPar
 
 int op_neighbour(Ctx* c) {
     k_posf<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S.x, c->S.y, c->pcell, c->K, c->posf, c->S.vol,
-                                                         c->mixed ? c->f_vol : nullptr);
+                                                         c->mixed ? c->f_vol : nullptr, c->mixed ? c->posd : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     StageTimer tk(c, BSC_T_K_NEIGHBOUR);
@@ -309,20 +381,20 @@ int op_neighbour(Ctx* c) {
         BSC_LAUNCH(c);
         if (c->mixed)
             k_neighbour<float, true><<<g, NB_BLOCK, 0, c->stream>>>(
-                c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, c->nbr, c->gw, c->gwf,
-                c->f_vol, c->ndist, c->cnt, c->d_flag, c->cand_nc);
+                c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, c->posd, c->nbr, c->gw,
+                c->gwf, c->f_vol, c->ndist, c->cnt, c->d_flag, c->cand_nc);
         else
             k_neighbour<double, true><<<g, NB_BLOCK, 0, c->stream>>>(
-                c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, c->nbr, c->gw, nullptr,
-                nullptr, c->ndist, c->cnt, c->d_flag, c->cand_nc);
+                c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, nullptr, c->nbr, c->gw,
+                nullptr, nullptr, c->ndist, c->cnt, c->d_flag, c->cand_nc);
     } else if (c->mixed)
         k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
-                                                          c->pcell, c->posf, c->nbr, c->gw, c->gwf, c->f_vol, c->ndist,
-                                                          c->cnt, c->d_flag);
+                                                          c->pcell, c->posf, c->posd, c->nbr, c->gw, c->gwf, c->f_vol,
+                                                          c->ndist, c->cnt, c->d_flag);
     else
         k_neighbour<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count,
-                                                           c->sorted, c->pcell, c->posf, c->nbr, c->gw, nullptr,
-                                                           nullptr, c->ndist, c->cnt, c->d_flag);
+                                                           c->sorted, c->pcell, c->posf, nullptr, c->nbr, c->gw,
+                                                           nullptr, nullptr, c->ndist, c->cnt, c->d_flag);
     BSC_LAUNCH(c);
     c->have_lists = true;
     return BSC_OK;

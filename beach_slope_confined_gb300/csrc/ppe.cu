@@ -166,16 +166,6 @@ __global__ void k_asm_df_pre(int64_t n, State S, KParams K, const int32_t* __res
     pre[4 * n + i] = df_pack(df_of(1.0 + S.oden[i] * (1.0 / (K.rho0 * K.rel_den))));
 }
 
-// x_i - x_j from the offsets and the cells' column (row) difference k:
-// (o_i - o_j) + k cs
-__device__ __forceinline__ df2 df_pair_offset(df2 oi, float2 oj, int k, df2 cs) {
-    df2 d = df_sub(oi, df_unpack(oj));
-    if (k == 1) d = df_add(d, cs);
-    else if (k == -1) d = df_sub(d, cs);
-    else if (k != 0) d = df_add(d, df_mul(cs, df2{(float)k, 0.0f}));
-    return d;
-}
-
 __global__ void __launch_bounds__(NB_BLOCK) k_assemble_df(int64_t n, State S, KParams K,
                                                            const int32_t* __restrict__ nbr,
                                                            const double2* __restrict__ gw,

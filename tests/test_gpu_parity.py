@@ -228,3 +228,37 @@ def test_warp_per_cell_search_gives_the_same_steps(precision):
     assert np.array_equal(oa, ob) and np.array_equal(ia, ib)
     for f in ("x", "y", "vx", "vy", "p", "nut", "porosity"):
         assert np.array_equal(a[f], b[f]), f
+
+
+@pytest.mark.parametrize("kernel", [1, 0])
+def test_mixed_neighbour_sets_equal_fp64_same_state(kernel):
+    """The mixed search decides membership from a double-float r^2 and takes
+    the exact FP64 test only within 1e-10 of the threshold (Wendland C2; the
+    reference's hybrid kernel keeps the FP64 test throughout).  The same
+    moving state, uploaded into an FP64 and a mixed context, gives the same
+    neighbour sets, bit for bit."""
+    spec = small_spec(dx=0.01, kernel=kernel, piston_ramp=0.0)
+    scen = sc.build(spec)
+    P64 = sc.make_params(spec, scen.bounds, precision="fp64", tol=1e-8, maxit=20000, precond="mg")
+    g = Solver(P64)
+    from beach_slope_confined_gb300 import setup_tank
+
+    setup_tank(g, scen)
+    g.step(3)
+    state = g.download_state()
+    t, dt = g.get_time()
+    g.close()
+    out = {}
+    for prec in ("fp64", "mixed"):
+        P = sc.make_params(spec, scen.bounds, precision=prec, tol=1e-8, maxit=20000, precond="mg")
+        h = Solver(P)
+        setup_tank(h, scen)
+        h.upload_state(state)
+        h.set_time(t, dt)
+        h.cellshift()
+        h.resetid()
+        h.neighbour()
+        out[prec] = h.get_neighbors()
+        h.close()
+    assert np.array_equal(out["fp64"][0], out["mixed"][0])
+    assert np.array_equal(out["fp64"][1], out["mixed"][1])
