@@ -272,6 +272,11 @@ struct Ctx {
     // as much as an FP64 add)
     float *f_vol = nullptr, *f_nu = nullptr, *f_nut = nullptr, *f_tke = nullptr, *f_varts = nullptr,
           *f_q = nullptr;
+    // the low part of V as a double-float {f_vol, f_vol_lo}, beside f_vol
+    float* f_vol_lo = nullptr;
+    // u = v/n as double-floats (hi x, lo x, hi y, lo y): eddyvis and varts
+    // take their velocity differences from them on the FP32 pipe
+    float4* udf = nullptr;
     // solids: their own cell list, static after upload
     double *sx = nullptr, *sy = nullptr, *svol = nullptr, *spor = nullptr;
     int32_t *scell_start = nullptr, *scell_count = nullptr;
@@ -282,10 +287,13 @@ struct Ctx {
 
     // neighbour lists
     int32_t* nbr = nullptr;
-    double2* gw = nullptr;        // FP64 grad W
+    double2* gw = nullptr;        // FP64 grad W (the FP64 path; the mixed path's FP64 assembly variants)
     double* ndist = nullptr;      // pair distance per slot (salinity: scalart's radial)
     double* sdisp = nullptr;      // salinity: D_x, D_y, Dm + nu_t/Sc, 1/n per particle (4n)
-    float2* gwf = nullptr;        // FP32 grad W (mixed)
+    // mixed path: grad W as a double-float, {gwf, gwl} (gwf alone is its FP32
+    // rounding, which the FP32 pair sums read)
+    float2* gwf = nullptr;
+    float2* gwl = nullptr;
     float2* asm_df = nullptr;     // mixed assembly: five per-particle double-float inputs
     float4* posd = nullptr;       // mixed search: offsets to the cell origin as double-floats
     bool asm_rcp = false;         // mixed assembly in FP64 with Newton reciprocals (BSC_ASSEMBLY=rcp)
@@ -329,6 +337,13 @@ struct Ctx {
     bool prof_iter = false;       // BSC_PROFILE_ITER=1: events around each Krylov kernel
     int mg_tail_cells = -1;       // BSC_MG_TAIL=<cells>: largest level in the single-CTA tail
     double mg_w[2] = {0.82, 0.82};  // smoother weights: the first sweep of a pre/post pair, the later ones
+    // post-sweeps on the cell levels and on the particle level (0:
+    // mg_sweeps) and the first post-sweep's weight (0: mg_w[0]); pre-sweeps
+    // on the particle level (0: mg_sweeps).  Defaults set at create;
+    // BSC_MG_POST=<coarse>,<fine>[,<w>] and BSC_MG_PRE=<n> override them
+    int mg_post[2] = {0, 0};
+    int mg_pre_fine = 0;
+    double mg_wpost = 0.0;
     bool exact_div = false;       // BSC_EXACT_DIV=1: IEEE divisions in the mixed path's FP64 assembly
     cudaEvent_t ev_it[6] = {};
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64

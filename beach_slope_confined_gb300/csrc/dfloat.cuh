@@ -52,6 +52,13 @@ __device__ __forceinline__ df2 df_add(df2 a, df2 b) {
 
 __device__ __forceinline__ df2 df_sub(df2 a, df2 b) { return df_add(a, df_neg(b)); }
 
+// a + b for an FP32 b: the TwoSum of the high parts, a.lo carried
+__device__ __forceinline__ df2 df_add_f(df2 a, float b) {
+    df2 s = df_two_sum(a.hi, b);
+    s.lo = __fadd_rn(s.lo, a.lo);
+    return df_quick_two_sum(s.hi, s.lo);
+}
+
 // a * b: the exact product of the high parts (TwoProduct by FMA) plus the
 // cross terms
 __device__ __forceinline__ df2 df_mul(df2 a, df2 b) {

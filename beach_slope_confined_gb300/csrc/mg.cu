@@ -416,8 +416,9 @@ struct TailLevel {
 };
 template <typename T>
 struct TailArgs {
-    int l0, nlev, nu, smem;
+    int l0, nlev, nu, nu_post, smem;
     T w, w1, scale;  // weights of the first and of the later sweeps
+    T wpost;         // weight of the first post-sweep
     const T* cinv;
     const Scalars* sk;
     TailLevel<T> L[MG_MAX_LEVELS + 1];
@@ -455,7 +456,8 @@ template <typename T>
 __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* tail_sm, const Scalars* sk) {
     const int t = threadIdx.x, NT = blockDim.x;
     const T w = P.w, w1 = P.w1, sc = P.scale;
-    const int nu = P.nu;
+    const int nu = P.nu, nup = P.nu_post;
+    const T wp = P.wpost;
     // level q as the phases see it: in global memory, or staged
     auto lv = [&](int q) -> TailLevel<T> {
         TailLevel<T> L = P.L[q];
@@ -525,10 +527,10 @@ __device__ __forceinline__ void tail_body(const TailArgs<T>& P, unsigned char* t
         const TailLevel<T> C = lv(l + 1);
         const int64_t nc = (int64_t)L.nx * L.ny;
         T* c0 = cur[l];
-        for (int k = 0; k < nu; ++k) {
-            T* out = (k == nu - 1) ? L.x : (c0 == L.y ? L.t : L.y);
+        for (int k = 0; k < nup; ++k) {
+            T* out = (k == nup - 1) ? L.x : (c0 == L.y ? L.t : L.y);
             for (int c = t; c < nc; c += NT)
-                out[c] = k == 0 ? smooth_at<T, 2>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, C.x, C.ny, sc, w)
+                out[c] = k == 0 ? smooth_at<T, 2>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, C.x, C.ny, sc, wp)
                                 : smooth_at<T, 0>(L.nx, L.ny, c, L.A, L.dinv, L.b, c0, nullptr, 0, sc, w1);
             __syncthreads();
             c0 = out;
@@ -677,12 +679,15 @@ int cycle_level(Ctx* c, int l) {
     Lv<T> v = level_view<T>(L);
     const unsigned g = blocks_for(L.nc, MG_BLOCK);
     const T w = (T)c->mg_w[0], w1 = (T)c->mg_w[1], sc = (T)c->P.mg_scale;
-    const int nu = c->P.mg_sweeps;
+    const T wp = c->mg_wpost > 0 ? (T)c->mg_wpost : w;
+    const int nu = c->P.mg_sweeps, nup = c->mg_post[0] > 0 ? c->mg_post[0] : nu;
     if (l >= mg.tail_l0) {  // this level and all coarser ones in one CTA
         TailArgs<T> P{};
         P.l0 = l;
         P.nlev = mg.nlev;
         P.nu = nu;
+        P.nu_post = nup;
+        P.wpost = wp;
         P.w = w;
         P.w1 = w1;
         P.scale = sc;
@@ -735,10 +740,10 @@ int cycle_level(Ctx* c, int l) {
     if (int rc = cycle_level<T>(c, l + 1)) return rc;
     // post-smoothing: the prolongation folded into the first sweep; the last
     // sweep writes x_l
-    for (int k = 0; k < nu; ++k) {
-        T* out = (k == nu - 1) ? v.x : (cur == v.y ? v.t : v.y);
+    for (int k = 0; k < nup; ++k) {
+        T* out = (k == nup - 1) ? v.x : (cur == v.y ? v.t : v.y);
         if (k == 0)
-            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w, w,
+            k_mg_smooth<T, 2><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, wp, wp,
                                                               out, c->mg.skip);
         else
             k_mg_smooth<T, 0><<<g, MG_BLOCK, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, nullptr, 0, sc, w1, w1,
@@ -757,7 +762,8 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
     using AV = typename FineOp<T>::type;  // the fine operator's type
     const AV A = fine_op<T>(c);
     const T w = (T)c->mg_w[0], w1 = (T)c->mg_w[1], sc = (T)c->P.mg_scale;
-    const int nu = c->P.mg_sweeps;
+    const T wp = c->mg_wpost > 0 ? (T)c->mg_wpost : w;
+    const int nu = c->P.mg_sweeps, nup = c->mg_post[1] > 0 ? c->mg_post[1] : nu;
     T *P0 = (T*)mg.y0, *Q0 = (T*)mg.t0, *R0 = (T*)mg.r0;
     // one row per thread: the fine-level passes have no reduction, and a full
     // grid keeps more rows' loads in flight than a grid-stride loop over a
@@ -765,12 +771,13 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
     const int G = (int)blocks_for(n, MG_BLOCK);
     if (c->prof_iter) record_event(c, c->ev_it[0]);
     T* cur = P0;
-    if (nu == 1)
+    const int nupre = c->mg_pre_fine > 0 ? c->mg_pre_fine : nu;
+    if (nupre == 1)
         k_mg0_scale<T, VI><<<G, MG_BLOCK, 0, c->stream>>>(n, vin, w, cur, c->mg.skip);
     else
         k_mg0_pre2<T, VI, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, w, w1, cur, c->mg.skip);
     BSC_LAUNCH(c);
-    for (int k = 2; k < nu; ++k) {
+    for (int k = 2; k < nupre; ++k) {
         T* out = cur == P0 ? Q0 : P0;
         k_mg0_sweep<T, VI, T, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w1, out, c->mg.skip);
         BSC_LAUNCH(c);
@@ -791,14 +798,14 @@ int vcycle(Ctx* c, const VI* vin, O* z) {
         rs = mg.rowslotsf;
     else
         rs = mg.rowslots;
-    for (int k = 0; k < nu; ++k) {
-        const bool last = k == nu - 1;
+    for (int k = 0; k < nup; ++k) {
+        const bool last = k == nup - 1;
         T* out = cur == P0 ? Q0 : P0;
         if (k == 0 && last)
-            k_mg0_post<T, O><<<G, MG_BLOCK, 0, c->stream>>>(n, L1.nx, L1.ny, cur, R0, v1.x, c->pcell, rs, sc, w, z,
+            k_mg0_post<T, O><<<G, MG_BLOCK, 0, c->stream>>>(n, L1.nx, L1.ny, cur, R0, v1.x, c->pcell, rs, sc, wp, z,
                                                             c->mg.skip);
         else if (k == 0)
-            k_mg0_post<T, T><<<G, MG_BLOCK, 0, c->stream>>>(n, L1.nx, L1.ny, cur, R0, v1.x, c->pcell, rs, sc, w,
+            k_mg0_post<T, T><<<G, MG_BLOCK, 0, c->stream>>>(n, L1.nx, L1.ny, cur, R0, v1.x, c->pcell, rs, sc, wp,
                                                             out, c->mg.skip);
         else if (last)
             k_mg0_sweep<T, VI, O, AV><<<G, MG_BLOCK, 0, c->stream>>>(n, A, vin, cur, w1, z, c->mg.skip);

@@ -48,17 +48,23 @@ __device__ __forceinline__ bool pre_ok(float2 p, float csf) {
     return fabsf(p.x) < PRE_GUARD * csf && fabsf(p.y) < PRE_GUARD * csf;
 }
 
-// (mixed path: also the FP32 twin of V for the neighbour search's M sum)
-// (mixed path: also the offsets as double-floats, (hi x, lo x, hi y, lo y))
+// (mixed path: also V as a double-float, {f_vol, f_vol_lo}: its FP32 twin
+// for the neighbour search's M sum; and the offsets as double-floats,
+// (hi x, lo x, hi y, lo y))
 __global__ void k_posf(int64_t n, const double* __restrict__ x, const double* __restrict__ y,
                        const int32_t* __restrict__ pcell, KParams K, float2* __restrict__ posf,
-                       const double* __restrict__ vol, float* __restrict__ f_vol, float4* __restrict__ posd) {
+                       const double* __restrict__ vol, float* __restrict__ f_vol, float* __restrict__ f_vol_lo,
+                       float4* __restrict__ posd) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const int c = pcell[i], cx = c / K.ny, cy = c - cx * K.ny;
     const double ox = x[i] - (K.gx0 + cx * K.cs), oy = y[i] - (K.gy0 + cy * K.cs);
     posf[i] = make_float2((float)ox, (float)oy);
-    if (f_vol) f_vol[i] = (float)vol[i];
+    if (f_vol) {
+        const df2 vd = df_of(vol[i]);
+        f_vol[i] = vd.hi;
+        f_vol_lo[i] = vd.lo;
+    }
     if (posd) {
         const df2 dx = df_of(ox), dy = df_of(oy);
         posd[i] = make_float4(dx.hi, dx.lo, dy.hi, dy.lo);
@@ -78,7 +84,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                                                          const float2* __restrict__ posf,
                                                          const float4* __restrict__ posd,
                                                          int32_t* __restrict__ nbr, double2* __restrict__ gw,
-                                                         float2* __restrict__ gwf, const float* __restrict__ f_vol,
+                                                         float2* __restrict__ gwf, float2* __restrict__ gwl,
+                                                         const float* __restrict__ f_vol,
                                                          double* __restrict__ ndist, int32_t* __restrict__ cnt,
                                                          int32_t* __restrict__ flag,
                                                          const int32_t* __restrict__ cand_nc = nullptr) {
@@ -144,8 +151,11 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
                     if (count < K.kmax) {
                         const int64_t e = ell(i, count, K.kmax);
                         nbr[e] = j;
-                        gw[e] = {df_to_double(gx), df_to_double(gy)};
+                        // grad W stored as the double-float it is; the FP64
+                        // copy only for the FP64 assembly variants
+                        if (gw) gw[e] = {df_to_double(gx), df_to_double(gy)};
                         gwf[e] = {gx.hi, gy.hi};
+                        if (gwl) gwl[e] = {gx.lo, gy.lo};
                         if (ndist) ndist[e] = df_to_double(r);
                     }
                     ++count;
@@ -179,8 +189,14 @@ __global__ void __launch_bounds__(NB_BLOCK) k_neighbour(int64_t n, State S, KPar
         if (count < K.kmax) {
             const int64_t e = ell(i, count, K.kmax);
             nbr[e] = j;
-            gw[e] = {gx64, gy64};
-            if (gwf) gwf[e] = {(float)gx, (float)gy};
+            if (gw) gw[e] = {gx64, gy64};
+            if (gwl) {  // the mixed path's double-float grad W (hi: the FP32 rounding)
+                const df2 ax = df_of(gx64), ay = df_of(gy64);
+                gwf[e] = {ax.hi, ay.hi};
+                gwl[e] = {ax.lo, ay.lo};
+            } else if (gwf) {
+                gwf[e] = {(float)gx, (float)gy};
+            }
             if (ndist) ndist[e] = r;
         }
         ++count;
@@ -370,9 +386,14 @@ __global__ void __launch_bounds__(WC_WARPS * 32) k_cand_warpcell(int ncell, KPar
 
 int op_neighbour(Ctx* c) {
     k_posf<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S.x, c->S.y, c->pcell, c->K, c->posf, c->S.vol,
-                                                         c->mixed ? c->f_vol : nullptr, c->mixed ? c->posd : nullptr);
+                                                         c->mixed ? c->f_vol : nullptr,
+                                                         c->mixed ? c->f_vol_lo : nullptr,
+                                                         c->mixed ? c->posd : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
+    // mixed path: grad W as a double-float only, unless an FP64 assembly
+    // variant (BSC_ASSEMBLY=rcp, BSC_EXACT_DIV=1) reads the FP64 copy
+    double2* gw64 = (c->asm_rcp || c->exact_div) ? c->gw : nullptr;
     StageTimer tk(c, BSC_T_K_NEIGHBOUR);
     if (c->nb_warpcell) {
         const unsigned gc = (unsigned)std::min<int64_t>((c->ncell + WC_WARPS - 1) / WC_WARPS, 152 * 32);
@@ -381,20 +402,20 @@ int op_neighbour(Ctx* c) {
         BSC_LAUNCH(c);
         if (c->mixed)
             k_neighbour<float, true><<<g, NB_BLOCK, 0, c->stream>>>(
-                c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, c->posd, c->nbr, c->gw,
-                c->gwf, c->f_vol, c->ndist, c->cnt, c->d_flag, c->cand_nc);
+                c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, c->posd, c->nbr, gw64,
+                c->gwf, c->gwl, c->f_vol, c->ndist, c->cnt, c->d_flag, c->cand_nc);
         else
             k_neighbour<double, true><<<g, NB_BLOCK, 0, c->stream>>>(
                 c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted, c->pcell, c->posf, nullptr, c->nbr, c->gw,
-                nullptr, nullptr, c->ndist, c->cnt, c->d_flag, c->cand_nc);
+                nullptr, nullptr, nullptr, c->ndist, c->cnt, c->d_flag, c->cand_nc);
     } else if (c->mixed)
         k_neighbour<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count, c->sorted,
-                                                          c->pcell, c->posf, c->posd, c->nbr, c->gw, c->gwf, c->f_vol,
-                                                          c->ndist, c->cnt, c->d_flag);
+                                                          c->pcell, c->posf, c->posd, c->nbr, gw64, c->gwf, c->gwl,
+                                                          c->f_vol, c->ndist, c->cnt, c->d_flag);
     else
         k_neighbour<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->cell_start, c->cell_count,
                                                            c->sorted, c->pcell, c->posf, nullptr, c->nbr, c->gw,
-                                                           nullptr, nullptr, c->ndist, c->cnt, c->d_flag);
+                                                           nullptr, nullptr, nullptr, c->ndist, c->cnt, c->d_flag);
     BSC_LAUNCH(c);
     c->have_lists = true;
     return BSC_OK;
@@ -431,7 +452,9 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
                                                       const float2* __restrict__ sposf,
                                                       const float* __restrict__ swf,
                                                       const double* __restrict__ svol,
-                                                      const double* __restrict__ spor) {
+                                                      const double* __restrict__ spor,
+                                                      float* __restrict__ f_vol = nullptr,
+                                                      float* __restrict__ f_vol_lo = nullptr) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     S.resist[i] = 0.0;
@@ -443,7 +466,10 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
     const float2 pi = make_float2((float)(xi - (K.gx0 + cx * K.cs)), (float)(yi - (K.gy0 + cy * K.cs)));
     const bool pre_i = pre_ok(pi, csf);
     R frac = 0;
-    double fsum = 0.0;  // mixed path: the FP64 sum of FP32 terms
+    // mixed path: the FP32 terms summed as a double-float (TwoSum on the FP32
+    // pipe; ~48 bits, more than the FP64 sum of FP32 terms needed, with no
+    // FP64 work inside the divergent candidate loop)
+    df2 fsum{0.0f, 0.0f};
     // the FP64 work of one solid: the exact test and its weighted W
     auto solid_term = [&](int s) {
         const double dx = xi - sx[s], dy = yi - sy[s];
@@ -510,12 +536,12 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
                             // Mixed path: each term in FP32 (W is continuous
                             // and vanishes at r = 2h, so the FP32 distance
                             // decides nothing that matters; weight
-                            // (1-n_s) V_s), the sum in FP64. The FP32 running
-                            // sum was the main error of the mixed velocities
-                            // (1.1e-6 against FP64 after the benchmark's
-                            // steps; 6.7e-7 with this sum, for one FP64 add
-                            // per term).
-                            if (r2f < (float)K.H2) fsum += f64_of(swf[s] * kern_w<float>(K, sqrtf(r2f)));
+                            // (1-n_s) V_s), the sum as a double-float. The
+                            // FP32 running sum was the main error of the mixed
+                            // velocities (1.1e-6 against FP64 after the
+                            // benchmark's steps; 6.7e-7 with a wide sum).
+                            if (r2f < (float)K.H2)
+                                fsum = df_add_f(fsum, swf[s] * kern_w<float>(K, sqrtf(r2f)));
                             continue;
                         }
                     }
@@ -524,7 +550,7 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
             }
         }
     }
-    double sf = (double)frac + fsum;
+    double sf = (double)frac + df_to_double(fsum);
     const double cap = 1.0 - porosity_at(K, xi, yi);
     if (sf > cap) sf = cap;
     const double nn = 1.0 - sf;
@@ -533,6 +559,11 @@ __global__ void __launch_bounds__(NB_BLOCK) k_effpor(int64_t n, State S, KParams
     S.por[i] = nn;
     S.rho[i] = rho;
     S.vol[i] = S.mass[i] / rho;
+    if (f_vol) {  // mixed path: V's double-float twin follows V
+        const df2 vd = df_of(S.vol[i]);
+        f_vol[i] = vd.hi;
+        f_vol_lo[i] = vd.lo;
+    }
     // Ergun/Darcy-Forchheimer coefficient (porous.f90:192,204-212),
     // Fch*sqrt(lamk) written as beta/sqrt(n^3)
     if constexpr (sizeof(R) == 4) {
@@ -560,7 +591,8 @@ int op_effpor(Ctx* c) {
     StageTimer tk(c, BSC_T_K_EFFPOR);
     if (c->mixed)
         k_effpor<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
-                                                       c->sx, c->sy, c->sposf, c->swf, c->svol, c->spor);
+                                                       c->sx, c->sy, c->sposf, c->swf, c->svol, c->spor, c->f_vol,
+                                                       c->f_vol_lo);
     else
         k_effpor<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, c->scell_start, c->scell_count,
                                                         c->sx, c->sy, c->sposf, c->swf, c->svol, c->spor);
@@ -569,15 +601,27 @@ int op_effpor(Ctx* c) {
 }
 
 // per-particle quotients shared by the pair loops: u = v/n (eddyvis, int_vel)
-// (mixed path: also the FP32 twin of V)
+// (mixed path: also the FP32 twin of V and u as double-floats)
 __global__ void k_vel_over_por(int64_t n, State S, double* __restrict__ ux, double* __restrict__ uy,
-                               float* __restrict__ f_vol) {
+                               float* __restrict__ f_vol, float4* __restrict__ udf) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double nn = S.por[i];
-    ux[i] = S.vx[i] / nn;
-    uy[i] = S.vy[i] / nn;
+    const double a = S.vx[i] / nn, b = S.vy[i] / nn;
+    ux[i] = a;
+    uy[i] = b;
     if (f_vol) f_vol[i] = (float)S.vol[i];
+    if (udf) {
+        const df2 ad = df_of(a), bd = df_of(b);
+        udf[i] = make_float4(ad.hi, ad.lo, bd.hi, bd.lo);
+    }
+}
+
+// u_j - u_i from the double-float twins, rounded to FP32: the FP32 rounding
+// of the FP64 difference to ~2^-48 of |u| (the differences cancel, so they
+// must not come from FP32 roundings of u), on the FP32 pipe
+__device__ __forceinline__ float2 udf_diff(float4 uj, float4 ui) {
+    return make_float2(df_sub(df2{uj.x, uj.y}, df2{ui.x, ui.y}).hi, df_sub(df2{uj.z, uj.w}, df2{ui.z, ui.w}).hi);
 }
 
 // ---- turbulence.f90:12-110 eddyvis -----------------------------------------------
@@ -585,11 +629,13 @@ template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                        const typename Vec2<R>::type* __restrict__ gw,
                                                        const int32_t* __restrict__ cnt, const double* __restrict__ ux,
-                                                       const double* __restrict__ uy, const float* __restrict__ f_vol) {
+                                                       const double* __restrict__ uy, const float* __restrict__ f_vol,
+                                                       const float4* __restrict__ udf) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || S.tid[i] != BSC_TID_FLUID) return;
     const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
     const double uxi = ux[i], uyi = uy[i];
+    [[maybe_unused]] const float4 udi = sizeof(R) == 4 ? udf[i] : float4{};
     R t1 = 0, t2 = 0, t3 = 0;
     const int m = cnt[i];
     for (int k = 0; k < m; ++k) {
@@ -601,9 +647,17 @@ __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParam
             vj = f_vol[j];
         else
             vj = S.vol[j];
-        // differences in FP64 (they cancel), rounded on the integer pipe for R = float
-        const R du = sizeof(R) == 4 ? (R)f32_of(ux[j] - uxi) : (R)(ux[j] - uxi);
-        const R dv = sizeof(R) == 4 ? (R)f32_of(uy[j] - uyi) : (R)(uy[j] - uyi);
+        // differences in FP64 (they cancel); for R = float in double-float
+        // arithmetic, rounded
+        R du, dv;
+        if constexpr (sizeof(R) == 4) {
+            const float2 d = udf_diff(udf[j], udi);
+            du = d.x;
+            dv = d.y;
+        } else {
+            du = ux[j] - uxi;
+            dv = uy[j] - uyi;
+        }
         const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
         t1 += vj * du * gx;
         t2 += vj * dv * gy;
@@ -619,13 +673,16 @@ __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParam
 int op_eddyvis(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "eddyvis before neighbour");
     double *ux = c->r, *uy = c->rh;  // Krylov work vectors double as scratch outside the solve
-    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy, c->mixed ? c->f_vol : nullptr);
+    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy, c->mixed ? c->f_vol : nullptr,
+                                                                 c->mixed ? c->udf : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
-        k_eddyvis<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy, c->f_vol);
+        k_eddyvis<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy, c->f_vol,
+                                                        c->udf);
     else
-        k_eddyvis<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy, nullptr);
+        k_eddyvis<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy, nullptr,
+                                                         nullptr);
     BSC_LAUNCH(c);
     return BSC_OK;
 }
@@ -637,11 +694,13 @@ __global__ void __launch_bounds__(NB_BLOCK) k_varts(int64_t n, State S, KParams 
                                                      const typename Vec2<R>::type* __restrict__ gw,
                                                      const int32_t* __restrict__ cnt, const double* __restrict__ ux,
                                                      const double* __restrict__ uy, const double* __restrict__ umax,
-                                                     const float* __restrict__ f_vol, float* __restrict__ f_varts) {
+                                                     const float* __restrict__ f_vol, float* __restrict__ f_varts,
+                                                     const float4* __restrict__ udf) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n || !(S.flags[i] & BSC_FLAG_FREE)) return;
     const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
     const double uxi = ux[i], uyi = uy[i];
+    [[maybe_unused]] const float4 udi = sizeof(R) == 4 ? udf[i] : float4{};
     R t1 = 0, t2 = 0;
     const int m = cnt[i];
     for (int k = 0; k < m; ++k) {
@@ -653,8 +712,15 @@ __global__ void __launch_bounds__(NB_BLOCK) k_varts(int64_t n, State S, KParams 
             vj = f_vol[j];
         else
             vj = S.vol[j];
-        const R du = sizeof(R) == 4 ? (R)f32_of(ux[j] - uxi) : (R)(ux[j] - uxi);
-        const R dv = sizeof(R) == 4 ? (R)f32_of(uy[j] - uyi) : (R)(uy[j] - uyi);
+        R du, dv;
+        if constexpr (sizeof(R) == 4) {
+            const float2 d = udf_diff(udf[j], udi);
+            du = d.x;
+            dv = d.y;
+        } else {
+            du = ux[j] - uxi;
+            dv = uy[j] - uyi;
+        }
         t1 += du * (L0 * g.x + L1 * g.y) * vj;
         t2 += dv * (L2 * g.x + L3 * g.y) * vj;
     }
@@ -673,7 +739,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
                                                        const int32_t* __restrict__ cnt,
                                                        const double* __restrict__ nu, double dt, const float* __restrict__ f_vol,
                                                        const float* __restrict__ f_nu, const float* __restrict__ f_nut,
-                                                       const float* __restrict__ f_tke, const float* __restrict__ f_varts) {
+                                                       const float* __restrict__ f_tke, const float* __restrict__ f_varts,
+                                                       const float2* __restrict__ posf, const int32_t* __restrict__ pcell) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     constexpr bool F32 = sizeof(R) == 4;  // FP32 sums: the per-particle fields come from their FP32 twins
@@ -681,6 +748,24 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
     if (S.tid[i] == BSC_TID_FLUID && !(fi & (BSC_FLAG_BUFFER | BSC_FLAG_DEAD))) {
         const R L0 = to_r<R>(S.L0[i]), L1 = to_r<R>(S.L1[i]), L2 = to_r<R>(S.L2[i]), L3 = to_r<R>(S.L3[i]);
         const double xi = S.x[i], yi = S.y[i], vxi = S.vx[i], vyi = S.vy[i];
+        // FP32 path: the pair offsets from the particles' FP32 offsets to
+        // their cells' origins (as the neighbour search wrote them) and the
+        // cells' column and row differences,
+        // the velocity differences from FP32 roundings of the velocities
+        // (their error, ~1e-7 of |v| per difference, reaches v* through
+        // dt nu / h^2 ~ 1e-3): no FP64 operation per pair
+        [[maybe_unused]] float2 pfi{};
+        [[maybe_unused]] int cxi = 0, cyi = 0;
+        [[maybe_unused]] float vxif = 0.f, vyif = 0.f;
+        [[maybe_unused]] const float csf = (float)K.cs;
+        if constexpr (F32) {
+            pfi = posf[i];
+            const int ci = pcell[i];
+            cxi = ci / K.ny;
+            cyi = ci - cxi * K.ny;
+            vxif = f32_of(vxi);
+            vyif = f32_of(vyi);
+        }
         const R nui = to_r<R>(nu[i]), nuti = to_r<R>(S.nut[i]), tkei = to_r<R>(S.tke[i]), ni = to_r<R>(S.por[i]);
         const bool free_i = fi & BSC_FLAG_FREE;
         const R varts_i = to_r<R>(S.varts[i]);
@@ -700,16 +785,21 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
             } else {
                 cmu = nui;
             }
-            const double dx = xi - S.x[j], dy = yi - S.y[j];
-            // on the FP32 path: offsets rounded on the integer pipe (f32_of),
-            // r^2 from them (the accuracy of rounding the FP64 r^2, without
-            // the FP64 products)
-            const R fx = F32 ? (R)f32_of(dx) : (R)dx, fy = F32 ? (R)f32_of(dy) : (R)dy;
-            R r2;
-            if constexpr (F32)
+            R fx, fy, r2;
+            [[maybe_unused]] double dx = 0.0, dy = 0.0;
+            if constexpr (F32) {
+                const float2 pfj = posf[j];
+                const int cj = pcell[j], cxj = cj / K.ny, cyj = cj - cxj * K.ny;
+                fx = (pfi.x - pfj.x) + (float)(cxi - cxj) * csf;
+                fy = (pfi.y - pfj.y) + (float)(cyi - cyj) * csf;
                 r2 = fx * fx + fy * fy;
-            else
+            } else {
+                dx = xi - S.x[j];
+                dy = yi - S.y[j];
+                fx = dx;
+                fy = dy;
                 r2 = dx * dx + dy * dy;
+            }
             R vart = 0;
             if (free_i) {
                 vart = varts_i;
@@ -725,9 +815,14 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
             const R p_dist = (R)1 / (r2 + (R)K.lam);
             const R gx = L0 * g.x + L1 * g.y, gy = L2 * g.x + L3 * g.y;
             const R geo = (R)2 * pvol * (fx * gx + fy * gy) * p_dist;
-            // FP64 differences (they cancel), then rounded
-            const R dvx = F32 ? (R)f32_of(vxi - S.vx[j]) : (R)(vxi - S.vx[j]);
-            const R dvy = F32 ? (R)f32_of(vyi - S.vy[j]) : (R)(vyi - S.vy[j]);
+            R dvx, dvy;
+            if constexpr (F32) {
+                dvx = vxif - f32_of(S.vx[j]);
+                dvy = vyif - f32_of(S.vy[j]);
+            } else {
+                dvx = vxi - S.vx[j];
+                dvy = vyi - S.vy[j];
+            }
             R visc = cmu + vart;
             if (fluid_j) {
                 const R nutj = F32 ? (R)f_nut[j] : (R)S.nut[j];
@@ -784,14 +879,15 @@ int op_int_vel(Ctx* c, const double* d_umax) {
     double *ux = c->r, *uy = c->rh, *nu = c->pd;
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     const bool mx = c->mixed;
-    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy, mx ? c->f_vol : nullptr);
+    k_vel_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, ux, uy, mx ? c->f_vol : nullptr,
+                                                                 mx ? c->udf : nullptr);
     BSC_LAUNCH(c);
     if (mx)
         k_varts<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, ux, uy, d_umax,
-                                                      c->f_vol, c->f_varts);
+                                                      c->f_vol, c->f_varts, c->udf);
     else
         k_varts<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, ux, uy, d_umax,
-                                                       nullptr, nullptr);
+                                                       nullptr, nullptr, nullptr);
     BSC_LAUNCH(c);
     k_kin_visc<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, nu, mx ? c->f_nu : nullptr,
                                                              mx ? c->f_nut : nullptr, mx ? c->f_tke : nullptr);
@@ -799,10 +895,12 @@ int op_int_vel(Ctx* c, const double* d_umax) {
     StageTimer tk(c, BSC_T_K_INT_VEL);
     if (mx)
         k_int_vel<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->cnt, nu, c->dt,
-                                                        c->f_vol, c->f_nu, c->f_nut, c->f_tke, c->f_varts);
+                                                        c->f_vol, c->f_nu, c->f_nut, c->f_tke, c->f_varts, c->posf,
+                                                        c->pcell);
     else
         k_int_vel<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, nu, c->dt,
-                                                         nullptr, nullptr, nullptr, nullptr, nullptr);
+                                                         nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                                                         nullptr);
     BSC_LAUNCH(c);
     return BSC_OK;
 }
@@ -810,14 +908,16 @@ int op_int_vel(Ctx* c, const double* d_umax) {
 // ---- integrator.f90:715-865 comp_vel (comp_pos is separate, cells.cu) ---------------
 // (mixed path: also the FP32 twins of q and V)
 __global__ void k_rho_over_por(int64_t n, State S, double* __restrict__ q, float* __restrict__ f_q,
-                               float* __restrict__ f_vol) {
+                               float* __restrict__ f_vol, float* __restrict__ f_vol_lo) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double v = S.rho[i] / S.por[i];
     q[i] = v;
     if (f_q) {
         f_q[i] = (float)v;
-        f_vol[i] = (float)S.vol[i];
+        const df2 vd = df_of(S.vol[i]);
+        f_vol[i] = vd.hi;
+        f_vol_lo[i] = vd.lo;
     }
 }
 
@@ -872,14 +972,16 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel(int64_t n, State S, KPara
 //   fluid j: (p_j q_i + p_i q_j)/(q_i+q_j) = p_i + q_i (p_j - p_i)/(q_i+q_j)
 //   wall j:  p_j + p_i = 2 p_i + (p_j - p_i)
 // so a_i = c0 [ 2 p_i sum_j V_j g_j  +  sum_j w_j (p_j - p_i) g_j ]; the first
-// (cancelling) sum runs in FP64, the second (difference) sum in FP32.
+// (cancelling) sum runs in double-float arithmetic from the double-float V
+// and grad W (~48 bits, on the FP32 pipe), the second (difference) sum in FP32.
 __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S, KParams K,
                                                               const int32_t* __restrict__ nbr,
-                                                              const double2* __restrict__ gw,
                                                               const float2* __restrict__ gwf,
+                                                              const float2* __restrict__ gwl,
                                                               const int32_t* __restrict__ cnt,
                                                               const float* __restrict__ f_q,
-                                                              const float* __restrict__ f_vol, double dt) {
+                                                              const float* __restrict__ f_vol,
+                                                              const float* __restrict__ f_vol_lo, double dt) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint8_t fi = S.flags[i];
@@ -888,23 +990,23 @@ __global__ void __launch_bounds__(NB_BLOCK) k_comp_vel_mixed(int64_t n, State S,
         const float L0f = f32_of(L0), L1f = f32_of(L1), L2f = f32_of(L2), L3f = f32_of(L3);
         const double pi = S.p[i];
         const float qi = f_q[i];
-        double sx = 0.0, sy = 0.0;
+        df2 sxd{0.f, 0.f}, syd{0.f, 0.f};
         float ax = 0.f, ay = 0.f;
         const int m = cnt[i];
         for (int k = 0; k < m; ++k) {
             const int64_t e = ell(i, k, K.kmax);
             const int j = nbr[e];
-            const double2 g = gw[e];
-            const float2 gf = gwf[e];
-            const double vj = S.vol[j];
-            sx += vj * g.x;  // sum V grad W; L applied after the loop
-            sy += vj * g.y;
+            const float2 gf = gwf[e], gl = gwl[e];
             const float vjf = f_vol[j];
+            const df2 vj{vjf, f_vol_lo[j]};
+            sxd = df_add(sxd, df_mul(vj, df2{gf.x, gl.x}));  // sum V grad W; L applied after the loop
+            syd = df_add(syd, df_mul(vj, df2{gf.y, gl.y}));
             const float w = (S.tid[j] == BSC_TID_FLUID) ? 2.f * vjf * qi / (qi + f_q[j]) : vjf;
             const float dp = f32_of(S.p[j] - pi);  // FP64 difference (pressures cancel), rounded on the integer pipe
             ax += w * dp * (L0f * gf.x + L1f * gf.y);
             ay += w * dp * (L2f * gf.x + L3f * gf.y);
         }
+        const double sx = df_to_double(sxd), sy = df_to_double(syd);
         const double hx = L0 * sx + L1 * sy, hy = L2 * sx + L3 * sy;
         const double ni = S.por[i], c0 = ni * ni / S.rho[i];
         const double vx = S.vxs[i] - dt * c0 * (2.0 * pi * hx + (double)ax);
@@ -926,12 +1028,13 @@ int op_comp_vel(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "comp_vel before neighbour");
     double* q = c->r;
     k_rho_over_por<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, q, c->mixed ? c->f_q : nullptr,
-                                                                 c->mixed ? c->f_vol : nullptr);
+                                                                 c->mixed ? c->f_vol : nullptr,
+                                                                 c->mixed ? c->f_vol_lo : nullptr);
     BSC_LAUNCH(c);
     const unsigned g = blocks_for(c->n, NB_BLOCK);
     if (c->mixed)
-        k_comp_vel_mixed<<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->gwf, c->cnt, c->f_q,
-                                                        c->f_vol, c->dt);
+        k_comp_vel_mixed<<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->gwl, c->cnt, c->f_q,
+                                                        c->f_vol, c->f_vol_lo, c->dt);
     else
         k_comp_vel<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, q, c->dt);
     BSC_LAUNCH(c);
@@ -945,14 +1048,18 @@ int op_comp_vel(Ctx* c) {
 // corrected with the unclamped shift and the corrected gradient.
 // R: type of the velocity-gradient sums of the Taylor correction.  The
 // position shift sum_j V_j grad W cancels to ~1e-3 of its terms inside the
-// fluid, so it stays FP64 on both paths.  The gradient sums only scale the
-// correction grad(v).delta, a fraction ~|delta|/L of v (1e-3 and below
-// here): on the mixed path they run in FP32 from FP64 velocity differences
-// (rounded on the integer pipe) and the FP32 grad W, so the kernel's FP64
-// work is four operations per pair instead of ten.
+// fluid: FP64 on the FP64 path, double-float (~48 bits, from the
+// double-float V and grad W) on the mixed path.  The gradient sums only
+// scale the correction grad(v).delta, a fraction ~|delta|/L of v (1e-3 and
+// below here): on the mixed path they run in FP32 from the FP32 roundings
+// of the velocities (taken on the integer pipe) and the FP32 grad W (an
+// error of ~1e-8 of v in the correction), so the kernel issues no FP64
+// operation per pair (ten on the FP64 path).
 template <typename R>
 __global__ void __launch_bounds__(NB_BLOCK) k_shift(int64_t n, State S, KParams K, const int32_t* __restrict__ nbr,
                                                      const double2* __restrict__ gw, const float2* __restrict__ gwf,
+                                                     const float2* __restrict__ gwl, const float* __restrict__ f_vol,
+                                                     const float* __restrict__ f_vol_lo,
                                                      const int32_t* __restrict__ cnt, int8_t* __restrict__ mark) {
     const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -968,23 +1075,28 @@ __global__ void __launch_bounds__(NB_BLOCK) k_shift(int64_t n, State S, KParams 
     // so L is applied once to the four sums of grad W (dv V) rather than per
     // pair
     double sx = 0, sy = 0;
+    [[maybe_unused]] df2 sxd{0.f, 0.f}, syd{0.f, 0.f};
+    [[maybe_unused]] const float vxif = f32_of(vxi), vyif = f32_of(vyi);
     R ax = 0, bx = 0, ay = 0, by = 0;
     for (int k = 0; k < m; ++k) {
         const int64_t e = ell(i, k, K.kmax);
         const int j = nbr[e];
-        const double2 g = gw[e];
-        const double vj = S.vol[j];
-        sx += g.x * vj;
-        sy += g.y * vj;
         R gx, gy, dvx, dvy;
         if constexpr (F32) {
-            const float2 gf = gwf[e];
-            const float vf = f32_of(vj);
+            const float2 gf = gwf[e], gl = gwl[e];
+            const float vf = f_vol[j];
+            const df2 vjd{vf, f_vol_lo[j]};
+            sxd = df_add(sxd, df_mul(df2{gf.x, gl.x}, vjd));
+            syd = df_add(syd, df_mul(df2{gf.y, gl.y}, vjd));
             gx = gf.x;
             gy = gf.y;
-            dvx = f32_of(S.vx[j] - vxi) * vf;
-            dvy = f32_of(S.vy[j] - vyi) * vf;
+            dvx = (f32_of(S.vx[j]) - vxif) * vf;
+            dvy = (f32_of(S.vy[j]) - vyif) * vf;
         } else {
+            const double2 g = gw[e];
+            const double vj = S.vol[j];
+            sx += g.x * vj;
+            sy += g.y * vj;
             gx = g.x;
             gy = g.y;
             dvx = (S.vx[j] - vxi) * vj;
@@ -994,6 +1106,10 @@ __global__ void __launch_bounds__(NB_BLOCK) k_shift(int64_t n, State S, KParams 
         bx += gy * dvx;
         ay += gx * dvy;
         by += gy * dvy;
+    }
+    if constexpr (F32) {
+        sx = df_to_double(sxd);
+        sy = df_to_double(syd);
     }
     const R tx1 = L0 * ax + L1 * bx, tx2 = L2 * ax + L3 * bx;
     const R ty1 = L0 * ay + L1 * by, ty2 = L2 * ay + L3 * by;
@@ -1023,16 +1139,20 @@ int op_opt2_shift(Ctx* c) {
     if (!c->have_lists) return set_err(c, BSC_E_INVALID, "opt2_shift before neighbour");
     int8_t* mark = (int8_t*)c->pslot;  // scratch: pslot is free between cell builds
     const unsigned g = blocks_for(c->n, NB_BLOCK);
-    // The position shift's sum is FP64 on both paths (with it in FP32 the
-    // mixed path's velocities moved by ~7e-6 from the FP64 path's after 8
-    // c3 steps, against ~1e-6 in FP64); on the mixed path the velocity
-    // gradient of the Taylor correction runs in FP32 (see k_shift)
+    // The position shift's sum is FP64 on the FP64 path and double-float on
+    // the mixed one (with it in FP32 the mixed path's velocities moved by
+    // ~7e-6 from the FP64 path's after 8 c3 steps, against ~1e-6 with a wide
+    // sum); on the mixed path the velocity gradient of the Taylor correction
+    // runs in FP32 (see k_shift).  V is the one effpor just wrote (with its
+    // double-float twin).
     {
         StageTimer tk(c, BSC_T_K_SHIFT);
         if (c->mixed)
-            k_shift<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->gwf, c->cnt, mark);
+            k_shift<float><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, nullptr, c->gwf, c->gwl,
+                                                          c->f_vol, c->f_vol_lo, c->cnt, mark);
         else
-            k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, nullptr, c->cnt, mark);
+            k_shift<double><<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, nullptr, nullptr,
+                                                           nullptr, nullptr, c->cnt, mark);
         BSC_LAUNCH(c);
     }
     k_shift_apply<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, mark);

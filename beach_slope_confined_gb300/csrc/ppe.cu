@@ -168,7 +168,8 @@ __global__ void k_asm_df_pre(int64_t n, State S, KParams K, const int32_t* __res
 
 __global__ void __launch_bounds__(NB_BLOCK) k_assemble_df(int64_t n, State S, KParams K,
                                                            const int32_t* __restrict__ nbr,
-                                                           const double2* __restrict__ gw,
+                                                           const float2* __restrict__ gwf,
+                                                           const float2* __restrict__ gwl,
                                                            const int32_t* __restrict__ cnt,
                                                            const int32_t* __restrict__ pcell,
                                                            const float2* __restrict__ pre, double* __restrict__ aval,
@@ -203,8 +204,9 @@ __global__ void __launch_bounds__(NB_BLOCK) k_assemble_df(int64_t n, State S, KP
     for (int k = 0; k < m; ++k) {
         const int64_t e = ell(i, k, K.kmax);
         const int j = nbr[e];
-        const double2 g64 = gw[e];
-        const df2 gxr = df_of(g64.x), gyr = df_of(g64.y);
+        // grad W as the neighbour search left it, a double-float
+        const float2 gh = gwf[e], gl = gwl[e];
+        const df2 gxr{gh.x, gl.x}, gyr{gh.y, gl.y};
         const int tid_j = S.tid[j];
         const int cj = pcell[j], cxj = cj / K.ny, cyj = cj - cxj * K.ny;
         const df2 dx = df_pair_offset(oxi, pox[j], cxi - cxj, cs);
@@ -331,8 +333,8 @@ int op_ppe_assemble(Ctx* c) {
         k_asm_df_pre<<<blocks_for(c->n, 256), 256, 0, c->stream>>>(c->n, c->S, c->K, c->pcell, q, c->asm_df);
         BSC_LAUNCH(c);
         StageTimer tk(c, BSC_T_K_ASSEMBLE);
-        k_assemble_df<<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gw, c->cnt, c->pcell, c->asm_df,
-                                                      c->aval, c->ellf, c->avalh, c->b, q, ux, uy, c->dt);
+        k_assemble_df<<<g, NB_BLOCK, 0, c->stream>>>(c->n, c->S, c->K, c->nbr, c->gwf, c->gwl, c->cnt, c->pcell,
+                                                      c->asm_df, c->aval, c->ellf, c->avalh, c->b, q, ux, uy, c->dt);
         BSC_LAUNCH(c);
     } else {
         StageTimer tk(c, BSC_T_K_ASSEMBLE);

@@ -49,7 +49,7 @@ sys.path.insert(0, ROOT)
 
 METRIC = "particle-steps/s at 1M (mixed vs FP64, PPE res 1e-8); adjoint/forward time"
 CONFIG = "c3"
-T_STEP, T_PPE_SOLVE, T_SPMV, T_SCALAR = 15, 8, 16, 24
+T_STEP, T_PPE_SOLVE, T_SPMV, T_UPLOAD, T_DOWNLOAD, T_SCALAR = 15, 8, 16, 17, 18, 24
 # single-kernel slots of bsc_timing (include/bsc.h)
 T_K_NEIGHBOUR, T_K_ASSEMBLE, T_K_INT_VEL, T_K_EFFPOR, T_K_SHIFT = 25, 26, 27, 28, 29
 
@@ -57,22 +57,48 @@ T_K_NEIGHBOUR, T_K_ASSEMBLE, T_K_INT_VEL, T_K_EFFPOR, T_K_SHIFT = 25, 26, 27, 28
 # formulas each kernel evaluates (an FMA is 2 flops; a division or a square
 # root is 1): kernel slot -> (FP64 path, mixed path).  Per neighbour pair:
 #   k_neighbour: offsets 2, d^2 3, root 1, grad W factor 6, grad W 2, the
-#     moment sum M 10 (mixed: M in FP32, so 14);
+#     moment sum M 10 (mixed: membership, root and grad W on FP32 pairs from
+#     double-float offsets, grad W stored as a double-float; the FP64 test
+#     only inside a 1e-10 band around the threshold, 0 per pair);
 #   k_assemble: offsets 2, 1/(r^2+lam) 5, L grad W 6, the coefficient 6, the
 #     diagonal 2, rho_ij 4, velocity differences 4, divergence 5, the Jacobi
 #     scaling 1 (mixed: k_assemble_df runs that arithmetic on FP32 pairs; its
-#     FP64 work is the two velocity differences and their splits, the split
-#     of grad W and the widening of the entry, 7);
+#     FP64 work is the two velocity differences and their splits and the
+#     widening of the entry, 5);
 #   k_int_vel: the two harmonic viscosity means and their sum 10, offsets
 #     and r^2 5, 1/(r^2+lam) 2, L grad W 6, the coefficient 6, velocity
 #     differences 2, viscous sums 6, SPS sums 6 (mixed: the offsets and
 #     velocity differences, 4);
-#   k_shift: 16 (mixed: the position-shift sums and the velocity differences,
-#     6; the velocity-gradient sums run in FP32).
+#   k_shift: 16 (mixed: 0; the position-shift sums run as double-floats,
+#     the velocity-gradient sums in FP32).
 # Per solid pair, k_effpor: offsets 2, d^2 3, root 1, W 9, the weighted sum
-# 4 (mixed: the FP64 sum of the FP32 terms, 1).
-FP64_FLOPS = {T_K_NEIGHBOUR: (24, 14), T_K_ASSEMBLE: (35, 7), T_K_INT_VEL: (43, 4), T_K_SHIFT: (16, 6),
-              T_K_EFFPOR: (19, 1)}
+# 4 (mixed: FP32 terms summed as a double-float, 0).
+FP64_FLOPS = {T_K_NEIGHBOUR: (24, 0), T_K_ASSEMBLE: (35, 5), T_K_INT_VEL: (43, 4), T_K_SHIFT: (16, 0),
+              T_K_EFFPOR: (19, 0)}
+# Algorithmic DRAM bytes: (per row, per neighbour entry) for each path, each
+# input read and each output written once (neighbours' particle data counted
+# once per row, as it is reused from cache):
+#   k_neighbour: x, y, offsets, cell, flags (row) and the cell lists' share;
+#     per entry the list index and grad W written (FP64, or the mixed path's
+#     two FP32 halves); L, tr M, flags and the count written per row;
+#   k_assemble: the row's and one neighbour's inputs (~100 B), the
+#     right-hand side; per entry the list index and grad W read, the value
+#     written (and the FP32 and FP16 copies on the mixed path);
+#   k_int_vel: 175 B per row; per entry the list index and grad W (FP32 on
+#     the mixed path);
+#   k_shift: 150 B per row; per entry the list index and grad W (its two
+#     FP32 halves on the mixed path);
+#   k_effpor: 73 B per row (solids: a few MB per launch, not counted).
+HBM_BYTES = {T_K_NEIGHBOUR: ((110, 20), (130, 20)), T_K_ASSEMBLE: ((108, 28), (148, 38)),
+             T_K_INT_VEL: ((175, 20), (175, 12)), T_K_SHIFT: ((150, 20), (150, 20)),
+             T_K_EFFPOR: ((73, 0), (73, 0))}
+# what ncu shows limits a kernel that neither bound reaches
+# (profiles/fp64_pipe_c2_pair_kernels.md, c2 captures)
+KERNEL_LIMITER = {
+    "k_neighbour<float>": "issue and latency: 57 % of issue slots, 35 % warps active (64 registers); FP64 28 %, "
+                          "FMA 27 %, ALU 29 % of their pipes, DRAM 8 %",
+    "k_assemble_df": "issue and latency: 60 % of issue slots, 30 % warps active (80 registers); FP64 44 %, FMA 36 %",
+}
 # the kernel each slot times: (FP64 path, mixed path)
 KERNEL_NAMES = {T_K_NEIGHBOUR: ("k_neighbour<double>", "k_neighbour<float>"),
                 T_K_ASSEMBLE: ("k_assemble<double>", "k_assemble_df"),
@@ -143,11 +169,18 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
             self.proc = None
+            return self
+        # nvidia-smi takes a moment to start: the timed region begins once it
+        # reports (bounded), so that its samples fall inside the region
+        t0 = time.perf_counter()
+        while not self.lines and self.proc.poll() is None and time.perf_counter() - t0 < 10.0:
+            time.sleep(0.01)
+        self.lines.clear()
         return self
 
     def _read(self):
@@ -276,10 +309,11 @@ def solid_pairs(scen) -> int:
     return int(tree.count_neighbors(cKDTree(np.column_stack([scen.x[fl], scen.y[fl]])), 2.0 * h * (1 - 1e-12)))
 
 
-def kernel_rooflines(t, steps: int, nnz: int, spairs: int, prec: str, fp64_peak: float):
-    """Per FP64-bound pair kernel: event-timed ms per launch, launches per
-    step, algorithmic FP64 GFLOP/s and its fraction of the measured FP64
-    peak (FMA rate)."""
+def kernel_rooflines(t, steps: int, nnz: int, spairs: int, n: int, prec: str, fp64_peak: float, hbm_peak: float):
+    """Per pair kernel: event-timed ms per launch, launches per step, its
+    algorithmic FP64 GFLOP/s against the measured FP64 FMA rate and its
+    algorithmic GB/s against the measured HBM copy bandwidth; `bound` is the
+    larger fraction."""
     out = []
     col = 0 if prec == "fp64" else 1
     for slot, name in KERNEL_NAMES.items():
@@ -290,10 +324,16 @@ def kernel_rooflines(t, steps: int, nnz: int, spairs: int, prec: str, fp64_peak:
         pairs = spairs if slot == T_K_EFFPOR else nnz
         flops = FP64_FLOPS[slot][col] * pairs
         gf = flops / (ms * 1e-3) / 1e9
-        out.append({"kernel": name[col], "ms_per_launch": ms,
-                    "launches_per_step": calls / steps, "ms_per_step": t.ms[slot] / steps,
-                    "fp64_flops_per_launch": flops, "pairs_per_launch": pairs, "achieved_gflops": gf,
-                    "peak_gflops": fp64_peak, "frac": gf / fp64_peak if fp64_peak else None})
+        row_b, ent_b = HBM_BYTES[slot][col]
+        byts = row_b * n + ent_b * nnz
+        gbs = byts / (ms * 1e-3) / 1e9
+        f64 = gf / fp64_peak if fp64_peak else 0.0
+        fhbm = gbs / hbm_peak if hbm_peak else 0.0
+        out.append({"kernel": name[col], "ms_per_launch": ms, "launches_per_step": calls / steps,
+                    "ms_per_step": t.ms[slot] / steps, "fp64_flops_per_launch": flops, "pairs_per_launch": pairs,
+                    "achieved_gflops": gf, "peak_gflops": fp64_peak, "frac": f64,
+                    "algorithmic_bytes_per_launch": byts, "achieved_gbs": gbs, "hbm_frac": fhbm,
+                    "bound": "fp64" if f64 >= fhbm else "hbm"})
     return out
 
 
@@ -337,7 +377,8 @@ def run_ours(args, dist: Dist):
                              iters=iters, spmv_ms=spmv_ms, spmv_calls=int(t.calls[T_SPMV]),
                              solve_ms=t.ms[T_PPE_SOLVE] / args.steps, launches=int(t.kernel_launches),
                              clocks=clk.summary(), n=scen.n,
-                             kernels=kernel_rooflines(t, args.steps, nnz, spairs, prec, peaks[0]))
+                             kernels=kernel_rooflines(t, args.steps, nnz, spairs, scen.n, prec, peaks[0],
+                                                      measured_peak_hbm()[0]))
         states[prec] = g.download_state()
         times[prec] = g.get_time()
         # e2e through the C ABI with host buffers in pinned memory: every
@@ -347,22 +388,37 @@ def run_ours(args, dist: Dist):
             up = {k: pinned_like(v.reshape(-1)) for k, v in host.items()}
             out = {k: pinned_like(v) for k, v in host.items()}
             h2d = sum(a.nbytes for a in up.values())
-            g.upload_state(up)
-            g.step(1)
+            # warm-up: an upload gathers the state into cell order, which
+            # swaps the cell-map buffer that the solver's cached CUDA graphs
+            # are keyed by, so successive iterations alternate between two
+            # graph sets; both are built before the timed region
+            for _ in range(max(3, args.warmup)):
+                g.upload_state(up)
+                g.step(1)
+                g.download_state(out)
             g.synchronize()
+            g.reset_timings()
             dist.barrier()
             t0 = time.perf_counter()
-            ke = max(1, min(args.steps, 3))
+            ke = max(1, min(args.steps, 5))
             for _ in range(ke):
                 g.upload_state(up)
                 g.step(1)
                 g.download_state(out)
             e2e_s = time.perf_counter() - t0
+            te = g.timings()
             d2h = sum(np.asarray(a).nbytes for a in out.values())
             ev, _ = aggregate(e2e_s, nf * ke, dist)
+            # where the time goes, per step: device-timed upload (copies,
+            # derived fields, cell build), step and download (gathers to id
+            # order, copies); the rest is host time between the calls
+            up_ms, dn_ms, st_ms = (te.ms[k] / ke for k in (T_UPLOAD, T_DOWNLOAD, T_STEP))
             results[prec]["e2e"] = dict(value=ev, unit="particle-steps/s", h2d_bytes_per_step=int(h2d),
                                         d2h_bytes_per_step=int(d2h), steps=ke,
-                                        host_memory="pinned" if PINNED else "pageable")
+                                        host_memory="pinned" if PINNED else "pageable",
+                                        ms_per_step=e2e_s / ke * 1e3, upload_ms=up_ms, step_ms=st_ms,
+                                        download_ms=dn_ms, h2d_gbs=h2d / (up_ms * 1e-3) / 1e9 if up_ms else None,
+                                        d2h_gbs=d2h / (dn_ms * 1e-3) / 1e9 if dn_ms else None)
         g.close()
     errs = None
     if "fp64" in states:
@@ -958,13 +1014,20 @@ def main():
     # rate), or the SpMV (against the measured HBM copy bandwidth)
     top = max(m["kernels"], key=lambda k: k["ms_per_step"]) if m["kernels"] else None
     if top and top["ms_per_step"] > spmv_roof["ms_per_step"]:
-        roofline = {"bound": "fp64", "kernel": top["kernel"] + " (mixed path)", "achieved": top["achieved_gflops"],
-                    "peak": top["peak_gflops"], "unit": "GFLOP/s", "frac": top["frac"],
-                    "traffic": kernel_traffic(top["kernel"], m["n"]),
-                    "algorithmic_fp64_flops_per_launch": top["fp64_flops_per_launch"],
-                    "avg_launch_ms": top["ms_per_launch"], "launches_per_step": top["launches_per_step"],
-                    "share_of_step": top["ms_per_step"] / m["ms_per_step"],
-                    "peak_source": "FP64 FMA rate measured by bsc_measure_peaks on this GPU (2 flops per FMA)"}
+        common = {"kernel": top["kernel"] + " (mixed path)", "traffic": kernel_traffic(top["kernel"], m["n"]),
+                  "avg_launch_ms": top["ms_per_launch"], "launches_per_step": top["launches_per_step"],
+                  "share_of_step": top["ms_per_step"] / m["ms_per_step"],
+                  "fp64": {"achieved_gflops": top["achieved_gflops"], "peak_gflops": top["peak_gflops"],
+                           "frac": top["frac"], "algorithmic_fp64_flops_per_launch": top["fp64_flops_per_launch"],
+                           "peak_source": "FP64 FMA rate measured by bsc_measure_peaks on this GPU (2 flops per FMA)"},
+                  "limiter": KERNEL_LIMITER.get(top["kernel"])}
+        if top["bound"] == "fp64":
+            roofline = {"bound": "fp64", "achieved": top["achieved_gflops"], "peak": top["peak_gflops"],
+                        "unit": "GFLOP/s", "frac": top["frac"], **common}
+        else:
+            roofline = {"bound": "hbm", "achieved": top["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                        "frac": top["hbm_frac"], "algorithmic_bytes_per_launch": top["algorithmic_bytes_per_launch"],
+                        "peak_source": f"{peak_kind} MEASURED_PEAKS.json hbm_gbs", **common}
     else:
         roofline = spmv_roof
     fp64 = None
