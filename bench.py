@@ -67,13 +67,13 @@ T_K_NEIGHBOUR, T_K_ASSEMBLE, T_K_INT_VEL, T_K_EFFPOR, T_K_SHIFT = 25, 26, 27, 28
 #     widening of the entry, 5);
 #   k_int_vel: the two harmonic viscosity means and their sum 10, offsets
 #     and r^2 5, 1/(r^2+lam) 2, L grad W 6, the coefficient 6, velocity
-#     differences 2, viscous sums 6, SPS sums 6 (mixed: the offsets and
-#     velocity differences, 4);
+#     differences 2, viscous sums 6, SPS sums 6 (mixed: 0; offsets from the
+#     FP32 cell offsets, velocity differences from FP32 roundings);
 #   k_shift: 16 (mixed: 0; the position-shift sums run as double-floats,
 #     the velocity-gradient sums in FP32).
 # Per solid pair, k_effpor: offsets 2, d^2 3, root 1, W 9, the weighted sum
 # 4 (mixed: FP32 terms summed as a double-float, 0).
-FP64_FLOPS = {T_K_NEIGHBOUR: (24, 0), T_K_ASSEMBLE: (35, 5), T_K_INT_VEL: (43, 4), T_K_SHIFT: (16, 0),
+FP64_FLOPS = {T_K_NEIGHBOUR: (24, 0), T_K_ASSEMBLE: (35, 5), T_K_INT_VEL: (43, 0), T_K_SHIFT: (16, 0),
               T_K_EFFPOR: (19, 0)}
 # Algorithmic DRAM bytes: (per row, per neighbour entry) for each path, each
 # input read and each output written once (neighbours' particle data counted
@@ -250,6 +250,31 @@ def spmv_mg_bytes(nnz: int, n: int, fp32: bool) -> int:
 PINNED = False
 
 
+def link_bandwidth(nbytes: int, reps: int = 3):
+    """GB/s of one pinned host->device and one device->host copy of `nbytes`
+    (torch copies timed with CUDA events): the host link the e2e copies run
+    over, measured on this machine for comparison."""
+    try:
+        import torch
+
+        h = torch.empty(nbytes, dtype=torch.uint8, pin_memory=True)
+        d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        out = {}
+        for name, dst, src in (("h2d_gbs", d, h), ("d2h_gbs", h, d)):
+            dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(reps):
+                dst.copy_(src, non_blocking=True)
+            e1.record()
+            torch.cuda.synchronize()
+            out[name] = reps * nbytes / (e0.elapsed_time(e1) * 1e-3) / 1e9
+        return out
+    except Exception as ex:  # no CUDA-capable torch
+        return {"unavailable": repr(ex)[:80]}
+
+
 def pinned_like(a: np.ndarray) -> np.ndarray:
     """A copy of `a` in page-locked host memory (torch's pinned allocator),
     so host<->device copies run at the interconnect's DMA rate."""
@@ -382,29 +407,36 @@ def run_ours(args, dist: Dist):
         states[prec] = g.download_state()
         times[prec] = g.get_time()
         # e2e through the C ABI with host buffers in pinned memory: every
-        # step uploads the state, steps, and downloads the state
+        # iteration uploads the state and its time (t, dt), steps, and
+        # downloads the state: the same step from the same inputs each time
+        # (the time is an input too: without it each repeat would drive the
+        # piston one step further from the uploaded particles)
         if prec == "mixed":
             host = g.download_state()
+            t_in, dt_in = g.get_time()
             up = {k: pinned_like(v.reshape(-1)) for k, v in host.items()}
             out = {k: pinned_like(v) for k, v in host.items()}
             h2d = sum(a.nbytes for a in up.values())
+
+            def e2e_iteration():
+                g.upload_state(up)
+                g.set_time(t_in, dt_in)
+                info = g.step(1)
+                g.download_state(out)
+                return info.iterations
+
             # warm-up: an upload gathers the state into cell order, which
             # swaps the cell-map buffer that the solver's cached CUDA graphs
             # are keyed by, so successive iterations alternate between two
             # graph sets; both are built before the timed region
             for _ in range(max(3, args.warmup)):
-                g.upload_state(up)
-                g.step(1)
-                g.download_state(out)
+                e2e_iteration()
             g.synchronize()
             g.reset_timings()
             dist.barrier()
             t0 = time.perf_counter()
             ke = max(1, min(args.steps, 5))
-            for _ in range(ke):
-                g.upload_state(up)
-                g.step(1)
-                g.download_state(out)
+            e2e_its = [e2e_iteration() for _ in range(ke)]
             e2e_s = time.perf_counter() - t0
             te = g.timings()
             d2h = sum(np.asarray(a).nbytes for a in out.values())
@@ -413,12 +445,24 @@ def run_ours(args, dist: Dist):
             # derived fields, cell build), step and download (gathers to id
             # order, copies); the rest is host time between the calls
             up_ms, dn_ms, st_ms = (te.ms[k] / ke for k in (T_UPLOAD, T_DOWNLOAD, T_STEP))
+            # after the measurement: the same iteration three more times, each
+            # read back on its own (device ms of upload, step, download), and
+            # the link's own copy rate for the same byte count
+            per_it = []
+            for _ in range(3):
+                g.reset_timings()
+                e2e_iteration()
+                tt = g.timings()
+                per_it.append([round(tt.ms[k], 3) for k in (T_UPLOAD, T_STEP, T_DOWNLOAD)])
+            link = link_bandwidth(int(h2d))
             results[prec]["e2e"] = dict(value=ev, unit="particle-steps/s", h2d_bytes_per_step=int(h2d),
                                         d2h_bytes_per_step=int(d2h), steps=ke,
                                         host_memory="pinned" if PINNED else "pageable",
                                         ms_per_step=e2e_s / ke * 1e3, upload_ms=up_ms, step_ms=st_ms,
                                         download_ms=dn_ms, h2d_gbs=h2d / (up_ms * 1e-3) / 1e9 if up_ms else None,
-                                        d2h_gbs=d2h / (dn_ms * 1e-3) / 1e9 if dn_ms else None)
+                                        d2h_gbs=d2h / (dn_ms * 1e-3) / 1e9 if dn_ms else None,
+                                        after_iterations_ms_upload_step_download=per_it, link=link,
+                                        ppe_iterations=e2e_its)
         g.close()
     errs = None
     if "fp64" in states:
