@@ -293,6 +293,47 @@ __global__ void __launch_bounds__(MG_BLOCK) k_mg_smooth(int nx, int ny, const T*
     if (!mg_skip(sk)) xout[c] = v;
 }
 
+// Both post-sweeps of a cell level in one launch: a block owns a tile of
+// PT_X x PT_Y cells (PT_Y along the grid's contiguous y index) and computes
+// the first sweep (prolonged correction folded in, weight w) on the tile and
+// its one-cell ring into shared memory, then the second sweep (weight w1) on
+// the tile from there.  The ring's first sweep is recomputed by the
+// neighbouring blocks (a third more first-sweep work) and one launch of the
+// latency-bound chain is saved per level.
+constexpr int PT_X = 8, PT_Y = 32;
+constexpr int PT_HX = PT_X + 2, PT_HY = PT_Y + 2;
+template <typename T>
+__global__ void __launch_bounds__(PT_X * PT_Y) k_mg_post2(int nx, int ny, const T* __restrict__ A,
+                                                           const T* __restrict__ dinv, const T* __restrict__ b,
+                                                           const T* __restrict__ xin, const T* __restrict__ xc,
+                                                           int nyc, T scale, T w, T w1, T* __restrict__ xout,
+                                                           const Scalars* __restrict__ sk) {
+    __shared__ T y1[PT_HX * PT_HY];
+    const int nc = nx * ny;
+    const int x0 = blockIdx.x * PT_X - 1, y0 = blockIdx.y * PT_Y - 1;  // ring origin
+    for (int h = threadIdx.x; h < PT_HX * PT_HY; h += blockDim.x) {
+        const int gx = x0 + h / PT_HY, gy = y0 + h % PT_HY;
+        T v = 0;
+        if (gx >= 0 && gx < nx && gy >= 0 && gy < ny)
+            v = smooth_at<T, 2>(nx, ny, gx * ny + gy, A, dinv, b, xin, xc, nyc, scale, w);
+        y1[h] = v;
+    }
+    __syncthreads();
+    const int tx = threadIdx.x / PT_Y, ty = threadIdx.x % PT_Y;
+    const int cx = x0 + 1 + tx, cy = y0 + 1 + ty;
+    if (cx >= nx || cy >= ny) return;
+    const int c = cx * ny + cy;
+    T ax = 0;
+#pragma unroll
+    for (int q = 0; q < 9; ++q) {
+        const int gx = cx + q / 3 - 1, gy = cy + q % 3 - 1;
+        if (gx < 0 || gx >= nx || gy < 0 || gy >= ny) continue;
+        ax += A[q * nc + c] * y1[(tx + q / 3) * PT_HY + (ty + q % 3)];
+    }
+    const T v = y1[(tx + 1) * PT_HY + (ty + 1)] + w1 * dinv[c] * (b[c] - ax);
+    if (!mg_skip(sk)) xout[c] = v;
+}
+
 // one sweep from a zero guess: x = w D^-1 b
 template <typename T>
 __global__ void k_mg_jacobi0(int64_t nc, const T* __restrict__ dinv, const T* __restrict__ b, T w, T* __restrict__ x,
@@ -740,6 +781,13 @@ int cycle_level(Ctx* c, int l) {
     if (int rc = cycle_level<T>(c, l + 1)) return rc;
     // post-smoothing: the prolongation folded into the first sweep; the last
     // sweep writes x_l
+    if (nup == 2 && c->mg_post_fused) {  // both sweeps in one launch
+        const dim3 gt((unsigned)((L.nx + PT_X - 1) / PT_X), (unsigned)((L.ny + PT_Y - 1) / PT_Y));
+        k_mg_post2<T><<<gt, PT_X * PT_Y, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, wp, w1,
+                                                          v.x, c->mg.skip);
+        BSC_LAUNCH(c);
+        return BSC_OK;
+    }
     for (int k = 0; k < nup; ++k) {
         T* out = (k == nup - 1) ? v.x : (cur == v.y ? v.t : v.y);
         if (k == 0)

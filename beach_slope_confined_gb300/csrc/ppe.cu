@@ -1343,6 +1343,11 @@ int run_fgmres_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
                 k_spmv_z<double><<<blocks_for(n, B), B, 0, c->stream>>>(n, A, zj, w, c->sc2);
                 if (c->timing) record_event(c, c->ev_spmv[3 + 2 * (j & 1)]);
                 if (c->prof_iter) record_event(c, c->ev_it[4]);
+                // separate single-block kernels for the column of H and the
+                // Givens step: in FP64 the fused last-block forms (as on the
+                // mixed path) measured slower, 122 against 107 us per
+                // iteration at 846k rows (their last block has a quarter of
+                // k_fg_hcol's warps)
                 k_fg_mdot<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc2);
                 k_fg_hcol<<<1, 1024, 0, c->stream>>>(c->part, c->Hd, F, j, 0, c->sc2);
                 k_fg_maxpy<double><<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, 1, c->part, c->sc2);
@@ -1415,19 +1420,20 @@ __global__ void __launch_bounds__(RED_BLOCK) k_spmv_f(int64_t n, EllPackF A, con
     GRID_LOOP(i, n) w[i] = A.template row<float, float>(i, z);
 }
 
-// h_i = V_i . w for i <= j, 8 columns per pass; the block that finishes last
-// (ticket taken after a fence) sums the partials into column j of H, one
-// warp per dot in lane order as k_fg_hcol does
-__global__ void __launch_bounds__(RED_BLOCK) k_fgf_mdot(int64_t n, const float* __restrict__ V,
-                                                         const float* __restrict__ w, int j,
+// h_i = V_i . w for i <= j, 8 columns per pass, summed per thread in T; the
+// block that finishes last (ticket taken after a fence) sums the partials
+// into column j of H, one warp per dot in lane order as k_fg_hcol does
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_fgf_mdot(int64_t n, const T* __restrict__ V,
+                                                         const T* __restrict__ w, int j,
                                                          double* __restrict__ part, const Scalars* __restrict__ sc,
                                                          unsigned* __restrict__ ticket, double* Hd, FgLayout F) {
     if (fg_skip(sc)) return;
     for (int i0 = 0; i0 <= j; i0 += 8) {
-        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        T acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
         const int cntv = min(8, j + 1 - i0);
         GRID_LOOP(k, n) {
-            const float wk = w[k];
+            const T wk = w[k];
 #pragma unroll
             for (int q = 0; q < 8; ++q)
                 if (q < cntv) acc[q] += V[(int64_t)(i0 + q) * n + k] * wk;
@@ -1459,25 +1465,26 @@ __global__ void __launch_bounds__(RED_BLOCK) k_fgf_mdot(int64_t n, const float* 
 // w -= sum_i h_i V_i and the partials of w.w; the block that finishes last
 // runs the Givens step of k_fg_givens (h(j+1,j) = ||w||, rotations,
 // residual estimate) and copies the scalars to the host mirror
-__global__ void __launch_bounds__(RED_BLOCK) k_fgf_maxpy_givens(int64_t n, const float* __restrict__ V,
-                                                                 float* __restrict__ w, int j, double* Hd, FgLayout F,
+template <typename T>
+__global__ void __launch_bounds__(RED_BLOCK) k_fgf_maxpy_givens(int64_t n, const T* __restrict__ V,
+                                                                 T* __restrict__ w, int j, double* Hd, FgLayout F,
                                                                  double* __restrict__ part, Scalars* sc,
                                                                  unsigned* __restrict__ ticket, Scalars* mirror) {
     if (fg_skip(sc)) {  // the cycle has stopped: publish the scalars as k_fg_givens does
         if (mirror && blockIdx.x == 0 && threadIdx.x == 0) *mirror = *sc;
         return;
     }
-    __shared__ float h[FG_MAXM];
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) h[i] = (float)Hd[F.hc(i)];
+    __shared__ T h[FG_MAXM];
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) h[i] = (T)Hd[F.hc(i)];
     __syncthreads();
-    float acc = 0.f;
+    T acc = 0;
     GRID_LOOP(k, n) {
-        float s = w[k];
+        T s = w[k];
         for (int i = 0; i <= j; ++i) s -= h[i] * V[(int64_t)i * n + k];
         w[k] = s;
         acc += s * s;
     }
-    float a[1] = {acc};
+    T a[1] = {acc};
     block_partials<1>(a, part);
     __shared__ bool last;
     __syncthreads();
@@ -1578,8 +1585,9 @@ int run_fgmres_ir_mg(Ctx* c, int64_t n, bsc_solve_info* si) {
                 if (c->prof_iter) record_event(c, c->ev_it[4]);
                 // the column of H and the Givens step finish in the last
                 // block of the dot and update kernels (no single-block launches)
-                k_fgf_mdot<<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc, c->ticket, c->Hd, F);
-                k_fgf_maxpy_givens<<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, c->part, c->sc, c->ticket, mirror);
+                k_fgf_mdot<float><<<G, B, 0, c->stream>>>(n, V, w, j, c->part, c->sc, c->ticket, c->Hd, F);
+                k_fgf_maxpy_givens<float><<<G, B, 0, c->stream>>>(n, V, w, j, c->Hd, F, c->part, c->sc, c->ticket,
+                                                                  mirror);
                 k_fgf_next<<<G, B, 0, c->stream>>>(n, w, V, j, c->sc);
                 if (c->prof_iter) record_event(c, c->ev_it[5]);
                 c->launches += 4;

@@ -95,8 +95,9 @@ HBM_BYTES = {T_K_NEIGHBOUR: ((110, 20), (130, 20)), T_K_ASSEMBLE: ((108, 28), (1
 # what ncu shows limits a kernel that neither bound reaches
 # (profiles/fp64_pipe_c2_pair_kernels.md, c2 captures)
 KERNEL_LIMITER = {
-    "k_neighbour<float>": "issue and latency: 57 % of issue slots, 35 % warps active (64 registers); FP64 28 %, "
-                          "FMA 27 %, ALU 29 % of their pipes, DRAM 8 %",
+    "k_neighbour<float>": "issue and latency of the double-float chains: 35 % warps active (64 registers), 10 cycles "
+                          "between a warp's instructions; FP64 17 %, FMA 28.5 %, ALU 25 % of their pipes",
+    "k_int_vel<float>": "latency of its per-neighbour gathers (long scoreboard 12.7 per issue), 34 % warps active",
     "k_assemble_df": "issue and latency: 60 % of issue slots, 30 % warps active (80 registers); FP64 44 %, FMA 36 %",
 }
 # the kernel each slot times: (FP64 path, mixed path)
