@@ -447,17 +447,6 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
     c->mg_w[0] = c->P.mg_omega;
     c->mg_w[1] = c->P.mg_sweeps == 2 ? c->P.mg_omega * ((2.0 + M_SQRT1_2) / (2.0 - M_SQRT1_2)) : c->P.mg_omega;
     if (const char* e = std::getenv("BSC_MG_W")) std::sscanf(e, "%lf,%lf", &c->mg_w[0], &c->mg_w[1]);
-    // with two sweeps per level, the particle level of the V-cycle takes one
-    // post-sweep on the mixed path and one pre-sweep on the FP64 path
-    // (measured on the 846k-row c3 tank: 8.07 -> 7.92 and 16.17 -> 15.33 ms
-    // per step at the same iteration counts; both cuts together cost 20 %
-    // more iterations on either path)
-    if (c->P.mg_sweeps == 2) {
-        if (c->mixed)
-            c->mg_post[1] = 1;
-        else
-            c->mg_pre_fine = 1;
-    }
     if (const char* e = std::getenv("BSC_MG_POST")) {
         std::sscanf(e, "%d,%d,%lf", &c->mg_post[0], &c->mg_post[1], &c->mg_wpost);
         for (int k = 0; k < 2; ++k) c->mg_post[k] = std::max(0, std::min(c->mg_post[k], 8));
