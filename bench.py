@@ -92,8 +92,8 @@ FP64_FLOPS = {T_K_NEIGHBOUR: (24, 0), T_K_ASSEMBLE: (35, 5), T_K_INT_VEL: (43, 0
 HBM_BYTES = {T_K_NEIGHBOUR: ((110, 20), (130, 20)), T_K_ASSEMBLE: ((108, 28), (148, 38)),
              T_K_INT_VEL: ((175, 20), (175, 12)), T_K_SHIFT: ((150, 20), (150, 20)),
              T_K_EFFPOR: ((73, 0), (73, 0))}
-# what ncu shows limits a kernel that neither bound reaches
-# (profiles/fp64_pipe_c2_pair_kernels.md, c2 captures)
+# what ncu shows limits a kernel that neither bound reaches (full captures of
+# one launch each on the c2 tank)
 KERNEL_LIMITER = {
     "k_neighbour<float>": "issue and latency of the double-float chains: 35 % warps active (64 registers), 10 cycles "
                           "between a warp's instructions; FP64 17 %, FMA 28.5 %, ALU 25 % of their pipes",
