@@ -638,6 +638,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_eddyvis(int64_t n, State S, KParam
     [[maybe_unused]] const float4 udi = sizeof(R) == 4 ? udf[i] : float4{};
     R t1 = 0, t2 = 0, t3 = 0;
     const int m = cnt[i];
+    // FP32 sums: four entries' gathers in flight (measured 3-7 % faster)
+    #pragma unroll(sizeof(R) == 4 ? 4 : 1)
     for (int k = 0; k < m; ++k) {
         const int64_t e = ell(i, k, K.kmax);
         const int j = nbr[e];
@@ -773,6 +775,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_int_vel(int64_t n, State S, KParam
         const R eps6 = (R)(double)1e-6f;
         R ax = 0, ay = 0, kx = 0, ky = 0;  // kx, ky: the SPS sum, scaled by (2/3) n_i once
         const int m = cnt[i];
+        // FP32 sums: four entries' gathers in flight (measured 3-7 % faster)
+        #pragma unroll(sizeof(R) == 4 ? 4 : 1)
         for (int k = 0; k < m; ++k) {
             const int64_t e = ell(i, k, K.kmax);
             const int j = nbr[e];
@@ -1078,6 +1082,8 @@ __global__ void __launch_bounds__(NB_BLOCK) k_shift(int64_t n, State S, KParams 
     [[maybe_unused]] df2 sxd{0.f, 0.f}, syd{0.f, 0.f};
     [[maybe_unused]] const float vxif = f32_of(vxi), vyif = f32_of(vyi);
     R ax = 0, bx = 0, ay = 0, by = 0;
+    // FP32 sums: four entries' gathers in flight (measured 3-7 % faster)
+    #pragma unroll(sizeof(R) == 4 ? 4 : 1)
     for (int k = 0; k < m; ++k) {
         const int64_t e = ell(i, k, K.kmax);
         const int j = nbr[e];
