@@ -98,7 +98,8 @@ KERNEL_LIMITER = {
     "k_neighbour<float>": "issue and latency of the double-float chains: 35 % warps active (64 registers), 10 cycles "
                           "between a warp's instructions; FP64 17 %, FMA 28.5 %, ALU 25 % of their pipes",
     "k_int_vel<float>": "latency of its per-neighbour gathers (long scoreboard 12.7 per issue), 34 % warps active",
-    "k_assemble_df": "issue and latency: 60 % of issue slots, 30 % warps active (80 registers); FP64 44 %, FMA 36 %",
+    "k_assemble_df": "issue and latency: 58 % of issue slots, 29 % warps active (80 registers); FP64 35.5 %, "
+                     "FMA 36.5 %, ALU 26 % of their pipes",
 }
 # the kernel each slot times: (FP64 path, mixed path)
 KERNEL_NAMES = {T_K_NEIGHBOUR: ("k_neighbour<double>", "k_neighbour<float>"),
