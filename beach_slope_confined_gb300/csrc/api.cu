@@ -453,6 +453,7 @@ int bsc_create(const bsc_params* p, bsc_ctx** out) {
     }
     if (const char* e = std::getenv("BSC_MG_PRE")) c->mg_pre_fine = std::max(0, std::min(std::atoi(e), 8));
     if (const char* e = std::getenv("BSC_MG_POST_FUSED")) c->mg_post_fused = e[0] != '0';
+    if (const char* e = std::getenv("BSC_MG_CELL_SWEEPS")) c->mg_cell4 = std::atoi(e) == 4;
     if (const char* e = std::getenv("BSC_EXACT_DIV")) c->exact_div = e[0] == '1';
     if (const char* e = std::getenv("BSC_ASSEMBLY")) c->asm_rcp = std::string(e) == "rcp";
     if (const char* e = std::getenv("BSC_NEIGHBOUR")) c->nb_warpcell = std::string(e) == "warpcell";

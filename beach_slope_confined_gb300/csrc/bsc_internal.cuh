@@ -347,6 +347,7 @@ struct Ctx {
     int mg_pre_fine = 0;
     double mg_wpost = 0.0;
     bool mg_post_fused = true;  // a cell level's two post-sweeps in one launch (BSC_MG_POST_FUSED=0: two)
+    bool mg_cell4 = false;      // BSC_MG_CELL_SWEEPS=4: four sweeps each way on the per-level cell levels
     bool exact_div = false;       // BSC_EXACT_DIV=1: IEEE divisions in the mixed path's FP64 assembly
     cudaEvent_t ev_it[6] = {};
     double* V = nullptr;          // FGMRES basis (m+1) x cap, FP64

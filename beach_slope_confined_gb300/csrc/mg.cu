@@ -334,6 +334,134 @@ __global__ void __launch_bounds__(PT_X * PT_Y) k_mg_post2(int nx, int ny, const 
     if (!mg_skip(sk)) xout[c] = v;
 }
 
+// Four sweeps per cell level (BSC_MG_CELL_SWEEPS=4), each direction in one
+// launch on the same PT_X x PT_Y tiles: a stage on ring r (the tile and r
+// cells around it) is one damped-Jacobi sweep whose neighbours' values come
+// from the previous stage on ring r + 1, in shared memory.  The weights
+// alternate w, w1, w, w1 as the two-sweep pair does.
+// out on ring r from prev on ring r + 1 (both tile-relative arrays)
+template <typename T>
+__device__ __forceinline__ void pt_sweep(int nx, int ny, const T* __restrict__ A, const T* __restrict__ dinv,
+                                         const T* __restrict__ b, int x0, int y0, int r, const T* prev, T* out,
+                                         T wgt) {
+    const int nc = nx * ny;
+    const int HY = PT_Y + 2 * r, HN = (PT_X + 2 * r) * HY, PY = PT_Y + 2 * (r + 1);
+    for (int h = threadIdx.x; h < HN; h += blockDim.x) {
+        const int gx = x0 - r + h / HY, gy = y0 - r + h % HY;
+        T v = 0;
+        if (gx >= 0 && gx < nx && gy >= 0 && gy < ny) {
+            const int c = gx * ny + gy;
+            const int px = h / HY + 1, py = h % HY + 1;  // (gx, gy) in prev's ring r + 1
+            T ax = 0;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                const int hx = gx + q / 3 - 1, hy = gy + q % 3 - 1;
+                if (hx < 0 || hx >= nx || hy < 0 || hy >= ny) continue;
+                ax += A[q * nc + c] * prev[(px + q / 3 - 1) * PY + (py + q % 3 - 1)];
+            }
+            v = prev[px * PY + py] + wgt * dinv[c] * (b[c] - ax);
+        }
+        out[h] = v;
+    }
+}
+
+constexpr int PT_R3 = (PT_X + 6) * (PT_Y + 6), PT_R2 = (PT_X + 4) * (PT_Y + 4), PT_R1 = (PT_X + 2) * (PT_Y + 2),
+              PT_R0 = PT_X * PT_Y;
+
+// pre-smoothing from zero (x1 = w D^-1 b folded into x2 on ring 3, then x3
+// on ring 2, x4 on ring 1), x4 on the tile into xout, the residual
+// b - A x4 on the tile, and its sums over each coarse cell's 2x2 children
+// (the tile holds whole coarse cells: its origin is even) into bc
+template <typename T>
+__global__ void __launch_bounds__(PT_X * PT_Y) k_mg_pre4_restrict(int nx, int ny, const T* __restrict__ A,
+                                                                   const T* __restrict__ dinv,
+                                                                   const T* __restrict__ b, T w, T w1,
+                                                                   T* __restrict__ xout, int nxc, int nyc,
+                                                                   T* __restrict__ bc,
+                                                                   const Scalars* __restrict__ sk) {
+    __shared__ T s3[PT_R3], s2[PT_R2], s1[PT_R1], s0[PT_R0];
+    const int x0 = blockIdx.x * PT_X, y0 = blockIdx.y * PT_Y;
+    {   // x2 on ring 3, from b alone (the first sweep from zero is pointwise)
+        const int HY = PT_Y + 6;
+        for (int h = threadIdx.x; h < PT_R3; h += blockDim.x) {
+            const int gx = x0 - 3 + h / HY, gy = y0 - 3 + h % HY;
+            T v = 0;
+            if (gx >= 0 && gx < nx && gy >= 0 && gy < ny)
+                v = smooth_at<T, 1>(nx, ny, gx * ny + gy, A, dinv, b, nullptr, nullptr, 0, (T)0, w1, w);
+            s3[h] = v;
+        }
+    }
+    __syncthreads();
+    pt_sweep<T>(nx, ny, A, dinv, b, x0, y0, 2, s3, s2, w);
+    __syncthreads();
+    pt_sweep<T>(nx, ny, A, dinv, b, x0, y0, 1, s2, s1, w1);
+    __syncthreads();
+    // the tile: x4 out, and the residual b - A x4 into s0
+    const int nc = nx * ny;
+    {
+        const int tx = threadIdx.x / PT_Y, ty = threadIdx.x % PT_Y;
+        const int cx = x0 + tx, cy = y0 + ty;
+        T rv = 0;
+        if (cx < nx && cy < ny) {
+            const int c = cx * ny + cy;
+            T ax = 0;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) {
+                const int hx = cx + q / 3 - 1, hy = cy + q % 3 - 1;
+                if (hx < 0 || hx >= nx || hy < 0 || hy >= ny) continue;
+                ax += A[q * nc + c] * s1[(tx + q / 3) * (PT_Y + 2) + (ty + q % 3)];
+            }
+            rv = b[c] - ax;
+            if (!mg_skip(sk)) xout[c] = s1[(tx + 1) * (PT_Y + 2) + (ty + 1)];
+        }
+        s0[threadIdx.x] = rv;
+    }
+    __syncthreads();
+    // the tile's PT_X/2 x PT_Y/2 coarse cells
+    if (threadIdx.x < (PT_X / 2) * (PT_Y / 2)) {
+        const int a = threadIdx.x / (PT_Y / 2), q = threadIdx.x % (PT_Y / 2);
+        const int X = x0 / 2 + a, Y = y0 / 2 + q;
+        if (X < nxc && Y < nyc) {
+            T sum = 0;
+            for (int i = 0; i < 2; ++i)
+                for (int j = 0; j < 2; ++j)
+                    if (2 * X + i < nx && 2 * Y + j < ny) sum += s0[(2 * a + i) * PT_Y + (2 * q + j)];
+            if (!mg_skip(sk)) bc[X * nyc + Y] = sum;
+        }
+    }
+}
+
+// post-smoothing: y1 on ring 3 (the prolonged correction folded in, as
+// k_mg_post2's first sweep), y2 on ring 2, y3 on ring 1, y4 on the tile
+template <typename T>
+__global__ void __launch_bounds__(PT_X * PT_Y) k_mg_post4(int nx, int ny, const T* __restrict__ A,
+                                                           const T* __restrict__ dinv, const T* __restrict__ b,
+                                                           const T* __restrict__ xin, const T* __restrict__ xc,
+                                                           int nyc, T scale, T w, T w1, T* __restrict__ xout,
+                                                           const Scalars* __restrict__ sk) {
+    __shared__ T s3[PT_R3], s2[PT_R2], s1[PT_R1], s0[PT_R0];
+    const int x0 = blockIdx.x * PT_X, y0 = blockIdx.y * PT_Y;
+    {
+        const int HY = PT_Y + 6;
+        for (int h = threadIdx.x; h < PT_R3; h += blockDim.x) {
+            const int gx = x0 - 3 + h / HY, gy = y0 - 3 + h % HY;
+            T v = 0;
+            if (gx >= 0 && gx < nx && gy >= 0 && gy < ny)
+                v = smooth_at<T, 2>(nx, ny, gx * ny + gy, A, dinv, b, xin, xc, nyc, scale, w);
+            s3[h] = v;
+        }
+    }
+    __syncthreads();
+    pt_sweep<T>(nx, ny, A, dinv, b, x0, y0, 2, s3, s2, w1);
+    __syncthreads();
+    pt_sweep<T>(nx, ny, A, dinv, b, x0, y0, 1, s2, s1, w);
+    __syncthreads();
+    pt_sweep<T>(nx, ny, A, dinv, b, x0, y0, 0, s1, s0, w1);
+    const int tx = threadIdx.x / PT_Y, ty = threadIdx.x % PT_Y;
+    const int cx = x0 + tx, cy = y0 + ty;
+    if (cx < nx && cy < ny && !mg_skip(sk)) xout[cx * ny + cy] = s0[threadIdx.x];
+}
+
 // one sweep from a zero guess: x = w D^-1 b
 template <typename T>
 __global__ void k_mg_jacobi0(int64_t nc, const T* __restrict__ dinv, const T* __restrict__ b, T w, T* __restrict__ x,
@@ -756,6 +884,17 @@ int cycle_level(Ctx* c, int l) {
     T* cur = v.y;
     const MgLevel& Lc = mg.L[l + 1];
     Lv<T> vc = level_view<T>(Lc);
+    if (c->mg_cell4 && nu == 2) {  // four sweeps each way, one launch each
+        const dim3 gt((unsigned)((L.nx + PT_X - 1) / PT_X), (unsigned)((L.ny + PT_Y - 1) / PT_Y));
+        k_mg_pre4_restrict<T><<<gt, PT_X * PT_Y, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, w, w1, cur, Lc.nx,
+                                                                  Lc.ny, vc.b, c->mg.skip);
+        BSC_LAUNCH(c);
+        if (int rc = cycle_level<T>(c, l + 1)) return rc;
+        k_mg_post4<T><<<gt, PT_X * PT_Y, 0, c->stream>>>(L.nx, L.ny, v.A, v.dinv, v.b, cur, vc.x, Lc.ny, sc, w, w1,
+                                                          v.x, c->mg.skip);
+        BSC_LAUNCH(c);
+        return BSC_OK;
+    }
     if (nu == 2 && L.R) {
         // both sweeps and the restriction in one launch
         k_mg_pre_restrict<T><<<g + blocks_for(Lc.nc, MG_BLOCK), MG_BLOCK, 0, c->stream>>>(
@@ -1012,7 +1151,7 @@ int mg_setup(Ctx* c) {
         k_mg_dense_inverse<double><<<1, 1024, smem, c->stream>>>(Lc.nx, Lc.ny, Lc.A, mg.cinv);
     BSC_LAUNCH(c);
     // the restriction operators of the levels swept by per-level kernels
-    if (c->P.mg_sweeps == 2)
+    if (c->P.mg_sweeps == 2 && !c->mg_cell4)
         for (int l = 1; l < mg.tail_l0; ++l) {
             const MgLevel &F = mg.L[l], &C = mg.L[l + 1];
             const unsigned gb = blocks_for(C.nc, 128);

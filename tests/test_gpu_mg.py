@@ -107,8 +107,10 @@ def test_mg_reorder_keeps_results():
             assert rel_l2(out[0][f], out[1][f]) < tol, (prec, f)
 
 
-@pytest.mark.parametrize("env", [{"BSC_MG_POST_FUSED": "0"}, {"BSC_MG_POST": "2,1"}, {"BSC_MG_PRE": "1"}],
-                         ids=["post-sweeps-unfused", "one-particle-post-sweep", "one-particle-pre-sweep"])
+@pytest.mark.parametrize("env", [{"BSC_MG_POST_FUSED": "0"}, {"BSC_MG_POST": "2,1"}, {"BSC_MG_PRE": "1"},
+                                 {"BSC_MG_CELL_SWEEPS": "4"}],
+                         ids=["post-sweeps-unfused", "one-particle-post-sweep", "one-particle-pre-sweep",
+                              "four-cell-level-sweeps"])
 @pytest.mark.parametrize("prec", ["fp64", "mixed"])
 def test_mg_sweep_variants_reach_the_same_solution(env, prec, monkeypatch):
     """The V-cycle's sweep variants only change how the solve gets there:
